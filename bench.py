@@ -1,0 +1,327 @@
+"""Benchmark: input GB/s of project + encode on one GB300.
+
+One step = one field through the whole path: reset of the edit
+accumulators, the alternating projections (iterated to the reference's
+termination rule), compaction + uint16 quantisation + flag packs, and the
+four-stream Huffman encode with ZSTD (level 20, as projection_example.cu
+uses), ending with the compressed bytes in host memory.
+
+  value : x and x' resident in HBM when the timed region starts
+          (ffcz_solve_all_abs_pair_device + ffcz_solver_encode);
+  e2e   : the reference-facing C ABI with host buffers -- initialize_all_abs
+          (H2D of x) + solve_all_abs (H2D of e0 = x' - x) + encode, so the
+          host->device copies are inside the timed region.
+Input bytes per step = N * sizeof(T) of the original field.
+
+--impl reference times the CPU restatement of the same path (FP64 pocketfft
+loop with scipy workers = all host cores, C compaction/quantiser/Huffman,
+libzstd) on the same workload.
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                       [--workload plain256] [--zstd-mode single|chunked]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "Input GB/s (project+encode) on 1 GB300, mixed-prec vs plain FP32, bounds met"
+PEAKS = ROOT / "MEASURED_PEAKS.json"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="plain256")
+    ap.add_argument("--zstd-level", type=int, default=20)
+    ap.add_argument("--zstd-mode", default="single", choices=["single", "chunked"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_init(n):
+    rank, world = int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+        dist.init_process_group("nccl")
+    return rank, world
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(v, world):
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        dev = os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0] or "0"
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={dev}", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                       "-lms", "100"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        self.p.wait()
+        self.f.seek(0)
+        rows = [r.split(",") for r in self.f.read().strip().splitlines() if r.count(",") >= 8]
+        os.unlink(self.f.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows]
+        mx = max(float(r[2]) for r in rows)
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].strip().lower() == "active"})
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": reasons, "samples": len(rows)}
+
+
+def load_workload(name):
+    from ffcz_gb300 import synth
+
+    fld, max_iter = synth.workload(name)
+    return fld, max_iter
+
+
+def peak_hbm():
+    try:
+        p = json.loads(PEAKS.read_text())
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+# --------------------------------------------------------------------------- CPU leg
+def cpu_step(fld, max_iter, level):
+    """One project+encode pass of the oracle restatement; returns seconds."""
+    from oracle import ffcz_oracle as O
+
+    t0 = time.perf_counter()
+    e0 = fld.xp.astype(np.float64) - fld.x.astype(np.float64)
+    r = O.solve_all_abs(e0.astype(fld.x.dtype), fld.shape, fld.eps, fld.delta, max_iter, 1e-7, np.float64)
+    fe = O.extract(r["freq_edits"].astype(fld.x.dtype))
+    se = O.extract(r["spatial_edits"].astype(fld.x.dtype))
+    for ex in (fe, se):
+        if ex["count"]:
+            O.huffman_zstd_compress(ex["quant"], level)
+            O.huffman_zstd_compress(ex["pack"], level)
+    return time.perf_counter() - t0, r["iterations"]
+
+
+def cpu_baseline(fld, max_iter, level, budget_s=25.0):
+    times, its = [], 0
+    t_start = time.perf_counter()
+    while not times or (time.perf_counter() - t_start < budget_s and len(times) < 3):
+        t, its = cpu_step(fld, max_iter, level)
+        times.append(t)
+    nbytes = fld.x.nbytes
+    return {"value": nbytes / statistics.median(times) / 1e9, "unit": "GB/s", "cores": os.cpu_count(),
+            "kind": "port",
+            "sample": f"{len(times)} full project+encode step(s) of the same field ({its} iteration(s), FP64 "
+                      f"pocketfft with {os.cpu_count()} workers, C compaction/Huffman, libzstd level {level})"}
+
+
+def run_reference(args):
+    rank, world = int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1))
+    if rank != 0:
+        return
+    fld, max_iter = load_workload(args.workload)
+    for _ in range(args.warmup):
+        cpu_step(fld, max_iter, args.zstd_level)
+    times = []
+    its = 0
+    for _ in range(args.steps):
+        t, its = cpu_step(fld, max_iter, args.zstd_level)
+        times.append(t)
+    total = sum(times)
+    v = fld.x.nbytes * args.steps / total / 1e9
+    line = {"metric": METRIC, "value": v, "unit": "GB/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "impl": "reference",
+            "config": config(args, fld, its),
+            "cpu_baseline": {"value": v, "unit": "GB/s", "cores": os.cpu_count(), "kind": "port",
+                             "sample": f"{args.steps} full project+encode steps of the workload "
+                                       f"({its} iteration(s) each) on {os.cpu_count()} host threads"},
+            "e2e": {"value": v, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def config(args, fld, its):
+    return {"workload": f"{args.workload}: {'x'.join(map(str, fld.shape))} {fld.x.dtype}, "
+                        f"E={fld.eps:.4g}, Delta={fld.delta:.4g}, max_iter 100, tol 1e-7",
+            "iterations": its, "zstd_level": args.zstd_level, "zstd_mode": args.zstd_mode,
+            "l2": "inputs and working set (x, x', e, spectrum, edits: >400 MB) larger than L2",
+            "parallelism": f"replicas x{args.gpus}"}
+
+
+# --------------------------------------------------------------------------- GPU leg
+def run_ours(args):
+    import torch
+
+    import ffcz_gb300 as F
+
+    rank, world = dist_init(args.gpus)
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+    fld, max_iter = load_workload(args.workload)
+    zmode = F.FFCZ_ZSTD_CHUNKED if args.zstd_mode == "chunked" else F.FFCZ_ZSTD_SINGLE
+    dt = fld.x.dtype
+    N = fld.x.size
+    x_h = torch.from_numpy(fld.x.reshape(-1)).pin_memory()
+    e0_np = (fld.xp - fld.x).astype(dt).reshape(-1)
+    e0_h = torch.from_numpy(e0_np).pin_memory()
+    dx = x_h.cuda()
+    dxp = torch.from_numpy(fld.xp.reshape(-1)).cuda()
+    s = F.ProjectionSolver(*fld.shape, dtype=dt)
+    s.set_stream(torch.cuda.current_stream())
+    s.set_profiling(True)
+    s.initialize_all_abs_device(dx, fld.eps, fld.delta)
+
+    def step_device():
+        s.reset_edit_accumulators()
+        s.solve_all_abs_pair_device(dx, dxp, max_iter, 1e-7)
+        out = s.encode(args.zstd_level, zmode)
+        return s.launch_count(), out
+
+    def step_e2e():
+        s.reset_edit_accumulators()
+        s.initialize_all_abs(x_h.numpy(), fld.eps, fld.delta)
+        s.solve_all_abs(e0_h.numpy(), max_iter, 1e-7)
+        out = s.encode(args.zstd_level, zmode)
+        return out
+
+    for _ in range(args.warmup):
+        step_device()
+    torch.cuda.synchronize()
+    clocks = Clocks()
+    barrier(world)
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    launches = 0
+    pass_ms = {}
+    ev0.record()
+    for _ in range(args.steps):
+        n, out = step_device()
+        launches += n
+        for i, (ms, by) in enumerate(s.pass_times()):
+            pass_ms.setdefault(i, []).append((ms, by))
+    ev1.record()
+    torch.cuda.synchronize()
+    barrier(world)
+    t_dev = ev0.elapsed_time(ev1) / 1e3
+    t_dev = max_over_ranks(t_dev, world)
+    clk = clocks.stop()
+    comp_bytes = sum(len(r.compressed_data) for r in out if r is not None)
+    its = s.iterations
+    counts = s.active_counts()
+
+    # e2e through the reference-facing API with host buffers
+    for _ in range(max(1, args.warmup // 2)):
+        step_e2e()
+    torch.cuda.synchronize()
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        out_e = step_e2e()
+    torch.cuda.synchronize()
+    t_e2e = max_over_ranks(time.perf_counter() - t0, world)
+    d2h = sum(len(r.bitstream) for r in out_e if r is not None) + 8 * 4
+
+    # dominant pass of the first iteration, from the events inside the graph
+    peak, peak_kind = peak_hbm()
+    names = pass_names(fld.shape)
+    avg = {i: (statistics.mean(m for m, _ in v), v[0][1]) for i, v in pass_ms.items()}
+    dom = max(avg, key=lambda i: avg[i][0])
+    ms_dom, by_dom = avg[dom]
+    achieved = by_dom / (ms_dom / 1e3) / 1e9
+    # GPU-only (project + Huffman, no ZSTD) for reference
+    value = N * dt.itemsize * args.steps * world / t_dev / 1e9
+    line = {
+        "metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * t_dev / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32" if dt == np.float32 else "f64",
+        "data": "synthetic", "config": config(args, fld, its),
+        "e2e": {"value": N * dt.itemsize * args.steps * world / t_e2e / 1e9, "unit": "GB/s",
+                "h2d_bytes_per_step": 2 * N * dt.itemsize, "d2h_bytes_per_step": d2h},
+        "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_source": f"{peak_kind} hbm_gbs", "traffic": None,
+                     "algorithmic_bytes_per_launch": by_dom, "avg_launch_ms": ms_dom},
+        "passes": {names[i]: {"ms": round(m, 5), "GB/s": round(b / (m / 1e3) / 1e9, 1)} for i, (m, b) in avg.items()},
+        "gpu_launches": launches,
+        "active_edits": {"freq": counts[0], "spatial": counts[1]},
+        "compressed_bytes": comp_bytes,
+        "clocks": clk,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(fld, max_iter, args.zstd_level)
+    if rank == 0:
+        print(json.dumps(line))
+    s.close()
+
+
+def pass_names(shape):
+    nx, ny, nz = shape
+    names = ["zfwd_r2c"]
+    if nx > 1:
+        if ny > 1:
+            names.append("y_fwd")
+        names.append("x_fwd_clamp_inv")
+        if ny > 1:
+            names.append("y_inv")
+    elif ny > 1:
+        names.append("y_fwd_clamp_inv")
+    else:
+        names.append("freq_clamp")
+    names.append("zinv_c2r_viol")
+    return names
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

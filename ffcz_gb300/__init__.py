@@ -1,0 +1,446 @@
+"""Python binding of the GB300 FFCz corrector and edit encoder (libffcz.so).
+
+Thin ctypes layer over the C ABI declared in include/ffcz.h, mirroring the
+reference's C++ interface:
+
+* ``ProjectionSolver`` -- ProjectionSolver<T> (projection_algorithm.cuh:238-333)
+* ``cuda_huffman_zstd_compress`` / ``cuda_huffman_zstd_decompress`` --
+  cudaHuffmanZstdCompress / cudaHuffmanZstdDecompress (HuffmanZSTDCoder.cuh:454-470)
+* ``read_raw_array_binary`` / ``write_raw_array_binary`` / ``write_map`` /
+  ``read_map`` -- fileIO.h:17-55
+
+All compute runs in the native library; this module only moves arguments.
+Importing it does not need a GPU; calling into the solver does.  If the
+library has not been built the import fails loudly (there is no fallback).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass, field
+from pathlib import Path
+
+import numpy as np
+
+_PKG = Path(__file__).resolve().parent
+LIB_PATH = _PKG / "_build" / "libffcz.so"
+
+FFCZ_OK = 0
+FFCZ_F32, FFCZ_F64 = 0, 1
+FFCZ_PACK_CORRECT, FFCZ_PACK_REFERENCE = 0, 1
+FFCZ_LOOP_GRAPH, FFCZ_LOOP_HOST = 0, 1
+FFCZ_ZSTD_SINGLE, FFCZ_ZSTD_CHUNKED = 0, 1
+ERRORS = {-1: "INVALID", -2: "CUDA", -3: "UNSUPPORTED", -4: "NOT_INITIALIZED", -5: "ZSTD",
+          -6: "CAPACITY", -7: "CODE_TOO_LONG", -8: "EMPTY", -9: "IO"}
+
+
+class FFCzError(RuntimeError):
+    """A non-zero status from the C ABI; ``code`` is the FFCZ_ERR_* value."""
+
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[{ERRORS.get(code, code)}] {msg}")
+        self.code = code
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    """Loads libffcz.so (once).  Raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        path = os.environ.get("FFCZ_LIB", str(LIB_PATH))
+        if not Path(path).exists():
+            raise ImportError(f"libffcz.so not found at {path}; run `python -m ffcz_gb300.build`")
+        _lib = C.CDLL(path)
+        _declare(_lib)
+    return _lib
+
+
+_sz = C.c_size_t
+_p = C.c_void_p
+_i = C.c_int
+_d = C.c_double
+_PP = C.POINTER(C.c_void_p)
+_SP = C.POINTER(C.c_size_t)
+
+# name -> argtypes (all return int unless listed in _RET)
+SIGNATURES = {
+    "ffcz_solver_create": [_sz, _sz, _sz, _i, _PP],
+    "ffcz_solver_destroy": [_p],
+    "ffcz_solver_set_stream": [_p, _p],
+    "ffcz_solver_set_loop_driver": [_p, _i],
+    "ffcz_solver_set_pack_mode": [_p, _i],
+    "ffcz_init_all_abs": [_p, _p, _d, _d],
+    "ffcz_init_all_abs_device": [_p, _p, _d, _d],
+    "ffcz_solve_all_abs": [_p, _p, _i, _d],
+    "ffcz_solve_all_abs_device": [_p, _p, _i, _d],
+    "ffcz_solve_all_abs_pair_device": [_p, _p, _p, _i, _d],
+    "ffcz_project_all_abs_device": [_p, _p, _i, _d],
+    "ffcz_extract": [_p],
+    "ffcz_reset_edit_accumulators": [_p],
+    "ffcz_solver_synchronize": [_p],
+    "ffcz_get_iterations": [_p, C.POINTER(C.c_int)],
+    "ffcz_get_convergence": [_p, C.POINTER(C.c_double)],
+    "ffcz_get_active_counts": [_p, _SP, _SP],
+    "ffcz_get_minmax": [_p] + [C.POINTER(C.c_double)] * 4,
+    "ffcz_get_results": [_p, _p],
+    "ffcz_get_freq_edits_full": [_p, _p, _sz],
+    "ffcz_get_spatial_edits_full": [_p, _p, _sz],
+    "ffcz_get_freq_quant": [_p, _p, _sz, _SP],
+    "ffcz_get_spatial_quant": [_p, _p, _sz, _SP],
+    "ffcz_get_freq_compact": [_p, _p, _sz, _SP],
+    "ffcz_get_spatial_compact": [_p, _p, _sz, _SP],
+    "ffcz_get_freq_flags_pack": [_p, _p, _sz, _SP],
+    "ffcz_get_spatial_flags_pack": [_p, _p, _sz, _SP],
+    "ffcz_get_freq_flags": [_p, _p, _sz, _SP],
+    "ffcz_get_spatial_flags": [_p, _p, _sz, _SP],
+    "ffcz_get_device_array": [_p, _i, _PP, _SP],
+    "ffcz_get_sizes": [_p, _SP, _SP],
+    "ffcz_get_launch_count": [_p, C.POINTER(C.c_longlong)],
+    "ffcz_solver_set_profiling": [_p, _i],
+    "ffcz_get_pass_times": [_p, _p, _p, _i, C.POINTER(C.c_int)],
+    "ffcz_huff_compress_u16": [_p, _sz, _i, _PP],
+    "ffcz_huff_compress_u8": [_p, _sz, _i, _PP],
+    "ffcz_huff_compress_device": [_p, _sz, _i, _i, _i, _p, _PP],
+    "ffcz_huff_result_free": [_p],
+    "ffcz_huff_result_sizes": [_p, _SP, _SP, _SP, _SP],
+    "ffcz_huff_result_compressed": [_p, _p, _sz],
+    "ffcz_huff_result_bitstream": [_p, _p, _sz],
+    "ffcz_huff_result_codes": [_p, _p, _p, _p, _sz],
+    "ffcz_huff_decompress_u16": [_p, _sz, _p, _p, _p, _sz, _sz, _sz, _p, _SP],
+    "ffcz_huff_decompress_u8": [_p, _sz, _p, _p, _p, _sz, _sz, _sz, _p, _SP],
+    "ffcz_solver_encode": [_p, _i, _i, C.POINTER(C.c_void_p * 4)],
+    "ffcz_read_raw": [C.c_char_p, _p, _sz, _sz],
+    "ffcz_write_raw": [C.c_char_p, _p, _sz, _sz],
+    "ffcz_write_map": [C.c_char_p, _p, _p, _p, _sz],
+    "ffcz_read_map": [C.c_char_p, _p, _p, _p, _sz, _SP],
+    "ffcz_last_error": [],
+    "ffcz_version": [],
+}
+_RET = {"ffcz_last_error": C.c_char_p, "ffcz_version": C.c_char_p, "ffcz_huff_result_free": None}
+
+
+def _declare(L: C.CDLL) -> None:
+    for name, args in SIGNATURES.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = _RET.get(name, C.c_int)
+
+
+def _check(rc: int) -> None:
+    if rc != FFCZ_OK:
+        raise FFCzError(rc, lib().ffcz_last_error().decode())
+
+
+def version() -> str:
+    return lib().ffcz_version().decode()
+
+
+def _np_ptr(a: np.ndarray) -> int:
+    return a.ctypes.data
+
+
+def _dev_ptr(t) -> int:
+    """Device address of a torch CUDA tensor (or an int address)."""
+    if isinstance(t, int):
+        return t
+    return t.data_ptr()
+
+
+class ProjectionSolver:
+    """ProjectionSolver<T> (projection_algorithm.cuh:238-333) for T = float32/float64.
+
+    Host methods take numpy arrays (borrowed for the call), ``*_device``
+    methods take torch CUDA tensors (or raw device addresses)."""
+
+    def __init__(self, nx: int, ny: int, nz: int, dtype=np.float32):
+        self.dtype = np.dtype(dtype)
+        if self.dtype not in (np.float32, np.float64):
+            raise ValueError("dtype must be float32 or float64")
+        self.shape = (int(nx), int(ny), int(nz))
+        self.N = int(nx) * int(ny) * int(nz)
+        self.H = int(nx) * int(ny) * (int(nz) // 2 + 1)
+        h = C.c_void_p()
+        _check(lib().ffcz_solver_create(nx, ny, nz, FFCZ_F32 if self.dtype == np.float32 else FFCZ_F64,
+                                        C.byref(h)))
+        self._h = h
+        self.iterations = 0
+
+    # -- lifetime ----------------------------------------------------------
+    def close(self) -> None:
+        if getattr(self, "_h", None) and self._h.value:
+            lib().ffcz_solver_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- configuration -------------------------------------------------------
+    def set_stream(self, stream) -> None:
+        """stream: torch.cuda.Stream, a raw cudaStream_t int, or None."""
+        ptr = 0 if stream is None else (stream if isinstance(stream, int) else stream.cuda_stream)
+        _check(lib().ffcz_solver_set_stream(self._h, C.c_void_p(ptr)))
+
+    def set_loop_driver(self, driver: int) -> None:
+        _check(lib().ffcz_solver_set_loop_driver(self._h, driver))
+
+    def set_pack_mode(self, mode: int) -> None:
+        _check(lib().ffcz_solver_set_pack_mode(self._h, mode))
+
+    # -- reference API -------------------------------------------------------
+    def _host(self, a) -> np.ndarray:
+        a = np.ascontiguousarray(a, dtype=self.dtype).reshape(-1)
+        if a.size != self.N:
+            raise ValueError(f"expected {self.N} elements, got {a.size}")
+        return a
+
+    def initialize_all_abs(self, x, spatial_epsilon: float, delta: float) -> None:
+        x = self._host(x)
+        _check(lib().ffcz_init_all_abs(self._h, _np_ptr(x), float(spatial_epsilon), float(delta)))
+
+    def initialize_all_abs_device(self, d_x, spatial_epsilon: float, delta: float) -> None:
+        _check(lib().ffcz_init_all_abs_device(self._h, _dev_ptr(d_x), float(spatial_epsilon), float(delta)))
+
+    def solve_all_abs(self, e0, max_iterations: int = 100, tol: float = 1e-7) -> int:
+        e0 = self._host(e0)
+        _check(lib().ffcz_solve_all_abs(self._h, _np_ptr(e0), int(max_iterations), float(tol)))
+        return self._iters()
+
+    def solve_all_abs_device(self, d_e0, max_iterations: int = 100, tol: float = 1e-7) -> int:
+        _check(lib().ffcz_solve_all_abs_device(self._h, _dev_ptr(d_e0), int(max_iterations), float(tol)))
+        return self._iters()
+
+    def solve_all_abs_pair_device(self, d_x, d_xprime, max_iterations: int = 100, tol: float = 1e-7) -> int:
+        _check(lib().ffcz_solve_all_abs_pair_device(self._h, _dev_ptr(d_x), _dev_ptr(d_xprime),
+                                                     int(max_iterations), float(tol)))
+        return self._iters()
+
+    def project_all_abs_device(self, d_e0, max_iterations: int = 100, tol: float = 1e-7) -> int:
+        _check(lib().ffcz_project_all_abs_device(self._h, _dev_ptr(d_e0), int(max_iterations), float(tol)))
+        return self._iters()
+
+    def extract_compact_representation(self) -> None:
+        _check(lib().ffcz_extract(self._h))
+
+    def reset_edit_accumulators(self) -> None:
+        _check(lib().ffcz_reset_edit_accumulators(self._h))
+
+    def synchronize(self) -> None:
+        _check(lib().ffcz_solver_synchronize(self._h))
+
+    def _iters(self) -> int:
+        v = C.c_int()
+        _check(lib().ffcz_get_iterations(self._h, C.byref(v)))
+        self.iterations = v.value
+        return v.value
+
+    # -- getters ---------------------------------------------------------------
+    @property
+    def convergence_metric(self) -> float:
+        v = C.c_double()
+        _check(lib().ffcz_get_convergence(self._h, C.byref(v)))
+        return v.value
+
+    def active_counts(self) -> tuple[int, int]:
+        a, b = C.c_size_t(), C.c_size_t()
+        _check(lib().ffcz_get_active_counts(self._h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    def minmax(self) -> tuple[float, float, float, float]:
+        v = [C.c_double() for _ in range(4)]
+        _check(lib().ffcz_get_minmax(self._h, *[C.byref(x) for x in v]))
+        return tuple(x.value for x in v)
+
+    def get_min_freq_edit(self): return self.dtype.type(self.minmax()[0])
+    def get_max_freq_edit(self): return self.dtype.type(self.minmax()[1])
+    def get_min_spatial_edit(self): return self.dtype.type(self.minmax()[2])
+    def get_max_spatial_edit(self): return self.dtype.type(self.minmax()[3])
+
+    def get_results(self) -> np.ndarray:
+        out = np.empty(self.N, self.dtype)
+        _check(lib().ffcz_get_results(self._h, _np_ptr(out)))
+        return out.reshape(self.shape)
+
+    def get_freq_edits_full(self) -> np.ndarray:
+        out = np.empty(2 * self.H, self.dtype)
+        _check(lib().ffcz_get_freq_edits_full(self._h, _np_ptr(out), out.size))
+        return out
+
+    def get_spatial_edits_full(self) -> np.ndarray:
+        out = np.empty(self.N, self.dtype)
+        _check(lib().ffcz_get_spatial_edits_full(self._h, _np_ptr(out), out.size))
+        return out
+
+    def _stream(self, fn, count: int, dtype) -> np.ndarray:
+        out = np.empty(max(count, 1), dtype)
+        n = C.c_size_t()
+        _check(getattr(lib(), fn)(self._h, _np_ptr(out), out.size, C.byref(n)))
+        return out[: n.value]
+
+    def get_active_freq_quant_edit_distances(self):
+        return self._stream("ffcz_get_freq_quant", self.active_counts()[0], np.uint16)
+
+    def get_active_spatial_quant_edit_distances(self):
+        return self._stream("ffcz_get_spatial_quant", self.active_counts()[1], np.uint16)
+
+    def get_active_freq_edit_distances(self):
+        return self._stream("ffcz_get_freq_compact", self.active_counts()[0], self.dtype)
+
+    def get_active_spatial_edit_distances(self):
+        return self._stream("ffcz_get_spatial_compact", self.active_counts()[1], self.dtype)
+
+    def get_freq_flags_pack(self):
+        return self._stream("ffcz_get_freq_flags_pack", (2 * self.H + 7) // 8, np.uint8)
+
+    def get_spatial_flags_pack(self):
+        return self._stream("ffcz_get_spatial_flags_pack", (self.N + 7) // 8, np.uint8)
+
+    def get_freq_flags(self):
+        return self._stream("ffcz_get_freq_flags", 2 * self.H, np.uint8).astype(bool)
+
+    def get_spatial_flags(self):
+        return self._stream("ffcz_get_spatial_flags", self.N, np.uint8).astype(bool)
+
+    def device_array(self, which: int) -> tuple[int, int]:
+        p, n = C.c_void_p(), C.c_size_t()
+        _check(lib().ffcz_get_device_array(self._h, which, C.byref(p), C.byref(n)))
+        return p.value or 0, n.value
+
+    def set_profiling(self, on: bool) -> None:
+        _check(lib().ffcz_solver_set_profiling(self._h, int(bool(on))))
+
+    def pass_times(self) -> list[tuple[float, float]]:
+        """[(ms, algorithmic bytes)] per pass of the last solve's first iteration."""
+        ms, by = np.zeros(8), np.zeros(8)
+        n = C.c_int()
+        _check(lib().ffcz_get_pass_times(self._h, _np_ptr(ms), _np_ptr(by), 8, C.byref(n)))
+        return [(float(ms[i]), float(by[i])) for i in range(n.value)]
+
+    def launch_count(self) -> int:
+        v = C.c_longlong()
+        _check(lib().ffcz_get_launch_count(self._h, C.byref(v)))
+        return v.value
+
+    def encode(self, zstd_level: int = 20, zstd_mode: int = FFCZ_ZSTD_SINGLE) -> list:
+        """The four streams of projection_example.cu:230-246 (None where skipped)."""
+        arr = (C.c_void_p * 4)()
+        _check(lib().ffcz_solver_encode(self._h, zstd_level, zstd_mode, C.byref(arr)))
+        return [None if not p else _take_result(p) for p in arr]
+
+
+# ---------------------------------------------------------------------------
+@dataclass
+class CompressionResult:
+    """SimpleCudaHuffmanZstdCompressor<T>::CompressionResult (HuffmanZSTDCoder.cuh:240-246)."""
+    compressed_data: bytes
+    code_table: dict = field(repr=False)      # symbol -> (code, length)
+    original_bitstream_size: int
+    num_elements: int
+    bitstream: bytes = field(repr=False, default=b"")
+
+    def arrays(self):
+        syms = np.array(sorted(self.code_table), dtype=np.uint32)
+        codes = np.array([self.code_table[s][0] for s in syms], dtype=np.uint32)
+        lens = np.array([self.code_table[s][1] for s in syms], dtype=np.int32)
+        return syms, codes, lens
+
+
+def _take_result(p: int) -> CompressionResult:
+    L = lib()
+    comp, bits, nel, nsym = (C.c_size_t() for _ in range(4))
+    _check(L.ffcz_huff_result_sizes(p, C.byref(comp), C.byref(bits), C.byref(nel), C.byref(nsym)))
+    cbuf = np.empty(max(comp.value, 1), np.uint8)
+    bbuf = np.empty(max(bits.value, 1), np.uint8)
+    _check(L.ffcz_huff_result_compressed(p, _np_ptr(cbuf), cbuf.size))
+    _check(L.ffcz_huff_result_bitstream(p, _np_ptr(bbuf), bbuf.size))
+    k = max(nsym.value, 1)
+    syms, codes, lens = np.empty(k, np.uint32), np.empty(k, np.uint32), np.empty(k, np.int32)
+    if nsym.value:
+        _check(L.ffcz_huff_result_codes(p, _np_ptr(syms), _np_ptr(codes), _np_ptr(lens), k))
+    table = {int(syms[i]): (int(codes[i]), int(lens[i])) for i in range(nsym.value)}
+    r = CompressionResult(bytes(cbuf[: comp.value]), table, bits.value, nel.value, bytes(bbuf[: bits.value]))
+    L.ffcz_huff_result_free(p)
+    return r
+
+
+def cuda_huffman_zstd_compress(data, zstd_level: int = 3) -> CompressionResult:
+    """cudaHuffmanZstdCompress<T> for uint8 / uint16 host data."""
+    a = np.ascontiguousarray(data)
+    if a.dtype not in (np.uint8, np.uint16):
+        raise TypeError("symbols must be uint8 or uint16")
+    out = C.c_void_p()
+    fn = lib().ffcz_huff_compress_u16 if a.dtype == np.uint16 else lib().ffcz_huff_compress_u8
+    _check(fn(_np_ptr(a) if a.size else None, a.size, int(zstd_level), C.byref(out)))
+    return _take_result(out.value)
+
+
+def cuda_huffman_zstd_compress_device(d_data, n: int, symbol_bytes: int, zstd_level: int = 3,
+                                      zstd_mode: int = FFCZ_ZSTD_SINGLE, stream=None) -> CompressionResult:
+    out = C.c_void_p()
+    sp = 0 if stream is None else (stream if isinstance(stream, int) else stream.cuda_stream)
+    _check(lib().ffcz_huff_compress_device(_dev_ptr(d_data), n, symbol_bytes, zstd_level, zstd_mode,
+                                            C.c_void_p(sp), C.byref(out)))
+    return _take_result(out.value)
+
+
+def cuda_huffman_zstd_decompress(compressed: bytes, code_table: dict, num_elements: int,
+                                 original_bitstream_size: int, dtype=np.uint16) -> np.ndarray:
+    """cudaHuffmanZstdDecompress<T> (HuffmanZSTDCoder.cuh:462-470)."""
+    dtype = np.dtype(dtype)
+    syms = np.array(sorted(code_table), dtype=np.uint32)
+    codes = np.array([code_table[s][0] for s in syms], dtype=np.uint32)
+    lens = np.array([code_table[s][1] for s in syms], dtype=np.int32)
+    comp = np.frombuffer(compressed, np.uint8) if len(compressed) else np.zeros(1, np.uint8)
+    out = np.empty(max(num_elements, 1), dtype)
+    n = C.c_size_t()
+    fn = lib().ffcz_huff_decompress_u16 if dtype == np.uint16 else lib().ffcz_huff_decompress_u8
+    _check(fn(_np_ptr(comp), len(compressed), _np_ptr(syms) if syms.size else None,
+              _np_ptr(codes) if codes.size else None, _np_ptr(lens) if lens.size else None, syms.size,
+              num_elements, original_bitstream_size, _np_ptr(out), C.byref(n)))
+    return out[: n.value]
+
+
+# ---------------------------------------------------------------------------
+def read_raw_array_binary(path, n: int, dtype) -> np.ndarray:
+    """readRawArrayBinary (fileIO.cpp:35-76)."""
+    dtype = np.dtype(dtype)
+    out = np.empty(max(n, 1), dtype)
+    _check(lib().ffcz_read_raw(str(path).encode(), _np_ptr(out), n, dtype.itemsize))
+    return out[:n]
+
+
+def write_raw_array_binary(a, path) -> None:
+    """writeRawArrayBinary / writeVectorBinary (fileIO.h:23-55)."""
+    a = np.ascontiguousarray(a)
+    _check(lib().ffcz_write_raw(str(path).encode(), _np_ptr(a), a.size, a.dtype.itemsize))
+
+
+def write_map(m: dict, path) -> None:
+    """writeMap (fileIO.cpp:3-14): {int key: (uint32 code, int len)}."""
+    keys = np.array(sorted(m), dtype=np.int32)
+    codes = np.array([m[k][0] for k in keys], dtype=np.uint32)
+    lens = np.array([m[k][1] for k in keys], dtype=np.int32)
+    _check(lib().ffcz_write_map(str(path).encode(), _np_ptr(keys), _np_ptr(codes), _np_ptr(lens), keys.size))
+
+
+def read_map(path) -> dict:
+    """readMap (fileIO.cpp:16-33)."""
+    n = C.c_size_t()
+    rc = lib().ffcz_read_map(str(path).encode(), None, None, None, 0, C.byref(n))
+    if rc not in (FFCZ_OK, -6):
+        _check(rc)
+    k = max(n.value, 1)
+    keys, codes, lens = np.empty(k, np.int32), np.empty(k, np.uint32), np.empty(k, np.int32)
+    _check(lib().ffcz_read_map(str(path).encode(), _np_ptr(keys), _np_ptr(codes), _np_ptr(lens), k,
+                               C.byref(n)))
+    return {int(keys[i]): (int(codes[i]), int(lens[i])) for i in range(n.value)}

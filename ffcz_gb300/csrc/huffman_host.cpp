@@ -1,0 +1,212 @@
+#include "huffman_host.h"
+
+#include <dlfcn.h>
+
+#include <algorithm>
+#include <functional>
+#include <mutex>
+#include <queue>
+#include <thread>
+#include <utility>
+
+#include "../../include/ffcz.h"
+
+namespace ffcz {
+
+int fail(int code, const std::string &msg);
+
+void build_codebook(const uint32_t *hist, size_t nbins, Codebook &cb) {
+  cb.sym.clear();
+  cb.freq.clear();
+  for (size_t s = 0; s < nbins; ++s) {
+    if (hist[s]) {
+      cb.sym.push_back((uint32_t)s);
+      cb.freq.push_back(hist[s]);
+    }
+  }
+  const int n = (int)cb.sym.size();
+  cb.code.assign(n, 0u);
+  cb.len.assign(n, 0);
+  cb.max_len = 0;
+  if (n == 0) return;
+  if (n == 1) {
+    cb.code[0] = 0u;
+    cb.len[0] = 1;
+    cb.max_len = 1;
+    return;
+  }
+  // Nodes: leaves 0..n-1, internal n..2n-2.
+  std::vector<int> left(2 * n - 1, -1), right(2 * n - 1, -1);
+  using Key = std::pair<uint32_t, int>;
+  std::priority_queue<Key, std::vector<Key>, std::greater<Key>> pq;
+  for (int i = 0; i < n; ++i) pq.push({cb.freq[i], i});
+  int next = n;
+  while (pq.size() > 1) {
+    const Key a = pq.top();
+    pq.pop();
+    const Key b = pq.top();
+    pq.pop();
+    left[next] = a.second;
+    right[next] = b.second;
+    pq.push({a.first + b.first, next});
+    ++next;
+  }
+  const int root = pq.top().second;
+  // Iterative depth-first walk from the root.
+  struct Item { int node; uint32_t code; int len; };
+  std::vector<Item> stack;
+  stack.push_back({root, 0u, 0});
+  while (!stack.empty()) {
+    const Item it = stack.back();
+    stack.pop_back();
+    if (left[it.node] < 0 && right[it.node] < 0) {
+      cb.code[it.node] = it.code;
+      cb.len[it.node] = it.len ? it.len : 1;
+      cb.max_len = std::max(cb.max_len, cb.len[it.node]);
+      continue;
+    }
+    if (right[it.node] >= 0) stack.push_back({right[it.node], (it.code << 1) | 1u, it.len + 1});
+    if (left[it.node] >= 0) stack.push_back({left[it.node], it.code << 1, it.len + 1});
+  }
+}
+
+std::vector<uint32_t> huffman_decode(const uint8_t *bits, size_t nbytes, const uint32_t *symbols,
+                                     const uint32_t *codes, const int32_t *lengths, size_t nsym,
+                                     size_t num_elements) {
+  // Binary trie of the codes of length 1..32 (longer codes are never
+  // matched by the reference decoder).  node 0 = root; child[2*i + bit].
+  std::vector<int> child(2, -1), leaf(1, -1);
+  for (size_t s = 0; s < nsym; ++s) {
+    const int L = lengths[s];
+    if (L < 1 || L > 32) continue;
+    int node = 0;
+    for (int d = L - 1; d >= 0; --d) {
+      const int bit = (codes[s] >> d) & 1u;
+      int &c = child[2 * node + bit];
+      if (c < 0) {
+        c = (int)leaf.size();
+        leaf.push_back(-1);
+        child.push_back(-1);
+        child.push_back(-1);
+      }
+      node = child[2 * node + bit];
+    }
+    if (leaf[node] < 0) leaf[node] = (int)s;
+  }
+  std::vector<uint32_t> out;
+  out.reserve(num_elements);
+  const size_t total = nbytes * 8;
+  size_t pos = 0;
+  while (out.size() < num_elements && pos < total) {
+    int node = 0;
+    size_t p = pos;
+    int sym = -1;
+    int depth = 0;
+    while (p < total && depth < 32) {
+      const int bit = (bits[p >> 3] >> (7 - (p & 7))) & 1;
+      node = child[2 * node + bit];
+      ++p;
+      ++depth;
+      if (node < 0) break;
+      if (leaf[node] >= 0) {
+        sym = leaf[node];
+        break;
+      }
+    }
+    if (sym >= 0) {
+      out.push_back(symbols[sym]);
+      pos = p;
+    } else {
+      ++pos;  // no code matches here: skip one bit (HuffmanZSTDCoder.cuh:442-446)
+    }
+  }
+  return out;
+}
+
+// ------------------------------------------------------------------ ZSTD --
+namespace {
+struct Zstd {
+  size_t (*compressBound)(size_t) = nullptr;
+  size_t (*compress)(void *, size_t, const void *, size_t, int) = nullptr;
+  size_t (*decompress)(void *, size_t, const void *, size_t) = nullptr;
+  unsigned (*isError)(size_t) = nullptr;
+  const char *(*getErrorName)(size_t) = nullptr;
+  bool ok = false;
+  std::string why;
+};
+Zstd &zstd() {
+  static Zstd z;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void *h = dlopen("libzstd.so.1", RTLD_NOW | RTLD_LOCAL);
+    if (!h) h = dlopen("libzstd.so", RTLD_NOW | RTLD_LOCAL);
+    if (!h) {
+      z.why = "libzstd.so.1 not found";
+      return;
+    }
+    z.compressBound = (size_t(*)(size_t))dlsym(h, "ZSTD_compressBound");
+    z.compress = (size_t(*)(void *, size_t, const void *, size_t, int))dlsym(h, "ZSTD_compress");
+    z.decompress = (size_t(*)(void *, size_t, const void *, size_t))dlsym(h, "ZSTD_decompress");
+    z.isError = (unsigned (*)(size_t))dlsym(h, "ZSTD_isError");
+    z.getErrorName = (const char *(*)(size_t))dlsym(h, "ZSTD_getErrorName");
+    z.ok = z.compressBound && z.compress && z.decompress && z.isError && z.getErrorName;
+    if (!z.ok) z.why = "libzstd.so.1 lacks a required symbol";
+  });
+  return z;
+}
+}  // namespace
+
+bool zstd_available(std::string *why) {
+  Zstd &z = zstd();
+  if (!z.ok && why) *why = z.why;
+  return z.ok;
+}
+
+static int compress_one(const uint8_t *src, size_t n, int level, std::vector<uint8_t> &out) {
+  Zstd &z = zstd();
+  const size_t bound = z.compressBound(n);
+  out.resize(bound);
+  const size_t r = z.compress(out.data(), bound, src, n, level);
+  if (z.isError(r)) return fail(FFCZ_ERR_ZSTD, std::string("ZSTD compression failed: ") + z.getErrorName(r));
+  out.resize(r);
+  return FFCZ_OK;
+}
+
+int zstd_compress(const uint8_t *src, size_t n, int level, bool chunked, std::vector<uint8_t> &out) {
+  std::string why;
+  if (!zstd_available(&why)) return fail(FFCZ_ERR_ZSTD, why);
+  if (!chunked || n < (256u << 10)) return compress_one(src, n, level, out);
+  unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+  size_t chunk = std::max<size_t>((n + hw - 1) / hw, 128u << 10);
+  const size_t nch = (n + chunk - 1) / chunk;
+  std::vector<std::vector<uint8_t>> parts(nch);
+  std::vector<int> rc(nch, FFCZ_OK);
+  std::vector<std::thread> th;
+  for (size_t c = 0; c < nch; ++c) {
+    th.emplace_back([&, c] {
+      const size_t off = c * chunk;
+      rc[c] = compress_one(src + off, std::min(chunk, n - off), level, parts[c]);
+    });
+  }
+  for (auto &t : th) t.join();
+  out.clear();
+  for (size_t c = 0; c < nch; ++c) {
+    if (rc[c] != FFCZ_OK) return rc[c];
+    out.insert(out.end(), parts[c].begin(), parts[c].end());
+  }
+  return FFCZ_OK;
+}
+
+int zstd_decompress(const uint8_t *src, size_t n, size_t expect, std::vector<uint8_t> &out) {
+  std::string why;
+  if (!zstd_available(&why)) return fail(FFCZ_ERR_ZSTD, why);
+  Zstd &z = zstd();
+  out.resize(expect);
+  const size_t r = z.decompress(out.data(), expect, src, n);
+  if (z.isError(r))
+    return fail(FFCZ_ERR_ZSTD, std::string("ZSTD decompression failed: ") + z.getErrorName(r));
+  out.resize(r);
+  return FFCZ_OK;
+}
+
+}  // namespace ffcz

@@ -1,0 +1,821 @@
+// ProjectionSolver<T> of projection_algorithm_impl.cuh:1-910 behind the C
+// ABI: device buffers, transform plans, the iteration loop (one CUDA graph
+// with a device-side WHILE node, or a host-driven loop), compaction, and
+// the four-stream encode of projection_example.cu:230-246.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <future>
+#include <memory>
+#include <vector>
+
+#include "extract.cuh"
+#include "fft_plan.h"
+#include "huffman.cuh"
+#include "passes.cuh"
+
+using namespace ffcz;
+
+namespace {
+
+constexpr size_t kSmemBudget = 113 * 1024;  // two blocks per SM
+constexpr size_t kSmemMax = 226 * 1024;  // 227 KB per block minus room for static shared memory
+
+struct GraphKey {
+  const void *a = nullptr, *b = nullptr;
+  int pro = -1, max_iter = -1;
+  double tol = 0, eps = 0, delta = 0;
+  cudaStream_t stream = nullptr;
+  int profile = 0;
+  bool operator==(const GraphKey &o) const {
+    return a == o.a && b == o.b && pro == o.pro && max_iter == o.max_iter && tol == o.tol &&
+           eps == o.eps && delta == o.delta && stream == o.stream && profile == o.profile;
+  }
+};
+
+struct Launch {  // geometry of one pass
+  unsigned grid = 0;
+  int threads = 0;
+  size_t smem = 0;
+};
+
+}  // namespace
+
+struct ffcz_solver {
+  int dtype = FFCZ_F32;
+  size_t es = 4;  // element size
+  size_t nx = 0, ny = 0, nz = 0, N = 0, H = 0;
+  int Hz = 0, Hzp = 0, M = 0, even = 0;
+  long long rows = 0;
+  int device = 0;
+  cudaStream_t stream = nullptr;      // user stream (NULL = legacy default)
+  cudaStream_t cap = nullptr;         // private capture stream
+  int loop_driver = FFCZ_LOOP_GRAPH;
+  int pack_mode = FFCZ_PACK_CORRECT;
+  // device arrays
+  void *d_x = nullptr, *d_e = nullptr, *d_spec = nullptr;
+  void *d_fedits = nullptr, *d_sedits = nullptr;
+  void *d_fcompact = nullptr, *d_scompact = nullptr;
+  uint16_t *d_fquant = nullptr, *d_squant = nullptr;
+  uint8_t *d_fpack = nullptr, *d_spack = nullptr;
+  size_t fpack_bytes = 0, spack_bytes = 0;  // allocated (multiple of 4)
+  void *d_tw = nullptr;
+  LoopCtl *d_ctl = nullptr, *h_ctl = nullptr;
+  unsigned *d_blk_cnt = nullptr;
+  void *d_blk_mn = nullptr, *d_blk_mx = nullptr, *d_mnmx = nullptr;
+  size_t nblk_max = 0;
+  // plans
+  AxisPlan pz{}, py{}, px{};
+  size_t post_off = 0;  // offset (complex entries) of the R2C split twiddles
+  ZArgs za{};
+  SArgs sy{}, sx{};
+  Launch lz_f, lz_i, ly, lx;
+  int has_x = 0, has_y = 0, fused = 0;  // fused: 0 none, 1 y, 2 x
+  // parameters
+  double eps = 0, delta = 0;
+  bool initialized = false;
+  bool extracted = false;
+  // graph cache
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  GraphKey gkey;
+  // bookkeeping
+  long long launches = 0;
+  int kernels_per_iter = 0;
+  HuffWorkspace huff;
+  // per-pass timing of the first iteration (events recorded inside the graph)
+  int profile = 0;
+  int npass = 0;
+  cudaEvent_t ev[8] = {};
+  double pass_bytes[7] = {};
+  int pro_last = 0;
+};
+
+namespace {
+
+int pick_tile(int rows_smem, int L, size_t es2, int twmax, Launch &ln, int &TW, int ept) {
+  const int kMaxThreads = es2 == 8 ? 512 : 256;
+  for (size_t budget : {kSmemBudget, kSmemMax}) {
+    for (int tw = twmax; tw >= 1; tw >>= 1) {
+      const size_t smem = (size_t)rows_smem * (tw + 1) * es2;
+      const long long need = ((long long)L * tw + ept - 1) / ept;
+      int thr = (int)std::max<long long>(64, ((need + 31) / 32) * 32);
+      if (smem <= budget && thr <= kMaxThreads) {
+        TW = tw;
+        ln.threads = thr;
+        ln.smem = smem;
+        return FFCZ_OK;
+      }
+    }
+  }
+  return fail(FFCZ_ERR_UNSUPPORTED, "axis length " + std::to_string(L) + " too long for one tile");
+}
+
+template <typename T> constexpr int ept_of() { return sizeof(T) == 4 ? 8 : 4; }
+
+template <typename T>
+int set_smem_attrs() {
+  constexpr int E = ept_of<T>();
+  const int mx = (int)kSmemMax;
+  FFCZ_CUDA(cudaFuncSetAttribute(k_zfwd<T, PRO_PLAIN, E>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+  FFCZ_CUDA(cudaFuncSetAttribute(k_zfwd<T, PRO_DIFF, E>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+  FFCZ_CUDA(cudaFuncSetAttribute(k_zfwd<T, PRO_CLAMP, E>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+  FFCZ_CUDA(cudaFuncSetAttribute(k_zinv<T, E>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+  FFCZ_CUDA(cudaFuncSetAttribute(k_strided<T, MODE_FWD, E>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+  FFCZ_CUDA(cudaFuncSetAttribute(k_strided<T, MODE_INV, E>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+  FFCZ_CUDA(cudaFuncSetAttribute(k_strided<T, MODE_FCI, E>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+  return FFCZ_OK;
+}
+
+template <typename T>
+int plan_solver(ffcz_solver *s) {
+  constexpr int E = ept_of<T>();
+  const size_t es2 = sizeof(c2<T>);
+  const int twmax = sizeof(T) == 4 ? 16 : 8;  // 128-byte tile rows
+  s->even = (s->nz % 2 == 0) ? 1 : 0;
+  s->Hz = (int)(s->nz / 2 + 1);
+  s->M = s->even ? (int)(s->nz / 2) : (int)s->nz;
+  s->Hzp = (int)round_up((size_t)s->Hz, (size_t)twmax);
+  s->rows = (long long)(s->nx * s->ny);
+  std::vector<std::complex<double>> table;
+  if (!build_axis_plan(s->M, s->pz, table))
+    return fail(FFCZ_ERR_UNSUPPORTED, "Nz = " + std::to_string(s->nz) + " has an unsupported prime factor");
+  s->has_y = s->ny > 1;
+  s->has_x = s->nx > 1;
+  if (s->has_y && !build_axis_plan((int)s->ny, s->py, table))
+    return fail(FFCZ_ERR_UNSUPPORTED, "Ny = " + std::to_string(s->ny) + " has an unsupported prime factor");
+  if (s->has_x && !build_axis_plan((int)s->nx, s->px, table))
+    return fail(FFCZ_ERR_UNSUPPORTED, "Nx = " + std::to_string(s->nx) + " has an unsupported prime factor");
+  s->post_off = table.size();
+  if (s->even)
+    for (int k = 0; k <= s->M; ++k) {
+      const double th = -2.0 * M_PI * (double)k / (double)s->nz;
+      table.push_back({std::cos(th), std::sin(th)});
+    }
+  if (table.empty()) table.push_back({1.0, 0.0});
+  std::vector<c2<T>> tw(table.size());
+  for (size_t i = 0; i < table.size(); ++i) tw[i] = mkc<T>((T)table[i].real(), (T)table[i].imag());
+  FFCZ_CUDA(cudaMalloc(&s->d_tw, tw.size() * es2));
+  FFCZ_CUDA(cudaMemcpy(s->d_tw, tw.data(), tw.size() * es2, cudaMemcpyHostToDevice));
+  s->pz.tw = s->d_tw;
+  s->py.tw = s->d_tw;
+  s->px.tw = s->d_tw;
+  // z passes
+  {
+    const int rows_smem = s->even ? s->M + 1 : (int)s->nz;
+    const int L = s->even ? s->M : (int)s->nz;
+    int TW = 1;
+    FFCZ_TRY(pick_tile(rows_smem, std::max(L, s->Hz), es2, twmax, s->lz_f, TW, E));
+    s->lz_i = s->lz_f;
+    s->za.rows = s->rows;
+    s->za.Nz = (int)s->nz;
+    s->za.M = s->M;
+    s->za.even = s->even;
+    s->za.Hz = s->Hz;
+    s->za.Hzp = s->Hzp;
+    s->za.TW = TW;
+    s->za.log2TW = __builtin_ctz(TW);
+    s->za.P = TW + 1;
+    s->lz_f.grid = s->lz_i.grid = (unsigned)ceil_div((size_t)s->rows, (size_t)TW);
+  }
+  auto plan_strided = [&](int L, int Q, long long B, SArgs &sa, Launch &ln) -> int {
+    int TW = 1;
+    FFCZ_TRY(pick_tile(L, L, es2, twmax, ln, TW, E));
+    sa.L = L;
+    sa.Q = Q;
+    sa.Hz = s->Hz;
+    sa.Hzp = s->Hzp;
+    sa.Wtot = (long long)Q * s->Hzp;
+    sa.TW = TW;
+    sa.log2TW = __builtin_ctz(TW);
+    sa.P = TW + 1;
+    sa.tpq = (int)ceil_div((size_t)s->Hz, (size_t)TW);
+    const long long tiles = B * Q * (long long)sa.tpq;
+    if (tiles > 0x7fffffffll) return fail(FFCZ_ERR_UNSUPPORTED, "too many tiles");
+    ln.grid = (unsigned)tiles;
+    return FFCZ_OK;
+  };
+  if (s->has_y) FFCZ_TRY(plan_strided((int)s->ny, 1, (long long)s->nx, s->sy, s->ly));
+  if (s->has_x) FFCZ_TRY(plan_strided((int)s->nx, (int)s->ny, 1, s->sx, s->lx));
+  s->fused = s->has_x ? 2 : (s->has_y ? 1 : 0);
+  s->kernels_per_iter = 2 /*z fwd, z inv*/ + 1 /*check*/ + (s->fused ? 1 : 1) +
+                        ((s->has_y && s->fused == 2) ? 2 : 0);
+  FFCZ_TRY(set_smem_attrs<T>());
+  return FFCZ_OK;
+}
+
+template <typename T> T *tp(void *p) { return (T *)p; }
+
+// One iteration: [prologue + R2C z] [y fwd] [fused fwd/clamp/inv] [y inv]
+// [C2R z + 1/N + violation] [check].
+template <typename T>
+void launch_iteration(ffcz_solver *s, cudaStream_t st, int pro, const void *a, const void *b, T tol,
+                      int max_iter, cudaGraphConditionalHandle h, int use_graph, bool record = false) {
+  constexpr int E = ept_of<T>();
+  int ne = 0;
+  // Inside a capture the records become event nodes of the graph.
+  auto mark = [&]() {
+    if (record) cudaEventRecordWithFlags(s->ev[ne++], st, use_graph ? cudaEventRecordExternal : 0);
+  };
+  mark();
+  const T eps = (T)s->eps, delta = (T)s->delta;
+  const c2<T> *post = (const c2<T> *)s->d_tw + s->post_off;
+  c2<T> *spec = (c2<T> *)s->d_spec;
+  const T *pa = (const T *)a, *pb = (const T *)b;
+  if (pro == PRO_PLAIN)
+    k_zfwd<T, PRO_PLAIN, E><<<s->lz_f.grid, s->lz_f.threads, s->lz_f.smem, st>>>(
+        pa, nullptr, tp<T>(s->d_sedits), eps, spec, s->za, s->pz, post);
+  else if (pro == PRO_DIFF)
+    k_zfwd<T, PRO_DIFF, E><<<s->lz_f.grid, s->lz_f.threads, s->lz_f.smem, st>>>(
+        pa, pb, tp<T>(s->d_sedits), eps, spec, s->za, s->pz, post);
+  else
+    k_zfwd<T, PRO_CLAMP, E><<<s->lz_f.grid, s->lz_f.threads, s->lz_f.smem, st>>>(
+        tp<T>(s->d_e), nullptr, tp<T>(s->d_sedits), eps, spec, s->za, s->pz, post);
+  mark();
+  const long long H = (long long)s->H;
+  if (s->fused == 2) {
+    if (s->has_y) {
+      k_strided<T, MODE_FWD, E><<<s->ly.grid, s->ly.threads, s->ly.smem, st>>>(spec, s->sy, s->py, delta,
+                                                                              tp<T>(s->d_fedits), H);
+      mark();
+    }
+    k_strided<T, MODE_FCI, E><<<s->lx.grid, s->lx.threads, s->lx.smem, st>>>(spec, s->sx, s->px, delta,
+                                                                            tp<T>(s->d_fedits), H);
+    mark();
+    if (s->has_y) {
+      k_strided<T, MODE_INV, E><<<s->ly.grid, s->ly.threads, s->ly.smem, st>>>(spec, s->sy, s->py, delta,
+                                                                              tp<T>(s->d_fedits), H);
+      mark();
+    }
+  } else if (s->fused == 1) {
+    k_strided<T, MODE_FCI, E><<<s->ly.grid, s->ly.threads, s->ly.smem, st>>>(spec, s->sy, s->py, delta,
+                                                                            tp<T>(s->d_fedits), H);
+    mark();
+  } else {
+    const long long tot = s->rows * s->Hz;
+    const unsigned g = (unsigned)std::min<long long>((tot + 255) / 256, 152 * 16);
+    k_clamp_freq<T><<<g, 256, 0, st>>>(spec, s->rows, s->Hz, s->Hzp, delta, tp<T>(s->d_fedits), H);
+    mark();
+  }
+  const T factor = T(1) / static_cast<T>(s->N);
+  k_zinv<T, E><<<s->lz_i.grid, s->lz_i.threads, s->lz_i.smem, st>>>(spec, tp<T>(s->d_e), eps, factor, s->d_ctl,
+                                                                    s->za, s->pz, post);
+  mark();
+  if (record) s->npass = ne - 1;
+  k_check<T><<<1, 1, 0, st>>>(s->d_ctl, tol, max_iter, h, use_graph);
+}
+
+template <typename T>
+void launch_final(ffcz_solver *s, cudaStream_t st) {
+  const unsigned g = (unsigned)std::min<size_t>(ceil_div(s->N, 256), 152 * 16);
+  k_final_clamp<T><<<g, 256, 0, st>>>(tp<T>(s->d_e), tp<T>(s->d_sedits), (T)s->eps, (long long)s->N, s->d_ctl);
+}
+
+template <typename T>
+int run_loop_graph(ffcz_solver *s, int pro, const void *a, const void *b, int max_iter, T tol) {
+  GraphKey key;
+  key.a = a;
+  key.b = b;
+  key.pro = pro;
+  key.max_iter = max_iter;
+  key.tol = (double)tol;
+  key.eps = s->eps;
+  key.delta = s->delta;
+  key.stream = s->stream;
+  key.profile = s->profile;
+  if (!(s->gexec && s->gkey == key)) {
+    if (s->gexec) cudaGraphExecDestroy(s->gexec);
+    if (s->graph) cudaGraphDestroy(s->graph);
+    s->gexec = nullptr;
+    s->graph = nullptr;
+    cudaStream_t cs = s->cap;
+    FFCZ_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+    cudaGraph_t g = nullptr;
+    cudaStreamCaptureStatus st;
+    const cudaGraphNode_t *deps = nullptr;
+    const cudaGraphEdgeData *edata = nullptr;
+    size_t ndeps = 0;
+    FFCZ_CUDA(cudaStreamGetCaptureInfo(cs, &st, nullptr, &g, &deps, &edata, &ndeps));
+    cudaGraphConditionalHandle h;
+    FFCZ_CUDA(cudaGraphConditionalHandleCreate(&h, g, 0, 0));
+    k_init_ctl<<<1, 1, 0, cs>>>(s->d_ctl);
+    launch_iteration<T>(s, cs, pro, a, b, tol, max_iter, h, 1, s->profile != 0);
+    FFCZ_CUDA(cudaStreamGetCaptureInfo(cs, &st, nullptr, &g, &deps, &edata, &ndeps));
+    cudaGraphNodeParams cp = {};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t wnode;
+    FFCZ_CUDA(cudaGraphAddNode(&wnode, g, deps, edata, ndeps, &cp));
+    FFCZ_CUDA(cudaStreamUpdateCaptureDependencies(cs, &wnode, nullptr, 1, cudaStreamSetCaptureDependencies));
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    cudaStream_t bs = nullptr;
+    FFCZ_CUDA(cudaStreamCreateWithFlags(&bs, cudaStreamNonBlocking));
+    FFCZ_CUDA(cudaStreamBeginCaptureToGraph(bs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    launch_iteration<T>(s, bs, PRO_CLAMP, nullptr, nullptr, tol, max_iter, h, 1);
+    cudaGraph_t body_out = nullptr;
+    cudaError_t e1 = cudaStreamEndCapture(bs, &body_out);
+    cudaStreamDestroy(bs);
+    FFCZ_CUDA(e1);
+    launch_final<T>(s, cs);
+    FFCZ_CUDA(cudaStreamEndCapture(cs, &s->graph));
+    FFCZ_CUDA(cudaGraphInstantiate(&s->gexec, s->graph, 0));
+    s->gkey = key;
+  }
+  FFCZ_CUDA(cudaGraphLaunch(s->gexec, s->stream));
+  return FFCZ_OK;
+}
+
+template <typename T>
+int run_loop_host(ffcz_solver *s, int pro, const void *a, const void *b, int max_iter, T tol) {
+  k_init_ctl<<<1, 1, 0, s->stream>>>(s->d_ctl);
+  cudaGraphConditionalHandle h = 0;
+  for (int it = 0; it < max_iter; ++it) {
+    launch_iteration<T>(s, s->stream, it == 0 ? pro : PRO_CLAMP, a, b, tol, max_iter, h, 0,
+                        it == 0 && s->profile != 0);
+    FFCZ_CUDA(cudaGetLastError());
+    FFCZ_CUDA(cudaMemcpyAsync(s->h_ctl, s->d_ctl, sizeof(LoopCtl), cudaMemcpyDeviceToHost, s->stream));
+    FFCZ_CUDA(cudaStreamSynchronize(s->stream));
+    if (!s->h_ctl->cont) break;
+  }
+  launch_final<T>(s, s->stream);
+  return FFCZ_OK;
+}
+
+template <typename T>
+int project(ffcz_solver *s, int pro, const void *a, const void *b, int max_iter, double tol_d) {
+  if (!s->initialized) return fail(FFCZ_ERR_NOT_INITIALIZED, "Solver not initialized");
+  const T tol = (T)tol_d;
+  s->pro_last = pro;
+  s->extracted = false;
+  if (max_iter <= 0) {
+    k_init_ctl<<<1, 1, 0, s->stream>>>(s->d_ctl);
+    const unsigned g = (unsigned)std::min<size_t>(ceil_div(s->N, 256), 152 * 16);
+    k_set_e<T><<<g, 256, 0, s->stream>>>(tp<T>(s->d_e), (const T *)a, (const T *)b, (long long)s->N);
+    FFCZ_CUDA(cudaGetLastError());
+    s->launches = 2;
+    return FFCZ_OK;
+  }
+  if (s->loop_driver == FFCZ_LOOP_HOST) {
+    FFCZ_TRY(run_loop_host<T>(s, pro, a, b, max_iter, tol));
+  } else {
+    FFCZ_TRY(run_loop_graph<T>(s, pro, a, b, max_iter, tol));
+  }
+  FFCZ_CUDA(cudaGetLastError());
+  FFCZ_CUDA(cudaMemcpyAsync(s->h_ctl, s->d_ctl, sizeof(LoopCtl), cudaMemcpyDeviceToHost, s->stream));
+  FFCZ_CUDA(cudaStreamSynchronize(s->stream));
+  s->launches = 1 + (long long)s->h_ctl->iterations * s->kernels_per_iter + 1;
+  return FFCZ_OK;
+}
+
+template <typename T>
+int extract_one(ffcz_solver *s, const T *a, size_t n, int which, T *compact, uint16_t *quant, uint8_t *pack,
+                size_t pack_alloc) {
+  const T thr = T(1e-7);
+  const size_t nblk = ceil_div(n, (size_t)EX_CHUNK);
+  cudaStream_t st = s->stream;
+  T *mnmx = (T *)s->d_mnmx + 2 * which;
+  k_ex_stats<T><<<(unsigned)nblk, EX_THREADS, 0, st>>>(a, (long long)n, thr, s->d_blk_cnt, (T *)s->d_blk_mn,
+                                                       (T *)s->d_blk_mx);
+  k_ex_scan<T><<<1, 1024, 0, st>>>(s->d_blk_cnt, (long long)nblk, (const T *)s->d_blk_mn,
+                                   (const T *)s->d_blk_mx, mnmx, s->d_ctl, which);
+  const int correct = s->pack_mode == FFCZ_PACK_CORRECT;
+  k_ex_compact<T><<<(unsigned)nblk, EX_THREADS, 0, st>>>(a, (long long)n, thr, s->d_blk_cnt, mnmx, compact, quant,
+                                                         (unsigned *)pack, correct);
+  s->launches += 3;
+  if (!correct) {
+    const unsigned g = (unsigned)std::min<size_t>(ceil_div(pack_alloc, 256), 152 * 16);
+    k_pack_reference<T><<<g, 256, 0, st>>>(a, (long long)n, thr, pack, (long long)pack_alloc);
+    s->launches += 1;
+  }
+  FFCZ_CUDA(cudaGetLastError());
+  return FFCZ_OK;
+}
+
+template <typename T>
+int extract(ffcz_solver *s) {
+  FFCZ_TRY(extract_one<T>(s, tp<T>(s->d_fedits), 2 * s->H, 0, tp<T>(s->d_fcompact), s->d_fquant, s->d_fpack,
+                          s->fpack_bytes));
+  FFCZ_TRY(extract_one<T>(s, tp<T>(s->d_sedits), s->N, 1, tp<T>(s->d_scompact), s->d_squant, s->d_spack,
+                          s->spack_bytes));
+  FFCZ_CUDA(cudaMemcpyAsync(s->h_ctl, s->d_ctl, sizeof(LoopCtl), cudaMemcpyDeviceToHost, s->stream));
+  FFCZ_CUDA(cudaStreamSynchronize(s->stream));
+  // The reference packs flags only when the stream is non-empty.
+  if (s->pack_mode == FFCZ_PACK_REFERENCE) {
+    if (s->h_ctl->count[0] == 0) FFCZ_CUDA(cudaMemsetAsync(s->d_fpack, 0, s->fpack_bytes, s->stream));
+    if (s->h_ctl->count[1] == 0) FFCZ_CUDA(cudaMemsetAsync(s->d_spack, 0, s->spack_bytes, s->stream));
+  }
+  s->extracted = true;
+  return FFCZ_OK;
+}
+
+void free_all(ffcz_solver *s) {
+  if (s->gexec) cudaGraphExecDestroy(s->gexec);
+  if (s->graph) cudaGraphDestroy(s->graph);
+  void *bufs[] = {s->d_x, s->d_e, s->d_spec, s->d_fedits, s->d_sedits, s->d_fcompact, s->d_scompact,
+                  s->d_fquant, s->d_squant, s->d_fpack, s->d_spack, s->d_tw, s->d_ctl, s->d_blk_cnt,
+                  s->d_blk_mn, s->d_blk_mx, s->d_mnmx};
+  for (void *p : bufs)
+    if (p) cudaFree(p);
+  if (s->h_ctl) cudaFreeHost(s->h_ctl);
+  if (s->cap) cudaStreamDestroy(s->cap);
+  for (cudaEvent_t e : s->ev)
+    if (e) cudaEventDestroy(e);
+}
+
+int check_solver(ffcz_solver *s) { return s ? FFCZ_OK : fail(FFCZ_ERR_INVALID, "solver is NULL"); }
+
+int check_dev_ptr(const void *p, const char *what) {
+  if (!p) return fail(FFCZ_ERR_INVALID, std::string(what) + " is NULL");
+  if (((uintptr_t)p) & 15) return fail(FFCZ_ERR_INVALID, std::string(what) + " must be 16-byte aligned");
+  return FFCZ_OK;
+}
+
+int copy_out(const void *src, size_t bytes, void *dst, size_t cap_bytes, cudaStream_t st) {
+  if (bytes == 0) return FFCZ_OK;
+  if (!dst) return fail(FFCZ_ERR_INVALID, "destination is NULL");
+  if (cap_bytes < bytes) return fail(FFCZ_ERR_CAPACITY, "destination too small");
+  FFCZ_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, st));
+  FFCZ_CUDA(cudaStreamSynchronize(st));
+  return FFCZ_OK;
+}
+
+}  // namespace
+
+#define DISPATCH(s, fn, ...) ((s)->dtype == FFCZ_F32 ? fn<float>(__VA_ARGS__) : fn<double>(__VA_ARGS__))
+
+extern "C" {
+
+int ffcz_solver_create(size_t nx, size_t ny, size_t nz, int dtype, ffcz_solver **out) {
+  if (!out) return fail(FFCZ_ERR_INVALID, "out is NULL");
+  *out = nullptr;
+  if (nx == 0 || ny == 0 || nz == 0) return fail(FFCZ_ERR_INVALID, "dimensions must be positive");
+  if (dtype != FFCZ_F32 && dtype != FFCZ_F64) return fail(FFCZ_ERR_INVALID, "dtype must be FFCZ_F32 or FFCZ_F64");
+  if (nx > (1u << 30) || ny > (1u << 30) || nz > (1u << 30)) return fail(FFCZ_ERR_UNSUPPORTED, "dimension too large");
+  std::unique_ptr<ffcz_solver> s(new ffcz_solver());
+  s->dtype = dtype;
+  s->es = dtype == FFCZ_F32 ? 4 : 8;
+  s->nx = nx;
+  s->ny = ny;
+  s->nz = nz;
+  s->N = nx * ny * nz;
+  s->H = nx * ny * (nz / 2 + 1);
+  if (2 * s->H >= (1ull << 32) || s->N >= (1ull << 32))
+    return fail(FFCZ_ERR_UNSUPPORTED, "more than 2^32 elements per accumulator");
+  FFCZ_CUDA(cudaGetDevice(&s->device));
+  int rc = DISPATCH(s.get(), plan_solver, s.get());
+  if (rc != FFCZ_OK) {
+    free_all(s.get());
+    return rc;
+  }
+  const size_t es = s->es, N = s->N, H2 = 2 * s->H;
+  s->fpack_bytes = round_up(H2, 32) / 8;
+  s->spack_bytes = round_up(N, 32) / 8;
+  s->nblk_max = ceil_div(std::max(H2, N), (size_t)EX_CHUNK);
+  auto alloc = [&](void **p, size_t bytes) -> int {
+    FFCZ_CUDA(cudaMalloc(p, std::max<size_t>(bytes, 16)));
+    return FFCZ_OK;
+  };
+  rc = FFCZ_OK;
+  if (rc == FFCZ_OK) rc = alloc(&s->d_x, N * es);
+  if (rc == FFCZ_OK) rc = alloc(&s->d_e, N * es);
+  if (rc == FFCZ_OK) rc = alloc(&s->d_spec, (size_t)s->rows * s->Hzp * 2 * es);
+  if (rc == FFCZ_OK) rc = alloc(&s->d_fedits, H2 * es);
+  if (rc == FFCZ_OK) rc = alloc(&s->d_sedits, N * es);
+  if (rc == FFCZ_OK) rc = alloc(&s->d_fcompact, H2 * es);
+  if (rc == FFCZ_OK) rc = alloc(&s->d_scompact, N * es);
+  if (rc == FFCZ_OK) rc = alloc((void **)&s->d_fquant, H2 * 2);
+  if (rc == FFCZ_OK) rc = alloc((void **)&s->d_squant, N * 2);
+  if (rc == FFCZ_OK) rc = alloc((void **)&s->d_fpack, s->fpack_bytes);
+  if (rc == FFCZ_OK) rc = alloc((void **)&s->d_spack, s->spack_bytes);
+  if (rc == FFCZ_OK) rc = alloc((void **)&s->d_ctl, sizeof(LoopCtl));
+  if (rc == FFCZ_OK) rc = alloc((void **)&s->d_blk_cnt, s->nblk_max * sizeof(unsigned));
+  if (rc == FFCZ_OK) rc = alloc(&s->d_blk_mn, s->nblk_max * es);
+  if (rc == FFCZ_OK) rc = alloc(&s->d_blk_mx, s->nblk_max * es);
+  if (rc == FFCZ_OK) rc = alloc(&s->d_mnmx, 4 * es);
+  if (rc == FFCZ_OK) {
+    cudaError_t e = cudaMallocHost(&s->h_ctl, sizeof(LoopCtl));
+    if (e != cudaSuccess) rc = cuda_fail(e, "cudaMallocHost", __FILE__, __LINE__);
+  }
+  if (rc == FFCZ_OK) {
+    cudaError_t e = cudaStreamCreateWithFlags(&s->cap, cudaStreamNonBlocking);
+    if (e != cudaSuccess) rc = cuda_fail(e, "cudaStreamCreate", __FILE__, __LINE__);
+  }
+  if (rc == FFCZ_OK) {
+    std::memset(s->h_ctl, 0, sizeof(LoopCtl));
+    cudaError_t e = cudaMemset(s->d_ctl, 0, sizeof(LoopCtl));
+    if (e == cudaSuccess) e = cudaMemset(s->d_fpack, 0, s->fpack_bytes);
+    if (e == cudaSuccess) e = cudaMemset(s->d_spack, 0, s->spack_bytes);
+    if (e == cudaSuccess) e = cudaMemset(s->d_fedits, 0, H2 * es);
+    if (e == cudaSuccess) e = cudaMemset(s->d_sedits, 0, N * es);
+    if (e != cudaSuccess) rc = cuda_fail(e, "cudaMemset", __FILE__, __LINE__);
+  }
+  if (rc != FFCZ_OK) {
+    free_all(s.get());
+    return rc;
+  }
+  *out = s.release();
+  return FFCZ_OK;
+}
+
+int ffcz_solver_destroy(ffcz_solver *s) {
+  if (!s) return FFCZ_OK;
+  cudaStreamSynchronize(s->stream);
+  free_all(s);
+  delete s;
+  return FFCZ_OK;
+}
+
+int ffcz_solver_set_stream(ffcz_solver *s, void *stream) {
+  FFCZ_TRY(check_solver(s));
+  s->stream = (cudaStream_t)stream;
+  return FFCZ_OK;
+}
+
+int ffcz_solver_set_loop_driver(ffcz_solver *s, int driver) {
+  FFCZ_TRY(check_solver(s));
+  if (driver != FFCZ_LOOP_GRAPH && driver != FFCZ_LOOP_HOST) return fail(FFCZ_ERR_INVALID, "unknown loop driver");
+  s->loop_driver = driver;
+  return FFCZ_OK;
+}
+
+int ffcz_solver_set_pack_mode(ffcz_solver *s, int mode) {
+  FFCZ_TRY(check_solver(s));
+  if (mode != FFCZ_PACK_CORRECT && mode != FFCZ_PACK_REFERENCE) return fail(FFCZ_ERR_INVALID, "unknown pack mode");
+  s->pack_mode = mode;
+  return FFCZ_OK;
+}
+
+static int init_common(ffcz_solver *s, const void *src, cudaMemcpyKind kind, double eps, double delta) {
+  FFCZ_TRY(check_solver(s));
+  if (!src) return fail(FFCZ_ERR_INVALID, "original data is NULL");
+  // eps / delta are stored rounded to the solver type (the reference's T
+  // parameters, impl:640-646).
+  s->eps = s->dtype == FFCZ_F32 ? (double)(float)eps : eps;
+  s->delta = s->dtype == FFCZ_F32 ? (double)(float)delta : delta;
+  FFCZ_CUDA(cudaMemcpyAsync(s->d_x, src, s->N * s->es, kind, s->stream));
+  FFCZ_CUDA(cudaStreamSynchronize(s->stream));
+  s->initialized = true;
+  return FFCZ_OK;
+}
+
+int ffcz_init_all_abs(ffcz_solver *s, const void *h_orig, double eps, double delta) {
+  return init_common(s, h_orig, cudaMemcpyHostToDevice, eps, delta);
+}
+int ffcz_init_all_abs_device(ffcz_solver *s, const void *d_orig, double eps, double delta) {
+  return init_common(s, d_orig, cudaMemcpyDeviceToDevice, eps, delta);
+}
+
+int ffcz_project_all_abs_device(ffcz_solver *s, const void *d_err, int max_iter, double tol) {
+  FFCZ_TRY(check_solver(s));
+  FFCZ_TRY(check_dev_ptr(d_err, "initial error"));
+  return DISPATCH(s, project, s, PRO_PLAIN, d_err, nullptr, max_iter, tol);
+}
+
+int ffcz_solve_all_abs_device(ffcz_solver *s, const void *d_err, int max_iter, double tol) {
+  FFCZ_TRY(ffcz_project_all_abs_device(s, d_err, max_iter, tol));
+  return DISPATCH(s, extract, s);
+}
+
+int ffcz_solve_all_abs_pair_device(ffcz_solver *s, const void *d_orig, const void *d_decomp, int max_iter,
+                                   double tol) {
+  FFCZ_TRY(check_solver(s));
+  FFCZ_TRY(check_dev_ptr(d_orig, "original data"));
+  FFCZ_TRY(check_dev_ptr(d_decomp, "decompressed data"));
+  FFCZ_TRY(DISPATCH(s, project, s, PRO_DIFF, d_decomp, d_orig, max_iter, tol));
+  return DISPATCH(s, extract, s);
+}
+
+int ffcz_solve_all_abs(ffcz_solver *s, const void *h_err, int max_iter, double tol) {
+  FFCZ_TRY(check_solver(s));
+  if (!h_err) return fail(FFCZ_ERR_INVALID, "initial error is NULL");
+  if (!s->initialized) return fail(FFCZ_ERR_NOT_INITIALIZED, "Solver not initialized");
+  // e0 is staged in the e buffer (impl:830-831); the first pass reads it.
+  FFCZ_CUDA(cudaMemcpyAsync(s->d_e, h_err, s->N * s->es, cudaMemcpyHostToDevice, s->stream));
+  FFCZ_TRY(DISPATCH(s, project, s, PRO_PLAIN, s->d_e, nullptr, max_iter, tol));
+  return DISPATCH(s, extract, s);
+}
+
+int ffcz_extract(ffcz_solver *s) {
+  FFCZ_TRY(check_solver(s));
+  return DISPATCH(s, extract, s);
+}
+
+int ffcz_reset_edit_accumulators(ffcz_solver *s) {
+  FFCZ_TRY(check_solver(s));
+  FFCZ_CUDA(cudaMemsetAsync(s->d_fedits, 0, 2 * s->H * s->es, s->stream));
+  FFCZ_CUDA(cudaMemsetAsync(s->d_sedits, 0, s->N * s->es, s->stream));
+  FFCZ_CUDA(cudaStreamSynchronize(s->stream));
+  return FFCZ_OK;
+}
+
+int ffcz_solver_synchronize(ffcz_solver *s) {
+  FFCZ_TRY(check_solver(s));
+  FFCZ_CUDA(cudaStreamSynchronize(s->stream));
+  return FFCZ_OK;
+}
+
+int ffcz_get_iterations(ffcz_solver *s, int *iterations) {
+  FFCZ_TRY(check_solver(s));
+  if (!iterations) return fail(FFCZ_ERR_INVALID, "NULL argument");
+  *iterations = s->h_ctl->iterations;
+  return FFCZ_OK;
+}
+
+int ffcz_get_convergence(ffcz_solver *s, double *metric) {
+  FFCZ_TRY(check_solver(s));
+  if (!metric) return fail(FFCZ_ERR_INVALID, "NULL argument");
+  *metric = s->h_ctl->last_viol;
+  return FFCZ_OK;
+}
+
+int ffcz_get_active_counts(ffcz_solver *s, size_t *n_freq, size_t *n_spatial) {
+  FFCZ_TRY(check_solver(s));
+  if (n_freq) *n_freq = s->extracted ? (size_t)s->h_ctl->count[0] : 0;
+  if (n_spatial) *n_spatial = s->extracted ? (size_t)s->h_ctl->count[1] : 0;
+  return FFCZ_OK;
+}
+
+int ffcz_get_minmax(ffcz_solver *s, double *fmin, double *fmax, double *smin, double *smax) {
+  FFCZ_TRY(check_solver(s));
+  if (fmin) *fmin = s->h_ctl->mn[0];
+  if (fmax) *fmax = s->h_ctl->mx[0];
+  if (smin) *smin = s->h_ctl->mn[1];
+  if (smax) *smax = s->h_ctl->mx[1];
+  return FFCZ_OK;
+}
+
+int ffcz_get_results(ffcz_solver *s, void *h_err) {
+  FFCZ_TRY(check_solver(s));
+  return copy_out(s->d_e, s->N * s->es, h_err, s->N * s->es, s->stream);
+}
+
+int ffcz_get_freq_edits_full(ffcz_solver *s, void *dst, size_t cap_elems) {
+  FFCZ_TRY(check_solver(s));
+  return copy_out(s->d_fedits, 2 * s->H * s->es, dst, cap_elems * s->es, s->stream);
+}
+
+int ffcz_get_spatial_edits_full(ffcz_solver *s, void *dst, size_t cap_elems) {
+  FFCZ_TRY(check_solver(s));
+  return copy_out(s->d_sedits, s->N * s->es, dst, cap_elems * s->es, s->stream);
+}
+
+static int get_stream(ffcz_solver *s, const void *src, size_t count, size_t esz, void *dst, size_t cap,
+                      size_t *len) {
+  FFCZ_TRY(check_solver(s));
+  if (len) *len = count;
+  if (count == 0) return FFCZ_OK;
+  return copy_out(src, count * esz, dst, cap * esz, s->stream);
+}
+
+int ffcz_get_freq_quant(ffcz_solver *s, uint16_t *dst, size_t cap, size_t *len) {
+  FFCZ_TRY(check_solver(s));
+  return get_stream(s, s->d_fquant, s->extracted ? s->h_ctl->count[0] : 0, 2, dst, cap, len);
+}
+int ffcz_get_spatial_quant(ffcz_solver *s, uint16_t *dst, size_t cap, size_t *len) {
+  FFCZ_TRY(check_solver(s));
+  return get_stream(s, s->d_squant, s->extracted ? s->h_ctl->count[1] : 0, 2, dst, cap, len);
+}
+int ffcz_get_freq_compact(ffcz_solver *s, void *dst, size_t cap, size_t *len) {
+  FFCZ_TRY(check_solver(s));
+  return get_stream(s, s->d_fcompact, s->extracted ? s->h_ctl->count[0] : 0, s->es, dst, cap, len);
+}
+int ffcz_get_spatial_compact(ffcz_solver *s, void *dst, size_t cap, size_t *len) {
+  FFCZ_TRY(check_solver(s));
+  return get_stream(s, s->d_scompact, s->extracted ? s->h_ctl->count[1] : 0, s->es, dst, cap, len);
+}
+int ffcz_get_freq_flags_pack(ffcz_solver *s, uint8_t *dst, size_t cap, size_t *len) {
+  FFCZ_TRY(check_solver(s));
+  return get_stream(s, s->d_fpack, (2 * s->H + 7) / 8, 1, dst, cap, len);
+}
+int ffcz_get_spatial_flags_pack(ffcz_solver *s, uint8_t *dst, size_t cap, size_t *len) {
+  FFCZ_TRY(check_solver(s));
+  return get_stream(s, s->d_spack, (s->N + 7) / 8, 1, dst, cap, len);
+}
+
+static int unpack_flags(ffcz_solver *s, const void *edits, size_t n, uint8_t *dst, size_t cap, size_t *len) {
+  // One byte per flag, recomputed from the accumulator with the extraction
+  // threshold (impl:384-398): identical to the correct pack's bits.
+  if (len) *len = n;
+  if (!dst) return fail(FFCZ_ERR_INVALID, "destination is NULL");
+  if (cap < n) return fail(FFCZ_ERR_CAPACITY, "destination too small");
+  std::vector<uint8_t> raw(n * s->es);
+  FFCZ_TRY(copy_out(edits, n * s->es, raw.data(), raw.size(), s->stream));
+  if (s->dtype == FFCZ_F32) {
+    const float *v = (const float *)raw.data();
+    for (size_t i = 0; i < n; ++i) dst[i] = std::fabs(v[i]) > 1e-7f;
+  } else {
+    const double *v = (const double *)raw.data();
+    for (size_t i = 0; i < n; ++i) dst[i] = std::fabs(v[i]) > 1e-7;
+  }
+  return FFCZ_OK;
+}
+
+int ffcz_get_freq_flags(ffcz_solver *s, uint8_t *dst, size_t cap, size_t *len) {
+  FFCZ_TRY(check_solver(s));
+  return unpack_flags(s, s->d_fedits, 2 * s->H, dst, cap, len);
+}
+int ffcz_get_spatial_flags(ffcz_solver *s, uint8_t *dst, size_t cap, size_t *len) {
+  FFCZ_TRY(check_solver(s));
+  return unpack_flags(s, s->d_sedits, s->N, dst, cap, len);
+}
+
+int ffcz_get_device_array(ffcz_solver *s, int which, void **dptr, size_t *bytes) {
+  FFCZ_TRY(check_solver(s));
+  if (!dptr) return fail(FFCZ_ERR_INVALID, "NULL argument");
+  const size_t es = s->es, N = s->N, H2 = 2 * s->H;
+  const size_t cf = s->extracted ? s->h_ctl->count[0] : 0, cs = s->extracted ? s->h_ctl->count[1] : 0;
+  void *p = nullptr;
+  size_t b = 0;
+  switch (which) {
+    case 0: p = s->d_e; b = N * es; break;
+    case 1: p = s->d_fedits; b = H2 * es; break;
+    case 2: p = s->d_sedits; b = N * es; break;
+    case 3: p = s->d_fquant; b = cf * 2; break;
+    case 4: p = s->d_squant; b = cs * 2; break;
+    case 5: p = s->d_fpack; b = (H2 + 7) / 8; break;
+    case 6: p = s->d_spack; b = (N + 7) / 8; break;
+    case 7: p = s->d_fcompact; b = cf * es; break;
+    case 8: p = s->d_scompact; b = cs * es; break;
+    default: return fail(FFCZ_ERR_INVALID, "unknown array");
+  }
+  *dptr = p;
+  if (bytes) *bytes = b;
+  return FFCZ_OK;
+}
+
+int ffcz_get_sizes(ffcz_solver *s, size_t *n, size_t *h) {
+  FFCZ_TRY(check_solver(s));
+  if (n) *n = s->N;
+  if (h) *h = s->H;
+  return FFCZ_OK;
+}
+
+int ffcz_get_launch_count(ffcz_solver *s, long long *launches) {
+  FFCZ_TRY(check_solver(s));
+  if (!launches) return fail(FFCZ_ERR_INVALID, "NULL argument");
+  *launches = s->launches;
+  return FFCZ_OK;
+}
+
+int ffcz_solver_set_profiling(ffcz_solver *s, int on) {
+  FFCZ_TRY(check_solver(s));
+  if (on && !s->ev[0])
+    for (cudaEvent_t &e : s->ev) FFCZ_CUDA(cudaEventCreate(&e));
+  s->profile = on ? 1 : 0;
+  return FFCZ_OK;
+}
+
+int ffcz_get_pass_times(ffcz_solver *s, double *ms, double *bytes, int cap, int *npass) {
+  FFCZ_TRY(check_solver(s));
+  if (!npass) return fail(FFCZ_ERR_INVALID, "NULL argument");
+  if (!s->profile || s->npass == 0) return fail(FFCZ_ERR_INVALID, "profiling is off or no solve ran");
+  *npass = s->npass;
+  if (cap < s->npass || !ms || !bytes) return fail(FFCZ_ERR_CAPACITY, "destination too small");
+  FFCZ_CUDA(cudaEventSynchronize(s->ev[s->npass]));
+  const double es = (double)s->es, N = (double)s->N, H = (double)s->H;
+  for (int i = 0; i < s->npass; ++i) {
+    float t = 0.f;
+    FFCZ_CUDA(cudaEventElapsedTime(&t, s->ev[i], s->ev[i + 1]));
+    ms[i] = t;
+    // algorithmic bytes: one read and one write of the data the pass maps
+    if (i == 0) bytes[i] = N * es * (s->pro_last == PRO_DIFF ? 2.0 : 1.0) + 2.0 * H * es;
+    else if (i == s->npass - 1) bytes[i] = 2.0 * H * es + N * es;
+    else bytes[i] = 4.0 * H * es;
+  }
+  return FFCZ_OK;
+}
+
+int ffcz_solver_encode(ffcz_solver *s, int zstd_level, int zstd_mode, ffcz_huff_result **out4) {
+  FFCZ_TRY(check_solver(s));
+  if (!out4) return fail(FFCZ_ERR_INVALID, "out4 is NULL");
+  for (int i = 0; i < 4; ++i) out4[i] = nullptr;
+  if (!s->extracted) return fail(FFCZ_ERR_INVALID, "extract before encode");
+  const size_t cf = s->h_ctl->count[0], cs = s->h_ctl->count[1];
+  struct Job { const void *d; size_t n; int sb; };
+  Job jobs[4] = {{s->d_fquant, cf, 2}, {s->d_fpack, cf ? (2 * s->H + 7) / 8 : 0, 1},
+                 {s->d_squant, cs, 2}, {s->d_spack, cs ? (s->N + 7) / 8 : 0, 1}};
+  std::unique_ptr<ffcz_huff_result> res[4];
+  std::vector<std::future<int>> z;
+  long long launches = 0;
+  for (int i = 0; i < 4; ++i) {
+    if (jobs[i].n == 0) continue;
+    res[i].reset(new ffcz_huff_result());
+    FFCZ_TRY(huff_encode_device(s->huff, jobs[i].d, jobs[i].n, jobs[i].sb, s->stream, *res[i]));
+    launches += s->huff.launches;
+    ffcz_huff_result *r = res[i].get();
+    z.push_back(std::async(std::launch::async, [r, zstd_level, zstd_mode] { return huff_zstd(*r, zstd_level, zstd_mode); }));
+  }
+  int rc = FFCZ_OK;
+  for (auto &f : z) {
+    const int r = f.get();
+    if (rc == FFCZ_OK) rc = r;
+  }
+  if (rc != FFCZ_OK) return rc;
+  s->launches += launches;
+  for (int i = 0; i < 4; ++i) out4[i] = res[i].release();
+  return FFCZ_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,256 @@
+/*
+ * ffcz.h -- C ABI of the GB300 (sm_103a) FFCz corrector and edit encoder.
+ *
+ * Every entry point is extern "C", takes plain pointers and sizes, and
+ * returns an int status (FFCZ_OK == 0, negative on failure).  The message of
+ * the last failure on the calling thread is available from
+ * ffcz_last_error().  Nothing here prints or exits the process; the C++
+ * drop-in headers (projection_algorithm.cuh, HuffmanZSTDCoder.cuh) turn the
+ * status codes back into the reference's behaviour (print + exit(1) for CUDA
+ * errors, std::runtime_error for usage errors).
+ *
+ * Reference interface replaced by each group is cited as file:line of the
+ * FFCz sources (projection_algorithm.cuh, projection_algorithm_impl.cuh,
+ * projection_algorithm.cu, HuffmanZSTDCoder.cuh, fileIO.h).
+ *
+ * Array layouts (identical to the reference):
+ *   spatial arrays   : Nx*Ny*Nz values of T, C order, z fastest.
+ *   spectrum index k : (ix*Ny + iy)*(Nz/2+1) + kz, the unnormalised R2C
+ *                      half spectrum of cufftPlan3d(Nx,Ny,Nz).
+ *   frequency edits  : planar, 2*H values of T: [Re(0..H-1) | Im(0..H-1)],
+ *                      H = Nx*Ny*(Nz/2+1).
+ *   flag packs       : LSB-first bit i of byte b = flag of element 8b+i.
+ *   Huffman streams  : MSB-first bitstream, zero padded to whole bytes.
+ */
+#ifndef FFCZ_H
+#define FFCZ_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define FFCZ_OK                   0
+#define FFCZ_ERR_INVALID         -1  /* bad argument / usage error            */
+#define FFCZ_ERR_CUDA            -2  /* a CUDA runtime call failed            */
+#define FFCZ_ERR_UNSUPPORTED     -3  /* size or mode not supported            */
+#define FFCZ_ERR_NOT_INITIALIZED -4  /* solve before initialize (impl:822)    */
+#define FFCZ_ERR_ZSTD            -5  /* libzstd missing or ZSTD error         */
+#define FFCZ_ERR_CAPACITY        -6  /* caller buffer too small               */
+#define FFCZ_ERR_CODE_TOO_LONG   -7  /* Huffman code longer than 32 bits      */
+#define FFCZ_ERR_EMPTY           -8  /* empty input (HuffmanZSTDCoder:250)    */
+#define FFCZ_ERR_IO              -9  /* file I/O failure (fileIO.cpp)         */
+
+/* ---- element types ----------------------------------------------------- */
+#define FFCZ_F32 0
+#define FFCZ_F64 1
+
+/* ---- flag-pack modes ---------------------------------------------------- */
+/* Correct LSB-first packing of every flag (default). */
+#define FFCZ_PACK_CORRECT   0
+/* Reproduces projection_algorithm.cu:382-405 as launched by
+ * projection_algorithm_impl.cuh:429-449: only the first ceil(nbytes/8) bytes
+ * are written and they hold flags [0, nbytes); the remaining bytes, which the
+ * reference leaves uninitialised, are zero. */
+#define FFCZ_PACK_REFERENCE 1
+
+/* ---- loop drivers --------------------------------------------------------- */
+/* Whole iteration loop inside one CUDA graph with a device-side WHILE node. */
+#define FFCZ_LOOP_GRAPH 0
+/* Host-driven loop, one 8-byte device->host read per iteration (the
+ * reference's structure, impl:835-852).  Same kernels, same results. */
+#define FFCZ_LOOP_HOST  1
+
+const char *ffcz_last_error(void);
+const char *ffcz_version(void);
+
+/* ======================================================================== *
+ * Solver (replaces template<class T> class ProjectionSolver,               *
+ * projection_algorithm.cuh:238-333, implemented in                        *
+ * projection_algorithm_impl.cuh:1-910)                                     *
+ * ======================================================================== */
+typedef struct ffcz_solver ffcz_solver;
+
+/* ProjectionSolver(Nx,Ny,Nz) -- impl:4-18 (allocation impl:27-61, plans
+ * impl:109-122, accumulators zeroed impl:133-147). dtype = FFCZ_F32/F64. */
+int ffcz_solver_create(size_t nx, size_t ny, size_t nz, int dtype,
+                       ffcz_solver **out);
+/* ~ProjectionSolver -- impl:20-25. NULL is accepted. */
+int ffcz_solver_destroy(ffcz_solver *s);
+/* Stream the solver launches on (cudaStream_t as void*; NULL = legacy
+ * default stream, like the reference). */
+int ffcz_solver_set_stream(ffcz_solver *s, void *stream);
+/* FFCZ_LOOP_GRAPH (default) or FFCZ_LOOP_HOST. */
+int ffcz_solver_set_loop_driver(ffcz_solver *s, int driver);
+/* FFCZ_PACK_CORRECT (default) or FFCZ_PACK_REFERENCE. */
+int ffcz_solver_set_pack_mode(ffcz_solver *s, int mode);
+
+/* initialize_all_abs(h_orig, eps, delta) -- impl:639-668.  x is a host
+ * array of Nx*Ny*Nz elements of the solver's dtype; eps and delta are
+ * converted to the solver's dtype. */
+int ffcz_init_all_abs(ffcz_solver *s, const void *h_orig, double eps,
+                      double delta);
+/* Same, x already resident on the device. */
+int ffcz_init_all_abs_device(ffcz_solver *s, const void *d_orig, double eps,
+                             double delta);
+
+/* solve_all_abs(h_err, max_iter, tol) -- impl:816-858: copies the initial
+ * error e0 = x' - x from the host, runs the alternating projections and the
+ * compaction (extract_compact_representation, impl:371-456).  tol is
+ * converted to the solver's dtype. Does not print. */
+int ffcz_solve_all_abs(ffcz_solver *s, const void *h_err, int max_iter,
+                       double tol);
+/* Same, e0 resident on the device (d_err is read, not modified). */
+int ffcz_solve_all_abs_device(ffcz_solver *s, const void *d_err,
+                              int max_iter, double tol);
+/* Device-resident pair: e0 = x' - x is formed inside the first forward
+ * pass (the subtraction projection_example.cu:173-176 does on the host).
+ * d_orig must be the array given to the initialiser; it is not re-read. */
+int ffcz_solve_all_abs_pair_device(ffcz_solver *s, const void *d_orig,
+                                   const void *d_decomp, int max_iter,
+                                   double tol);
+/* Projection loop only, without the compaction (impl:835-852). */
+int ffcz_project_all_abs_device(ffcz_solver *s, const void *d_err,
+                                int max_iter, double tol);
+/* extract_compact_representation() -- impl:371-456 (flags, whole-array
+ * min/max, scan, compaction, uint16 quantisation, flag packs). */
+int ffcz_extract(ffcz_solver *s);
+/* reset_edit_accumulators() -- impl:133-147. */
+int ffcz_reset_edit_accumulators(ffcz_solver *s);
+/* Waits for the solver's stream. */
+int ffcz_solver_synchronize(ffcz_solver *s);
+
+/* ---- results (impl:458-595, 904-910) ------------------------------------ */
+/* iterations (impl:843), last convergence metric (impl:842) as double. */
+int ffcz_get_iterations(ffcz_solver *s, int *iterations);
+int ffcz_get_convergence(ffcz_solver *s, double *metric);
+/* h_num_active_freq / h_num_active_spatial (impl:412, 424). */
+int ffcz_get_active_counts(ffcz_solver *s, size_t *n_freq, size_t *n_spatial);
+/* get_min/max_freq/spatial_edit (impl:573-595); values as double. */
+int ffcz_get_minmax(ffcz_solver *s, double *fmin, double *fmax,
+                    double *smin, double *smax);
+/* get_results(h_err) -- impl:904-910: the corrected error e (x^ = x + e). */
+int ffcz_get_results(ffcz_solver *s, void *h_err);
+/* get_freq_edits_full / get_spatial_edits_full -- impl:555-571. */
+int ffcz_get_freq_edits_full(ffcz_solver *s, void *dst, size_t cap_elems);
+int ffcz_get_spatial_edits_full(ffcz_solver *s, void *dst, size_t cap_elems);
+/* get_active_*_quant_edit_distances -- impl:507-529 (uint16). */
+int ffcz_get_freq_quant(ffcz_solver *s, uint16_t *dst, size_t cap,
+                        size_t *len);
+int ffcz_get_spatial_quant(ffcz_solver *s, uint16_t *dst, size_t cap,
+                           size_t *len);
+/* get_active_*_edit_distances -- impl:531-553 (T). */
+int ffcz_get_freq_compact(ffcz_solver *s, void *dst, size_t cap, size_t *len);
+int ffcz_get_spatial_compact(ffcz_solver *s, void *dst, size_t cap,
+                             size_t *len);
+/* get_*_flags_pack -- impl:487-505; length is ceil(n/8) bytes. */
+int ffcz_get_freq_flags_pack(ffcz_solver *s, uint8_t *dst, size_t cap,
+                             size_t *len);
+int ffcz_get_spatial_flags_pack(ffcz_solver *s, uint8_t *dst, size_t cap,
+                                size_t *len);
+/* get_freq_flags / get_spatial_flags -- impl:459-485, one byte per flag. */
+int ffcz_get_freq_flags(ffcz_solver *s, uint8_t *dst, size_t cap,
+                        size_t *len);
+int ffcz_get_spatial_flags(ffcz_solver *s, uint8_t *dst, size_t cap,
+                           size_t *len);
+/* Device pointers of the solver-owned arrays (for zero-copy callers):
+ * which = 0 e, 1 freq_edits, 2 spatial_edits, 3 freq quant, 4 spatial
+ * quant, 5 freq pack, 6 spatial pack, 7 freq compact, 8 spatial compact. */
+int ffcz_get_device_array(ffcz_solver *s, int which, void **dptr,
+                          size_t *bytes);
+/* Sizes: n = Nx*Ny*Nz, h = Nx*Ny*(Nz/2+1). */
+int ffcz_get_sizes(ffcz_solver *s, size_t *n, size_t *h);
+/* Kernel launches issued since the last solve started (projection loop,
+ * compaction and any encode of its streams). */
+int ffcz_get_launch_count(ffcz_solver *s, long long *launches);
+/* Per-pass timing: when on, CUDA events are recorded around each pass of
+ * the first iteration of every solve (inside the captured graph).
+ * ffcz_get_pass_times returns, for the last solve, each pass's elapsed ms
+ * and its algorithmic bytes (one read + one write of the data it maps):
+ * order z-forward, [y-forward], fused axis or clamp, [y-inverse],
+ * z-inverse. */
+int ffcz_solver_set_profiling(ffcz_solver *s, int on);
+int ffcz_get_pass_times(ffcz_solver *s, double *ms, double *bytes, int cap,
+                        int *npass);
+
+/* ======================================================================== *
+ * Huffman + ZSTD coder (replaces SimpleCudaHuffmanZstdCompressor<T>,       *
+ * HuffmanZSTDCoder.cuh:236-451, cudaHuffmanZstdCompress/Decompress :454-470)*
+ * ======================================================================== */
+typedef struct ffcz_huff_result ffcz_huff_result;
+
+/* ZSTD framing of the Huffman bitstream. */
+#define FFCZ_ZSTD_SINGLE 0   /* one ZSTD_compress call (reference :359-375) */
+#define FFCZ_ZSTD_CHUNKED 1  /* independent frames over host threads; the  */
+                             /* concatenation decodes with ZSTD_decompress */
+
+/* compress(data, level) for T = uint16_t / uint8_t from HOST data --
+ * HuffmanZSTDCoder.cuh:248-376.  Histogram, code lengths, bit offsets and
+ * bit packing run on the GPU; the codebook (:85-178) and ZSTD on the host. */
+int ffcz_huff_compress_u16(const uint16_t *h_data, size_t n, int zstd_level,
+                           ffcz_huff_result **out);
+int ffcz_huff_compress_u8(const uint8_t *h_data, size_t n, int zstd_level,
+                          ffcz_huff_result **out);
+/* Same from DEVICE data, with the ZSTD framing mode and a stream. */
+int ffcz_huff_compress_device(const void *d_data, size_t n, int symbol_bytes,
+                              int zstd_level, int zstd_mode, void *stream,
+                              ffcz_huff_result **out);
+/* Huffman bitstream only, no ZSTD (ZSTD level < 0 means the same). */
+void ffcz_huff_result_free(ffcz_huff_result *r);
+/* CompressionResult fields (:240-246). */
+int ffcz_huff_result_sizes(const ffcz_huff_result *r, size_t *compressed_bytes,
+                           size_t *bitstream_bytes, size_t *num_elements,
+                           size_t *num_symbols);
+int ffcz_huff_result_compressed(const ffcz_huff_result *r, uint8_t *dst,
+                                size_t cap);
+/* The uncompressed Huffman bitstream (before ZSTD). */
+int ffcz_huff_result_bitstream(const ffcz_huff_result *r, uint8_t *dst,
+                               size_t cap);
+/* Code table as three parallel arrays in ascending symbol order. */
+int ffcz_huff_result_codes(const ffcz_huff_result *r, uint32_t *symbols,
+                           uint32_t *codes, int32_t *lengths, size_t cap);
+
+/* decompress(...) -- HuffmanZSTDCoder.cuh:378-450: ZSTD_decompress, then a
+ * prefix decode with the same stop and bit-skip rules.  out must hold
+ * num_elements symbols; *out_len receives the decoded count. */
+int ffcz_huff_decompress_u16(const uint8_t *comp, size_t comp_len,
+                             const uint32_t *symbols, const uint32_t *codes,
+                             const int32_t *lengths, size_t num_symbols,
+                             size_t num_elements, size_t bitstream_bytes,
+                             uint16_t *out, size_t *out_len);
+int ffcz_huff_decompress_u8(const uint8_t *comp, size_t comp_len,
+                            const uint32_t *symbols, const uint32_t *codes,
+                            const int32_t *lengths, size_t num_symbols,
+                            size_t num_elements, size_t bitstream_bytes,
+                            uint8_t *out, size_t *out_len);
+
+/* Encode the solver's four streams the way projection_example.cu:230-246
+ * does (frequency quantised edits, frequency flag pack, spatial quantised
+ * edits, spatial flag pack; a pair only when its count is non-zero).
+ * out[4] receives results or NULL for skipped streams; the caller frees. */
+int ffcz_solver_encode(ffcz_solver *s, int zstd_level, int zstd_mode,
+                       ffcz_huff_result **out4);
+
+/* ======================================================================== *
+ * File formats (fileIO.h:17-55, fileIO.cpp:3-85)                           *
+ * ======================================================================== */
+/* readRawArrayBinary -- fileIO.cpp:35-76: headerless array; the file size
+ * must equal n*elem_bytes exactly. */
+int ffcz_read_raw(const char *path, void *dst, size_t n, size_t elem_bytes);
+/* writeRawArrayBinary / writeVectorBinary -- fileIO.h:23-55. */
+int ffcz_write_raw(const char *path, const void *src, size_t n,
+                   size_t elem_bytes);
+/* writeMap / readMap -- fileIO.cpp:3-33: size_t n, then n x (int key,
+ * uint32 code, int len), keys ascending. */
+int ffcz_write_map(const char *path, const int32_t *keys,
+                   const uint32_t *codes, const int32_t *lens, size_t n);
+int ffcz_read_map(const char *path, int32_t *keys, uint32_t *codes,
+                  int32_t *lens, size_t cap, size_t *n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FFCZ_H */

@@ -1,0 +1,94 @@
+"""C ABI checks that need no GPU: the library loads, exports every entry
+point include/ffcz.h declares, and its host-only entry points (file
+formats, Huffman+ZSTD decode) agree with the reference / oracle."""
+import ctypes
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import ffcz_gb300 as F
+from oracle import ffcz_oracle as O
+
+HEADER = Path(__file__).resolve().parents[1] / "include" / "ffcz.h"
+
+
+def declared_functions():
+    text = HEADER.read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(ffcz_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_symbol():
+    lib = F.lib()
+    names = declared_functions()
+    assert len(names) >= 45
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+    assert set(names) == set(F.SIGNATURES), set(names) ^ set(F.SIGNATURES)
+
+
+def test_version_and_errors():
+    assert "sm_103a" in F.version()
+    with pytest.raises(F.FFCzError):
+        F.read_raw_array_binary("/nonexistent/file.bin", 4, np.float32)
+
+
+def test_raw_roundtrip_and_size_check(tmp_path):
+    a = np.arange(37, dtype=np.float32) * 0.5
+    p = tmp_path / "a.bin"
+    F.write_raw_array_binary(a, p)
+    assert p.read_bytes() == a.tobytes()  # headerless little-endian
+    assert np.array_equal(F.read_raw_array_binary(p, 37, np.float32), a)
+    with pytest.raises(F.FFCzError) as ei:
+        F.read_raw_array_binary(p, 36, np.float32)
+    assert "File size does not match array size" in str(ei.value)
+
+
+def test_map_bytes_equal_reference_writeMap(golden_huffman, tmp_path):
+    g = golden_huffman["geometric"]
+    m = {int(s): (int(c), int(l)) for s, c, l in zip(g["ref_sym"], g["ref_code"], g["ref_len"])}
+    p = tmp_path / "t.map"
+    F.write_map(m, p)
+    assert p.read_bytes() == g["ref_map_bytes"].tobytes()
+    assert F.read_map(p) == m
+
+
+def test_decompress_golden_through_cabi(golden_huffman):
+    """ffcz_huff_decompress_* (host side of the coder) on the reference's code
+    tables and the oracle's bitstreams, ZSTD-framed by libzstd."""
+    for name, g in golden_huffman.items():
+        sym = g["symbols"]
+        book = O.huffman_codebook(sym)
+        bits, _ = O.huffman_bitstream(sym, book)
+        comp = O.zstd_compress(bits, 19)
+        table = {int(s): (int(c), int(l)) for s, c, l in zip(g["ref_sym"], g["ref_code"], g["ref_len"])}
+        dec = F.cuda_huffman_zstd_decompress(comp, table, sym.size, len(bits), sym.dtype)
+        assert np.array_equal(dec, sym), name
+
+
+def test_decompress_skip_rule_and_truncation():
+    table = {9: (0, 1)}
+    comp = O.zstd_compress(bytes([0b10100000]), 3)
+    dec = F.cuda_huffman_zstd_decompress(comp, table, 3, 1, np.uint16)
+    assert list(dec) == [9, 9, 9]
+    # fewer bits than elements: decoding stops at the end of the stream
+    dec = F.cuda_huffman_zstd_decompress(O.zstd_compress(bytes([0xFF]), 3), {1: (1, 1)}, 20, 1, np.uint8)
+    assert list(dec) == [1] * 8
+
+
+def test_zstd_error_reported():
+    with pytest.raises(F.FFCzError) as ei:
+        F.cuda_huffman_zstd_decompress(b"not a zstd frame", {1: (0, 1)}, 4, 4, np.uint8)
+    assert ei.value.code == -5
+
+
+def test_solver_create_without_gpu_fails_cleanly():
+    import torch
+
+    if torch.cuda.is_available():
+        pytest.skip("GPU present")
+    with pytest.raises(F.FFCzError) as ei:
+        F.ProjectionSolver(8, 8, 8)
+    assert ei.value.code == -2
