@@ -111,6 +111,8 @@ SIGNATURES = {
     "ffcz_huff_decompress_u16": [_p, _sz, _p, _p, _p, _sz, _sz, _sz, _p, _SP],
     "ffcz_huff_decompress_u8": [_p, _sz, _p, _p, _p, _sz, _sz, _sz, _p, _SP],
     "ffcz_solver_encode": [_p, _i, _i, C.POINTER(C.c_void_p * 4)],
+    "ffcz_compact_quantize_noalloc": [_p, _sz, _i, _p, _p, _p, _i, _p, _SP, C.POINTER(C.c_double),
+                                      C.POINTER(C.c_double)],
     "ffcz_read_raw": [C.c_char_p, _p, _sz, _sz],
     "ffcz_write_raw": [C.c_char_p, _p, _sz, _sz],
     "ffcz_write_map": [C.c_char_p, _p, _p, _p, _sz],

@@ -235,6 +235,37 @@ int ffcz_solver_encode(ffcz_solver *s, int zstd_level, int zstd_mode,
                        ffcz_huff_result **out4);
 
 /* ======================================================================== *
+ * Allocation-free compaction                                               *
+ * ======================================================================== */
+/* No counterpart in the reference.  The compaction of one edit accumulator
+ * (what ffcz_extract does per array: flags |v| > 1e-7, whole-array min and
+ * max, scatter of the active values, their uint16 codes and the flag pack)
+ * for callers that cannot allocate device memory: applications that
+ * reserve the GPU's memory up front in their own pool and forbid further
+ * device allocations, and latency-bound pipelines that cannot afford the
+ * implicit device synchronisation of cudaMalloc/cudaFree.  It calls no
+ * allocator; its scratch is a fixed FFCZ_NOALLOC_SCRATCH_BYTES device array
+ * inside the library, held by every GPU that loads it until process exit.
+ *   d_edits   : n values of dtype (FFCZ_F32 / FFCZ_F64), device memory;
+ *               n <= FFCZ_NOALLOC_MAX_ELEMS, else FFCZ_ERR_CAPACITY.
+ *   d_compact : room for n values of dtype; receives the active values.
+ *   d_quant   : room for n uint16; receives their codes.
+ *   d_pack    : 4-byte aligned, room for 4*ceil(n/32) bytes; receives the
+ *               flag pack (FFCZ_PACK_CORRECT or FFCZ_PACK_REFERENCE).
+ *   count, min_edit, max_edit : host outputs (min/max may be NULL).
+ * The call runs on `stream` and returns after it finished.  The first call
+ * on a device (with that device current) resolves the scratch array's
+ * device address; make it before any stream capture.  All calls on a device
+ * share the scratch, so calls that overlap on the GPU race. */
+#define FFCZ_NOALLOC_MAX_ELEMS 67108864u      /* 16384 blocks of 4096 values */
+#define FFCZ_NOALLOC_SCRATCH_BYTES 328192u
+int ffcz_compact_quantize_noalloc(const void *d_edits, size_t n, int dtype,
+                                  void *d_compact, uint16_t *d_quant,
+                                  uint8_t *d_pack, int pack_mode,
+                                  void *stream, size_t *count,
+                                  double *min_edit, double *max_edit);
+
+/* ======================================================================== *
  * File formats (fileIO.h:17-55, fileIO.cpp:3-85)                           *
  * ======================================================================== */
 /* readRawArrayBinary -- fileIO.cpp:35-76: headerless array; the file size
