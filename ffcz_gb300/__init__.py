@@ -111,6 +111,8 @@ SIGNATURES = {
     "ffcz_huff_decompress_u16": [_p, _sz, _p, _p, _p, _sz, _sz, _sz, _p, _SP],
     "ffcz_huff_decompress_u8": [_p, _sz, _p, _p, _p, _sz, _sz, _sz, _p, _SP],
     "ffcz_solver_encode": [_p, _i, _i, C.POINTER(C.c_void_p * 4)],
+    "ffcz_zstd_bound": [_sz],
+    "ffcz_zstd_compress": [_p, _sz, _i, _i, _p, _sz, _SP],
     "ffcz_compact_quantize_noalloc": [_p, _sz, _i, _p, _p, _p, _i, _p, _SP, C.POINTER(C.c_double),
                                       C.POINTER(C.c_double)],
     "ffcz_read_raw": [C.c_char_p, _p, _sz, _sz],
@@ -120,7 +122,8 @@ SIGNATURES = {
     "ffcz_last_error": [],
     "ffcz_version": [],
 }
-_RET = {"ffcz_last_error": C.c_char_p, "ffcz_version": C.c_char_p, "ffcz_huff_result_free": None}
+_RET = {"ffcz_last_error": C.c_char_p, "ffcz_version": C.c_char_p, "ffcz_huff_result_free": None,
+        "ffcz_zstd_bound": C.c_size_t}
 
 
 def _declare(L: C.CDLL) -> None:
@@ -393,6 +396,18 @@ def cuda_huffman_zstd_compress_device(d_data, n: int, symbol_bytes: int, zstd_le
     _check(lib().ffcz_huff_compress_device(_dev_ptr(d_data), n, symbol_bytes, zstd_level, zstd_mode,
                                             C.c_void_p(sp), C.byref(out)))
     return _take_result(out.value)
+
+
+def zstd_compress(data: bytes, level: int, mode: int = FFCZ_ZSTD_SINGLE) -> bytes:
+    """The coder's ZSTD stage on host bytes (native; releases the GIL)."""
+    src = np.frombuffer(data, np.uint8) if len(data) else np.zeros(1, np.uint8)
+    cap = lib().ffcz_zstd_bound(len(data))
+    if cap == 0:
+        raise FFCzError(-5, "libzstd.so.1 not available")
+    dst = np.empty(cap, np.uint8)
+    n = C.c_size_t()
+    _check(lib().ffcz_zstd_compress(_np_ptr(src), len(data), int(level), int(mode), _np_ptr(dst), cap, C.byref(n)))
+    return bytes(dst[: n.value])
 
 
 def cuda_huffman_zstd_decompress(compressed: bytes, code_table: dict, num_elements: int,

@@ -18,7 +18,7 @@ ROOT = PKG.parent
 CSRC = PKG / "csrc"
 OUT = PKG / "_build"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-LIB_SOURCES = ["solver.cu", "huffman.cu", "legacy_kernels.cu", "noalloc.cu", "fft_plan.cpp",
+LIB_SOURCES = ["solver.cu", "static_kernels.cu", "huffman.cu", "legacy_kernels.cu", "noalloc.cu", "fft_plan.cpp",
                "huffman_host.cpp", "capi_misc.cpp"]
 
 

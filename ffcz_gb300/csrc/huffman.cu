@@ -409,6 +409,19 @@ int ffcz_huff_compress_device(const void *d_data, size_t n, int symbol_bytes, in
 }
 void ffcz_huff_result_free(ffcz_huff_result *r) { delete r; }
 
+size_t ffcz_zstd_bound(size_t n) { return zstd_bound(n); }
+
+int ffcz_zstd_compress(const uint8_t *src, size_t n, int level, int mode, uint8_t *dst, size_t cap,
+                       size_t *out_len) {
+  if ((!src && n) || !dst || !out_len) return fail(FFCZ_ERR_INVALID, "NULL argument");
+  std::vector<uint8_t> out;
+  FFCZ_TRY(zstd_compress(src, n, level, mode == FFCZ_ZSTD_CHUNKED, out));
+  *out_len = out.size();
+  if (cap < out.size()) return fail(FFCZ_ERR_CAPACITY, "destination too small");
+  if (!out.empty()) std::memcpy(dst, out.data(), out.size());
+  return FFCZ_OK;
+}
+
 int ffcz_huff_result_sizes(const ffcz_huff_result *r, size_t *compressed_bytes, size_t *bitstream_bytes,
                            size_t *num_elements, size_t *num_symbols) {
   if (!r) return fail(FFCZ_ERR_INVALID, "result is NULL");

@@ -172,12 +172,24 @@ static int compress_one(const uint8_t *src, size_t n, int level, std::vector<uin
   return FFCZ_OK;
 }
 
+static size_t chunk_size(size_t n) {
+  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+  return std::max<size_t>((n + hw - 1) / hw, 128u << 10);
+}
+
+size_t zstd_bound(size_t n) {
+  if (!zstd_available(nullptr)) return 0;
+  Zstd &z = zstd();
+  const size_t chunk = chunk_size(n);
+  const size_t nch = (n + chunk - 1) / chunk;
+  return std::max(z.compressBound(n), nch * z.compressBound(std::min(chunk, n)));
+}
+
 int zstd_compress(const uint8_t *src, size_t n, int level, bool chunked, std::vector<uint8_t> &out) {
   std::string why;
   if (!zstd_available(&why)) return fail(FFCZ_ERR_ZSTD, why);
   if (!chunked || n < (256u << 10)) return compress_one(src, n, level, out);
-  unsigned hw = std::max(1u, std::thread::hardware_concurrency());
-  size_t chunk = std::max<size_t>((n + hw - 1) / hw, 128u << 10);
+  const size_t chunk = chunk_size(n);
   const size_t nch = (n + chunk - 1) / chunk;
   std::vector<std::vector<uint8_t>> parts(nch);
   std::vector<int> rc(nch, FFCZ_OK);

@@ -45,6 +45,8 @@ bool zstd_available(std::string *why);
 // ZSTD_compress(level) of the whole buffer, or (chunked) independent frames
 // of about size/threads bytes compressed on host threads and concatenated.
 int zstd_compress(const uint8_t *src, size_t n, int level, bool chunked, std::vector<uint8_t> &out);
+// Upper bound of zstd_compress's output in either mode (0 without libzstd).
+size_t zstd_bound(size_t n);
 // ZSTD_decompress into exactly `expect` bytes.
 int zstd_decompress(const uint8_t *src, size_t n, size_t expect, std::vector<uint8_t> &out);
 

@@ -363,7 +363,7 @@ __global__ void k_clamp_freq(c2<T> *__restrict__ spec, long long rows, int Hz, i
 }
 
 // ---------------------------------------------------------------------------
-__global__ void k_init_ctl(LoopCtl *ctl) {
+static __global__ void k_init_ctl(LoopCtl *ctl) {
   ctl->viol_bits = 0ull;
   ctl->last_viol = 0.0;
   ctl->iterations = 0;

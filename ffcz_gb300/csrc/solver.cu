@@ -13,6 +13,7 @@
 #include "fft_plan.h"
 #include "huffman.cuh"
 #include "passes.cuh"
+#include "static_kernels.h"
 
 using namespace ffcz;
 
@@ -71,6 +72,9 @@ struct ffcz_solver {
   SArgs sy{}, sx{};
   Launch lz_f, lz_i, ly, lx;
   int has_x = 0, has_y = 0, fused = 0;  // fused: 0 none, 1 y, 2 x
+  // kernels of each pass (generic or compile-time-sized), typed at launch
+  void *kzf[3] = {}, *kzi = nullptr, *ky[3] = {}, *kx[3] = {};
+  int static_z = 0, static_y = 0, static_x = 0;
   // parameters
   double eps = 0, delta = 0;
   bool initialized = false;
@@ -127,6 +131,60 @@ int set_smem_attrs() {
   return FFCZ_OK;
 }
 
+// Generic kernels for every pass, replaced by the compile-time-sized ones
+// where the axis length has one (power of two, FP32 up to 1024, FP64 up to
+// 512); the static kernels fix their own tile width, so the pass arguments
+// and grids are recomputed for them.
+template <typename T>
+int select_kernels(ffcz_solver *s) {
+  constexpr int E = ept_of<T>();
+  s->kzf[PRO_PLAIN] = (void *)k_zfwd<T, PRO_PLAIN, E>;
+  s->kzf[PRO_DIFF] = (void *)k_zfwd<T, PRO_DIFF, E>;
+  s->kzf[PRO_CLAMP] = (void *)k_zfwd<T, PRO_CLAMP, E>;
+  s->kzi = (void *)k_zinv<T, E>;
+  void *gen[3] = {(void *)k_strided<T, MODE_FWD, E>, (void *)k_strided<T, MODE_INV, E>,
+                  (void *)k_strided<T, MODE_FCI, E>};
+  for (int m = 0; m < 3; ++m) s->ky[m] = s->kx[m] = gen[m];
+  const char *off = getenv("FFCZ_GENERIC_KERNELS");
+  if (off && off[0] == '1') return FFCZ_OK;
+  StaticGeom g;
+  if (s->even) {
+    ZfwdFn<T> f[3];
+    ZinvFn<T> fi;
+    bool ok = static_zinv<T>(s->M, fi, g);
+    for (int pro = 0; pro < 3 && ok; ++pro) ok = static_zfwd<T>(s->M, pro, f[pro], g);
+    if (ok) {
+      for (int pro = 0; pro < 3; ++pro) s->kzf[pro] = (void *)f[pro];
+      s->kzi = (void *)fi;
+      s->za.TW = g.TW;
+      s->za.log2TW = __builtin_ctz(g.TW);
+      s->za.P = g.TW + 1;
+      s->lz_f.threads = s->lz_i.threads = g.threads;
+      s->lz_f.smem = s->lz_i.smem = g.smem;
+      s->lz_f.grid = s->lz_i.grid = (unsigned)ceil_div((size_t)s->rows, (size_t)g.TW);
+      s->static_z = 1;
+    }
+  }
+  auto strided = [&](int L, int Q, long long B, SArgs &sa, Launch &ln, void **k, int &flag) {
+    StridedFn<T> f[3];
+    bool ok = true;
+    for (int m = 0; m < 3 && ok; ++m) ok = static_strided<T>(L, m, f[m], g);
+    if (!ok) return;
+    for (int m = 0; m < 3; ++m) k[m] = (void *)f[m];
+    sa.TW = g.TW;
+    sa.log2TW = __builtin_ctz(g.TW);
+    sa.P = g.TW + 1;
+    sa.tpq = (int)ceil_div((size_t)s->Hz, (size_t)g.TW);
+    ln.threads = g.threads;
+    ln.smem = g.smem;
+    ln.grid = (unsigned)(B * Q * (long long)sa.tpq);
+    flag = 1;
+  };
+  if (s->has_y) strided((int)s->ny, 1, (long long)s->nx, s->sy, s->ly, s->ky, s->static_y);
+  if (s->has_x) strided((int)s->nx, (int)s->ny, 1, s->sx, s->lx, s->kx, s->static_x);
+  return FFCZ_OK;
+}
+
 template <typename T>
 int plan_solver(ffcz_solver *s) {
   constexpr int E = ept_of<T>();
@@ -165,7 +223,7 @@ int plan_solver(ffcz_solver *s) {
     const int rows_smem = s->even ? s->M + 1 : (int)s->nz;
     const int L = s->even ? s->M : (int)s->nz;
     int TW = 1;
-    FFCZ_TRY(pick_tile(rows_smem, std::max(L, s->Hz), es2, twmax, s->lz_f, TW, E));
+    FFCZ_TRY(pick_tile(rows_smem, L, es2, twmax, s->lz_f, TW, E));
     s->lz_i = s->lz_f;
     s->za.rows = s->rows;
     s->za.Nz = (int)s->nz;
@@ -198,9 +256,10 @@ int plan_solver(ffcz_solver *s) {
   if (s->has_y) FFCZ_TRY(plan_strided((int)s->ny, 1, (long long)s->nx, s->sy, s->ly));
   if (s->has_x) FFCZ_TRY(plan_strided((int)s->nx, (int)s->ny, 1, s->sx, s->lx));
   s->fused = s->has_x ? 2 : (s->has_y ? 1 : 0);
-  s->kernels_per_iter = 2 /*z fwd, z inv*/ + 1 /*check*/ + (s->fused ? 1 : 1) +
+  s->kernels_per_iter = 2 /*z fwd, z inv*/ + 1 /*check*/ + 1 /*fused axis or clamp*/ +
                         ((s->has_y && s->fused == 2) ? 2 : 0);
   FFCZ_TRY(set_smem_attrs<T>());
+  FFCZ_TRY(select_kernels<T>(s));
   return FFCZ_OK;
 }
 
@@ -222,34 +281,35 @@ void launch_iteration(ffcz_solver *s, cudaStream_t st, int pro, const void *a, c
   const c2<T> *post = (const c2<T> *)s->d_tw + s->post_off;
   c2<T> *spec = (c2<T> *)s->d_spec;
   const T *pa = (const T *)a, *pb = (const T *)b;
+  const ZfwdFn<T> kzf = (ZfwdFn<T>)s->kzf[pro];
   if (pro == PRO_PLAIN)
-    k_zfwd<T, PRO_PLAIN, E><<<s->lz_f.grid, s->lz_f.threads, s->lz_f.smem, st>>>(
-        pa, nullptr, tp<T>(s->d_sedits), eps, spec, s->za, s->pz, post);
+    kzf<<<s->lz_f.grid, s->lz_f.threads, s->lz_f.smem, st>>>(pa, nullptr, tp<T>(s->d_sedits), eps, spec, s->za,
+                                                              s->pz, post);
   else if (pro == PRO_DIFF)
-    k_zfwd<T, PRO_DIFF, E><<<s->lz_f.grid, s->lz_f.threads, s->lz_f.smem, st>>>(
-        pa, pb, tp<T>(s->d_sedits), eps, spec, s->za, s->pz, post);
+    kzf<<<s->lz_f.grid, s->lz_f.threads, s->lz_f.smem, st>>>(pa, pb, tp<T>(s->d_sedits), eps, spec, s->za, s->pz,
+                                                              post);
   else
-    k_zfwd<T, PRO_CLAMP, E><<<s->lz_f.grid, s->lz_f.threads, s->lz_f.smem, st>>>(
-        tp<T>(s->d_e), nullptr, tp<T>(s->d_sedits), eps, spec, s->za, s->pz, post);
+    kzf<<<s->lz_f.grid, s->lz_f.threads, s->lz_f.smem, st>>>(tp<T>(s->d_e), nullptr, tp<T>(s->d_sedits), eps, spec,
+                                                              s->za, s->pz, post);
   mark();
   const long long H = (long long)s->H;
   if (s->fused == 2) {
     if (s->has_y) {
-      k_strided<T, MODE_FWD, E><<<s->ly.grid, s->ly.threads, s->ly.smem, st>>>(spec, s->sy, s->py, delta,
-                                                                              tp<T>(s->d_fedits), H);
+      ((StridedFn<T>)s->ky[MODE_FWD])<<<s->ly.grid, s->ly.threads, s->ly.smem, st>>>(spec, s->sy, s->py, delta,
+                                                                                     tp<T>(s->d_fedits), H);
       mark();
     }
-    k_strided<T, MODE_FCI, E><<<s->lx.grid, s->lx.threads, s->lx.smem, st>>>(spec, s->sx, s->px, delta,
-                                                                            tp<T>(s->d_fedits), H);
+    ((StridedFn<T>)s->kx[MODE_FCI])<<<s->lx.grid, s->lx.threads, s->lx.smem, st>>>(spec, s->sx, s->px, delta,
+                                                                                   tp<T>(s->d_fedits), H);
     mark();
     if (s->has_y) {
-      k_strided<T, MODE_INV, E><<<s->ly.grid, s->ly.threads, s->ly.smem, st>>>(spec, s->sy, s->py, delta,
-                                                                              tp<T>(s->d_fedits), H);
+      ((StridedFn<T>)s->ky[MODE_INV])<<<s->ly.grid, s->ly.threads, s->ly.smem, st>>>(spec, s->sy, s->py, delta,
+                                                                                     tp<T>(s->d_fedits), H);
       mark();
     }
   } else if (s->fused == 1) {
-    k_strided<T, MODE_FCI, E><<<s->ly.grid, s->ly.threads, s->ly.smem, st>>>(spec, s->sy, s->py, delta,
-                                                                            tp<T>(s->d_fedits), H);
+    ((StridedFn<T>)s->ky[MODE_FCI])<<<s->ly.grid, s->ly.threads, s->ly.smem, st>>>(spec, s->sy, s->py, delta,
+                                                                                   tp<T>(s->d_fedits), H);
     mark();
   } else {
     const long long tot = s->rows * s->Hz;
@@ -258,8 +318,8 @@ void launch_iteration(ffcz_solver *s, cudaStream_t st, int pro, const void *a, c
     mark();
   }
   const T factor = T(1) / static_cast<T>(s->N);
-  k_zinv<T, E><<<s->lz_i.grid, s->lz_i.threads, s->lz_i.smem, st>>>(spec, tp<T>(s->d_e), eps, factor, s->d_ctl,
-                                                                    s->za, s->pz, post);
+  ((ZinvFn<T>)s->kzi)<<<s->lz_i.grid, s->lz_i.threads, s->lz_i.smem, st>>>(spec, tp<T>(s->d_e), eps, factor,
+                                                                          s->d_ctl, s->za, s->pz, post);
   mark();
   if (record) s->npass = ne - 1;
   k_check<T><<<1, 1, 0, st>>>(s->d_ctl, tol, max_iter, h, use_graph);

@@ -213,6 +213,14 @@ int ffcz_huff_result_bitstream(const ffcz_huff_result *r, uint8_t *dst,
 int ffcz_huff_result_codes(const ffcz_huff_result *r, uint32_t *symbols,
                            uint32_t *codes, int32_t *lengths, size_t cap);
 
+/* The ZSTD stage alone (HuffmanZSTDCoder.cuh:359-375) on host bytes, so
+ * that callers can run it on their own threads, overlapped with the GPU
+ * work of later fields.  FFCZ_ZSTD_SINGLE gives exactly ZSTD_compress's
+ * bytes.  ffcz_zstd_bound is an upper bound on the output size. */
+size_t ffcz_zstd_bound(size_t n);
+int ffcz_zstd_compress(const uint8_t *src, size_t n, int level, int mode,
+                       uint8_t *dst, size_t cap, size_t *out_len);
+
 /* decompress(...) -- HuffmanZSTDCoder.cuh:378-450: ZSTD_decompress, then a
  * prefix decode with the same stop and bit-skip rules.  out must hold
  * num_elements symbols; *out_len receives the decoded count. */

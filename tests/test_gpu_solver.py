@@ -229,3 +229,25 @@ def test_launch_count_reported(cuda):
         s.project_all_abs_device(cuda.from_numpy((fld.xp - fld.x).reshape(-1)).cuda(), 100, 1e-7)
         it = s.iterations
         assert s.launch_count() == 2 + 6 * it
+
+
+@pytest.mark.parametrize("shape", [(64, 64, 64), (32, 48, 20), (16, 1024, 32), (8, 16, 2048), (40, 512, 256)])
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_static_kernels_match_generic(cuda, shape, dtype, monkeypatch):
+    """Compile-time-sized pass kernels (power-of-two axes) against the
+    runtime-planned engine on the same input."""
+    fld = synth.make_field(shape, 11 / 3, 13, 1e-3, 1e-3, dtype, noise=0.3)
+    delta = synth.stress_delta(fld, 1.5)
+    e0 = (fld.xp.astype(np.float64) - fld.x.astype(np.float64)).astype(dtype)
+    out = []
+    for generic in ("0", "1"):
+        monkeypatch.setenv("FFCZ_GENERIC_KERNELS", generic)
+        with F.ProjectionSolver(*shape, dtype=dtype) as s:
+            s.initialize_all_abs(fld.x, fld.eps, delta)
+            it = s.solve_all_abs(e0, 100, 1e-7)
+            out.append((it, s.get_results().reshape(-1), s.get_freq_edits_full()))
+    assert out[0][0] == out[1][0]
+    tol = 1e-6 if dtype == np.float32 else 1e-14
+    assert np.abs(out[0][1] - out[1][1]).max() <= tol * np.abs(e0).max() * out[0][0]
+    fs = float(np.abs(out[1][2]).max()) or 1.0
+    assert np.abs(out[0][2] - out[1][2]).max() <= tol * max(fs, float(delta))
