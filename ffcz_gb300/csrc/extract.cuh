@@ -5,9 +5,10 @@
 //   k_ex_stats   : per 4096-element chunk: #(|v| > thr), min, max   (R n*s)
 //   k_ex_scan    : one block: chunk offsets (exclusive scan), global
 //                  min/max, active count                        (tiny)
-//   k_ex_compact : chunk re-read; ballot + popc positions; scatter of the
-//                  active values and their uint16 quantisation; LSB-first
-//                  flag words straight from the ballots    (R n*s, W 2*cnt*s + n/8)
+//   k_ex_compact : chunk re-read; per-thread flag bits + one block scan give
+//                  the positions; scatter of the active values and their
+//                  uint16 quantisation; LSB-first flag words from thread
+//                  pairs                                   (R n*s, W 2*cnt*s + n/8)
 #pragma once
 
 #include "common.cuh"
@@ -45,22 +46,56 @@ __device__ __forceinline__ uint16_t quantize16(T v, T mn, T mx) {
   return (uint16_t)(unsigned)q;
 }
 
+// Thread t of a block owns the 16 consecutive values [base + 16t, +16) of
+// its 4096-value chunk: 16-byte vector loads, thread-order = element order.
+constexpr int EX_PER = EX_CHUNK / EX_THREADS;  // 16
+
+template <typename T>
+__device__ __forceinline__ int load16(const T *__restrict__ a, long long n, long long i0, T (&v)[EX_PER]) {
+  if (i0 + EX_PER <= n) {
+    if (sizeof(T) == 4) {
+      const float4 *p = reinterpret_cast<const float4 *>(a + i0);
+#pragma unroll
+      for (int q = 0; q < EX_PER / 4; ++q) {
+        const float4 f = p[q];
+        v[4 * q] = (T)f.x;
+        v[4 * q + 1] = (T)f.y;
+        v[4 * q + 2] = (T)f.z;
+        v[4 * q + 3] = (T)f.w;
+      }
+    } else {
+      const double2 *p = reinterpret_cast<const double2 *>(a + i0);
+#pragma unroll
+      for (int q = 0; q < EX_PER / 2; ++q) {
+        const double2 f = p[q];
+        v[2 * q] = (T)f.x;
+        v[2 * q + 1] = (T)f.y;
+      }
+    }
+    return EX_PER;
+  }
+  const int cnt = (int)max(0ll, min((long long)EX_PER, n - i0));
+#pragma unroll
+  for (int t = 0; t < EX_PER; ++t) v[t] = (t < cnt) ? a[i0 + t] : T(0);
+  return cnt;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(EX_THREADS) k_ex_stats(const T *__restrict__ a, long long n, T thr,
                                                          unsigned *__restrict__ blk_cnt,
                                                          T *__restrict__ blk_mn,
                                                          T *__restrict__ blk_mx) {
-  const long long base = (long long)blockIdx.x * EX_CHUNK;
+  const long long i0 = (long long)blockIdx.x * EX_CHUNK + (long long)threadIdx.x * EX_PER;
+  T v[EX_PER];
+  const int cnt_valid = load16<T>(a, n, i0, v);
   unsigned cnt = 0;
   T mn = dev_inf<T>(), mx = -dev_inf<T>();
-#pragma unroll 4
-  for (int r = 0; r < EX_ROUNDS; ++r) {
-    const long long i = base + r * EX_THREADS + threadIdx.x;
-    if (i < n) {
-      const T v = a[i];
-      cnt += (fabs(v) > thr) ? 1u : 0u;
-      mn = (v < mn) ? v : mn;
-      mx = (v > mx) ? v : mx;
+#pragma unroll
+  for (int t = 0; t < EX_PER; ++t) {
+    if (t < cnt_valid) {
+      cnt += (fabs(v[t]) > thr) ? 1u : 0u;
+      mn = (v[t] < mn) ? v[t] : mn;
+      mx = (v[t] > mx) ? v[t] : mx;
     }
   }
   __shared__ unsigned sc[EX_THREADS / 32];
@@ -81,14 +116,16 @@ __global__ void __launch_bounds__(EX_THREADS) k_ex_stats(const T *__restrict__ a
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    for (int w = 1; w < EX_THREADS / 32; ++w) {
-      cnt = sc[0] += sc[w];
-      smn[0] = (smn[w] < smn[0]) ? smn[w] : smn[0];
-      smx[0] = (smx[w] > smx[0]) ? smx[w] : smx[0];
+    unsigned c = 0;
+    T lo = smn[0], hi = smx[0];
+    for (int w = 0; w < EX_THREADS / 32; ++w) {
+      c += sc[w];
+      lo = (smn[w] < lo) ? smn[w] : lo;
+      hi = (smx[w] > hi) ? smx[w] : hi;
     }
-    blk_cnt[blockIdx.x] = sc[0];
-    blk_mn[blockIdx.x] = smn[0];
-    blk_mx[blockIdx.x] = smx[0];
+    blk_cnt[blockIdx.x] = c;
+    blk_mn[blockIdx.x] = lo;
+    blk_mx[blockIdx.x] = hi;
   }
 }
 
@@ -168,46 +205,47 @@ __global__ void __launch_bounds__(1024) k_ex_scan(unsigned *__restrict__ blk_cnt
   }
 }
 
+// Positions: per-thread count of active values -> block exclusive scan
+// (one barrier) -> each thread writes its active values in order.  Flag
+// words: thread pairs (2u, 2u+1) hold the 32 flags of word base/32 + u.
 template <typename T>
 __global__ void __launch_bounds__(EX_THREADS) k_ex_compact(
     const T *__restrict__ a, long long n, T thr, const unsigned *__restrict__ blk_off,
     const T *__restrict__ mnmx, T *__restrict__ compact, uint16_t *__restrict__ quant,
     unsigned *__restrict__ pack_words, int write_pack) {
-  __shared__ unsigned wc[EX_THREADS / 32];
-  const long long base = (long long)blockIdx.x * EX_CHUNK;
+  __shared__ unsigned wsum[EX_THREADS / 32];
+  const long long i0 = (long long)blockIdx.x * EX_CHUNK + (long long)threadIdx.x * EX_PER;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const T mn = mnmx[0], mx = mnmx[1];
-  unsigned running = blk_off[blockIdx.x];
-  const unsigned lt = (1u << lane) - 1u;
-  for (int r = 0; r < EX_ROUNDS; ++r) {
-    const long long i0 = base + r * EX_THREADS;
-    if (i0 >= n) break;
-    const long long i = i0 + threadIdx.x;
-    T v = T(0);
-    bool f = false;
-    if (i < n) {
-      v = a[i];
-      f = fabs(v) > thr;
-    }
-    const unsigned bal = __ballot_sync(0xffffffffu, f);
-    const long long wbase = i0 + warp * 32;
-    if (write_pack && lane == 0 && wbase < n) pack_words[wbase >> 5] = bal;
-    if (lane == 0) wc[warp] = __popc(bal);
-    __syncthreads();
-    unsigned woff = 0, tot = 0;
+  T v[EX_PER];
+  const int cnt_valid = load16<T>(a, n, i0, v);
+  unsigned bits = 0;
 #pragma unroll
-    for (int w = 0; w < EX_THREADS / 32; ++w) {
-      const unsigned c = wc[w];
-      woff += (w < warp) ? c : 0u;
-      tot += c;
+  for (int t = 0; t < EX_PER; ++t)
+    if (t < cnt_valid && fabs(v[t]) > thr) bits |= 1u << t;
+  const unsigned mine = __popc(bits);
+  unsigned x = mine;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) wsum[warp] = x;
+  const unsigned partner = __shfl_down_sync(0xffffffffu, bits, 1);
+  if (write_pack && !(lane & 1) && i0 < n) pack_words[i0 >> 5] = bits | (partner << 16);
+  __syncthreads();
+  unsigned wpre = 0;
+#pragma unroll
+  for (int w = 0; w < EX_THREADS / 32; ++w) wpre += (w < warp) ? wsum[w] : 0u;
+  if (!bits) return;
+  const T mn = mnmx[0], mx = mnmx[1];
+  unsigned pos = blk_off[blockIdx.x] + wpre + x - mine;
+#pragma unroll
+  for (int t = 0; t < EX_PER; ++t) {
+    if (bits & (1u << t)) {
+      compact[pos] = v[t];
+      quant[pos] = quantize16<T>(v[t], mn, mx);
+      ++pos;
     }
-    if (f) {
-      const unsigned pos = running + woff + __popc(bal & lt);
-      compact[pos] = v;
-      quant[pos] = quantize16<T>(v, mn, mx);
-    }
-    running += tot;
-    __syncthreads();
   }
 }
 

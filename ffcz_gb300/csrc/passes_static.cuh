@@ -1,248 +1,211 @@
-// Compile-time-sized pass kernels for power-of-two axis lengths.
+// Compile-time-sized, register-resident pass kernels for power-of-two axis
+// lengths L = 16 .. 4096.
 //
-// Same kernels, arguments, layouts and arithmetic as passes.cuh, with the
-// axis length L, the tile width TW and the block size NT fixed at compile
-// time, so that:
-//   * the stage sequence (radix 8 stages, then one radix 4 or 2 stage, the
-//     factorisation fft_plan.cpp uses) is unrolled, with shifts in place of
-//     the divisions by the sub-transform span;
-//   * each block needs no register-heavy radix switch (fewer registers,
-//     more resident blocks per SM);
-//   * every thread issues all of its global loads before its first shared
-//     store, so a tile's loads are in flight together.
-// The twiddle table offsets still come from the runtime AxisPlan.
+// Each column (strided passes) or row (z passes) of length L is handled by
+// TC = L/E threads holding E elements each (E = the largest radix of the
+// stage list).  A stage of radix R runs E/R butterflies per thread in
+// registers; butterfly j = t + m*TC reads Stockham positions j + r*L/R and
+// writes (j/Ns)*Ns*R + j%Ns + r*Ns.  Stages exchange data through shared
+// memory, but the first stage reads its inputs straight from HBM into
+// registers and the last stage writes straight to HBM, so a transform of
+// S stages makes S-1 shared-memory round trips (one for L = 256 = 16*16).
+// In the fused pass (forward, frequency clamp, inverse) the inverse's
+// first radix equals the forward's last, so the clamped coefficients feed
+// the inverse without an exchange.
+//
+// The inverse runs the forward stage list in reverse order.
+// Twiddles come from a table built on the host for the same lists:
+// AxisPlan.twoff[s] for forward stage s, twoff[kInvBase + s] for inverse
+// stage s.
 #pragma once
 
 #include "passes.cuh"
 
 namespace ffcz {
 
+constexpr int kInvBase = 12;
+
 __host__ __device__ constexpr int ilog2(int n) { return n <= 1 ? 0 : 1 + ilog2(n >> 1); }
 
-// Radix of stage s for L = 2^lg: 8, 8, ..., then 4 or 2 for the remainder.
-__host__ __device__ constexpr int p2_nst(int lg) { return lg / 3 + (lg % 3 ? 1 : 0); }
-__host__ __device__ constexpr int p2_radix(int lg, int s) { return s < lg / 3 ? 8 : (lg % 3 == 2 ? 4 : 2); }
-__host__ __device__ constexpr int p2_lgns(int lg, int s) { return 3 * (s < lg / 3 ? s : lg / 3); }
-
-template <typename T, int DIR, int R, int LGNS, int L, int LGTW, int NT>
-__device__ __forceinline__ void sstage(c2<T> *buf, const c2<T> *__restrict__ tw, int tid) {
-  using V = c2<T>;
-  constexpr int TW = 1 << LGTW, P = TW + 1, M = L / R, NITEMS = M * TW;
-  constexpr int K = (NITEMS + NT - 1) / NT;
-  constexpr int NS = 1 << LGNS;
-  V v[K][R];
-#pragma unroll
-  for (int kk = 0; kk < K; ++kk) {
-    const int item = tid + kk * NT;
-    if (NITEMS % NT == 0 || item < NITEMS) {
-      const int j = item >> LGTW;
-      const int c = item & (TW - 1);
-#pragma unroll
-      for (int r = 0; r < R; ++r) v[kk][r] = buf[(j + r * M) * P + c];
-      if (NS > 1) {
-        const int k = j & (NS - 1);
-        const V *t = tw + k * (R - 1);
-#pragma unroll
-        for (int r = 1; r < R; ++r) {
-          const V w = t[r - 1];
-          v[kk][r] = (DIR < 0) ? cmul(v[kk][r], w) : cmulc(v[kk][r], w);
-        }
-      }
-      Dft<R, DIR, V>::run(v[kk]);
-    }
-  }
-  __syncthreads();
-#pragma unroll
-  for (int kk = 0; kk < K; ++kk) {
-    const int item = tid + kk * NT;
-    if (NITEMS % NT == 0 || item < NITEMS) {
-      const int j = item >> LGTW;
-      const int c = item & (TW - 1);
-      const int base = ((j >> LGNS) << (LGNS + ilog2(R))) + (j & (NS - 1));
-#pragma unroll
-      for (int r = 0; r < R; ++r) buf[(base + r * NS) * P + c] = v[kk][r];
-    }
-  }
-  __syncthreads();
+// Stage lists.  Strided passes (CAP 16): 16:[16] 32:[8,4] 64:[8,8]
+// 128:[16,8] 256:[16,16] 512:[8,8,8] 1024:[16,8,8] 2048:[16,16,8]
+// 4096:[16,16,16].  z passes (CAP 8, 16+ threads per row): radix-8 stages
+// then one radix 4 or 2 stage for the remainder.
+__host__ __device__ constexpr int rp_nst(int L, int cap = 16) {
+  return cap == 8 ? (ilog2(L) / 3 + (ilog2(L) % 3 ? 1 : 0)) : (L == 16 ? 1 : (L <= 256 ? 2 : 3));
+}
+__host__ __device__ constexpr int rp_radix(int L, int s, int cap = 16) {
+  return cap == 8 ? (s < ilog2(L) / 3 ? 8 : (ilog2(L) % 3 == 2 ? 4 : 2))
+       : L == 16 ? 16
+       : L == 32 ? (s == 0 ? 8 : 4)
+       : L == 64 ? 8
+       : L == 128 ? (s == 0 ? 16 : 8)
+       : L == 256 ? 16
+       : L == 512 ? 8
+       : L == 1024 ? (s == 0 ? 16 : 8)
+       : L == 2048 ? (s < 2 ? 16 : 8)
+       : 16;
+}
+__host__ __device__ constexpr int rp_elems(int L, int cap = 16) {
+  return cap == 8 ? 8 : ((L == 32 || L == 64 || L == 512) ? 8 : 16);
+}
+// radix of stage s in direction DIR (inverse = reversed list)
+__host__ __device__ constexpr int rp_rad(int L, int dir, int s, int cap = 16) {
+  return dir < 0 ? rp_radix(L, s, cap) : rp_radix(L, rp_nst(L, cap) - 1 - s, cap);
+}
+// log2 of the span Ns before stage s in direction dir
+__host__ __device__ constexpr int rp_lgns(int L, int dir, int s, int cap = 16) {
+  return s == 0 ? 0 : rp_lgns(L, dir, s - 1, cap) + ilog2(rp_rad(L, dir, s - 1, cap));
 }
 
-template <typename T, int DIR, int L, int LGTW, int NT, int S>
-struct SFft {
-  static __device__ __forceinline__ void run(c2<T> *buf, const AxisPlan &p, int tid) {
-    constexpr int lg = ilog2(L);
-    if constexpr (S < p2_nst(lg)) {
-      sstage<T, DIR, p2_radix(lg, S), p2_lgns(lg, S), L, LGTW, NT>(buf, (const c2<T> *)p.tw + p.twoff[S], tid);
-      SFft<T, DIR, L, LGTW, NT, S + 1>::run(buf, p, tid);
+// Radix 16 = 4 x 4 with the w16 twiddles between the two radix-4 layers.
+template <int DIR, typename V> struct Dft<16, DIR, V> {
+  __device__ __forceinline__ static void run(V *v) {
+    using S = decltype(v[0].x);
+    const S c1 = S(0.9238795325112867), s1 = S(0.3826834323650898), h = S(0.7071067811865476);
+    // layer 1: for each n2, radix-4 over n1 (elements 4*n1 + n2)
+#pragma unroll
+    for (int n2 = 0; n2 < 4; ++n2) bfly4<DIR>(v[n2], v[4 + n2], v[8 + n2], v[12 + n2]);
+    // twiddle w16^(n2*k1): element (k1, n2) at v[4*k1 + n2]
+    auto tw = [&](V &a, S c, S s) {  // a *= (c, DIR*s)
+      V r;
+      const S sd = DIR < 0 ? -s : s;
+      r.x = a.x * c - a.y * sd;
+      r.y = a.x * sd + a.y * c;
+      a = r;
+    };
+    tw(v[4 + 1], c1, s1);   // k1=1,n2=1 : w^1
+    tw(v[4 + 2], h, h);     // k1=1,n2=2 : w^2
+    tw(v[4 + 3], s1, c1);   // k1=1,n2=3 : w^3
+    v[8 + 1] = (DIR < 0) ? mkc<S>((v[9].x + v[9].y) * h, (v[9].y - v[9].x) * h)
+                         : mkc<S>((v[9].x - v[9].y) * h, (v[9].x + v[9].y) * h);  // w^2
+    v[8 + 2] = cmul_i<DIR>(v[8 + 2]);                                              // w^4
+    tw(v[8 + 3], -h, h);    // w^6
+    tw(v[12 + 1], s1, c1);  // w^3
+    tw(v[12 + 2], -h, h);   // w^6
+    tw(v[12 + 3], -c1, -s1);  // w^9
+    // layer 2: for each k1, radix-4 over n2 -> outputs k1 + 4*k2
+    V out[16];
+#pragma unroll
+    for (int k1 = 0; k1 < 4; ++k1) {
+      V a0 = v[4 * k1], a1 = v[4 * k1 + 1], a2 = v[4 * k1 + 2], a3 = v[4 * k1 + 3];
+      bfly4<DIR>(a0, a1, a2, a3);
+      out[k1] = a0;
+      out[k1 + 4] = a1;
+      out[k1 + 8] = a2;
+      out[k1 + 12] = a3;
+    }
+#pragma unroll
+    for (int k = 0; k < 16; ++k) v[k] = out[k];
+  }
+};
+
+// Butterflies of one stage on the thread's registers: v[m*R + r] is input
+// r of butterfly m (j = t + m*TC) and becomes output r.
+template <typename T, int DIR, int R, int LGNS, int L, int E>
+__device__ __forceinline__ void rstage(c2<T> (&v)[E], int t, const c2<T> *__restrict__ tw) {
+  using V = c2<T>;
+  constexpr int TC = L / E, NS = 1 << LGNS;
+#pragma unroll
+  for (int m = 0; m < E / R; ++m) {
+    if (NS > 1) {
+      const int j = t + m * TC;
+      const V *w = tw + (j & (NS - 1)) * (R - 1);
+#pragma unroll
+      for (int r = 1; r < R; ++r) {
+        const V ww = w[r - 1];
+        v[m * R + r] = (DIR < 0) ? cmul(v[m * R + r], ww) : cmulc(v[m * R + r], ww);
+      }
+    }
+    Dft<R, DIR, V>::run(&v[m * R]);
+  }
+}
+
+// Shared-memory layouts of a tile of positions x columns.  Strided passes
+// (lanes along columns): element (pos, c) at pos*P + c, P = TW + 1.  z passes
+// (lanes along positions): row-major with one pad slot every 16 positions,
+// so that the stride-R output positions of a stage fall in distinct banks.
+template <int P>
+struct ColLayout {
+  static __device__ __forceinline__ int idx(int pos, int c) { return pos * P + c; }
+};
+template <int RP>
+struct RowLayout {
+  static __device__ __forceinline__ int idx(int pos, int c) { return c * RP + pos + (pos >> 4); }
+};
+__host__ __device__ constexpr int row_pitch(int M) { return M + (M >> 4) + 1; }
+
+template <int L, int E, int R>
+__device__ __forceinline__ int in_pos(int t, int m, int r) {
+  return t + m * (L / E) + r * (L / R);
+}
+template <int L, int E, int R, int LGNS>
+__device__ __forceinline__ int out_pos(int t, int m, int r) {
+  const int j = t + m * (L / E);
+  return ((j >> LGNS) << (LGNS + ilog2(R))) + (j & ((1 << LGNS) - 1)) + (r << LGNS);
+}
+
+// Runs stages S..end of direction DIR; v holds stage S's inputs.  Between
+// stages the data goes through shared memory (layout LY).  On return v
+// holds the last stage's outputs (positions out_pos of that stage).
+template <typename T, int DIR, int L, typename LY, int S, int CAP = 16>
+struct RRun {
+  static constexpr int E = rp_elems(L, CAP);
+  static __device__ __forceinline__ void run(c2<T> (&v)[E], c2<T> *buf, int t, int c, const AxisPlan &p) {
+    if constexpr (S < rp_nst(L, CAP)) {
+      constexpr int R = rp_rad(L, DIR, S, CAP), LG = rp_lgns(L, DIR, S, CAP);
+      const c2<T> *tw = (const c2<T> *)p.tw + p.twoff[(DIR < 0 ? 0 : kInvBase) + S];
+      rstage<T, DIR, R, LG, L, E>(v, t, tw);
+      if constexpr (S + 1 < rp_nst(L, CAP)) {
+        constexpr int R2 = rp_rad(L, DIR, S + 1, CAP);
+#pragma unroll
+        for (int m = 0; m < E / R; ++m)
+#pragma unroll
+          for (int r = 0; r < R; ++r) buf[LY::idx(out_pos<L, E, R, LG>(t, m, r), c)] = v[m * R + r];
+        __syncthreads();
+#pragma unroll
+        for (int m = 0; m < E / R2; ++m)
+#pragma unroll
+          for (int r = 0; r < R2; ++r) v[m * R2 + r] = buf[LY::idx(in_pos<L, E, R2>(t, m, r), c)];
+        __syncthreads();
+        RRun<T, DIR, L, LY, S + 1, CAP>::run(v, buf, t, c, p);
+      }
     }
   }
 };
 
-template <typename T, int DIR, int L, int LGTW, int NT>
-__device__ __forceinline__ void sfft(c2<T> *buf, const AxisPlan &p, int tid) {
-  SFft<T, DIR, L, LGTW, NT, 0>::run(buf, p, tid);
+// Position of v[i] after the last stage of direction DIR.
+template <int L, int DIR, int CAP = 16>
+__device__ __forceinline__ int last_pos(int t, int i) {
+  constexpr int S = rp_nst(L, CAP) - 1, E = rp_elems(L, CAP), R = rp_rad(L, DIR, S, CAP),
+                LG = rp_lgns(L, DIR, S, CAP);
+  return out_pos<L, E, R, LG>(t, i / R, i % R);
 }
+// Position of v[i] as input of the first stage of direction DIR.
+template <int L, int DIR, int CAP = 16>
+__device__ __forceinline__ int first_pos(int t, int i) {
+  constexpr int E = rp_elems(L, CAP), R = rp_rad(L, DIR, 0, CAP);
+  return in_pos<L, E, R>(t, i / R, i % R);
+}
+
+// Resident blocks the 256-thread FP32 strided tiles are compiled for (three
+// per SM fit their 35 KB tiles and keep 24 warps resident); others: one.
+__host__ __device__ constexpr int strided_minb(int es, int nt) { return (es == 4 && nt == 256) ? 3 : 1; }
 
 // ---------------------------------------------------------------------------
-// R2C along z (even Nz = 2M, M = 2^k) for TW rows; see k_zfwd.
-template <typename T, int PRO, int M, int LGTW, int NT>
-__global__ void __launch_bounds__(NT) ks_zfwd(const T *__restrict__ a, const T *__restrict__ b,
-                                             T *__restrict__ sedits, T eps, c2<T> *__restrict__ spec, ZArgs z,
-                                             AxisPlan p, const c2<T> *__restrict__ post) {
+// Strided C2C pass.  Block = TC threads per column x TW columns (c fastest
+// across lanes, so each row access is TW contiguous complex values).
+template <typename T, int MODE, int L, int LGTW>
+__global__ void __launch_bounds__((L / rp_elems(L)) << LGTW,
+                                  strided_minb(sizeof(T), (L / rp_elems(L)) << LGTW)) ks_strided(c2<T> *__restrict__ spec, SArgs s,
+                                                                        AxisPlan p, T delta,
+                                                                        T *__restrict__ fedits, long long H) {
   using V = c2<T>;
+  constexpr int E = rp_elems(L), TW = 1 << LGTW, P = TW + 1;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   V *buf = reinterpret_cast<V *>(smem_raw);
-  constexpr int TW = 1 << LGTW, P = TW + 1, LGM = ilog2(M);
-  constexpr int NLD = M * TW, KLD = (NLD + NT - 1) / NT;
-  const int tid = threadIdx.x;
-  const long long row0 = (long long)blockIdx.x * TW;
-  const int nrows = (int)min((long long)TW, z.rows - row0);
-  V v[KLD];
-#pragma unroll
-  for (int kk = 0; kk < KLD; ++kk) {
-    const int it = tid + kk * NT;
-    const int c = it >> LGM, n = it & (M - 1);
-    v[kk] = mkc<T>(T(0), T(0));
-    if ((NLD % NT == 0 || it < NLD) && c < nrows) {
-      const long long gi = (row0 + c) * (long long)(2 * M) + 2 * n;
-      v[kk] = *reinterpret_cast<const V *>(a + gi);
-      if (PRO == PRO_DIFF) {
-        const V w = *reinterpret_cast<const V *>(b + gi);
-        v[kk].x -= w.x;
-        v[kk].y -= w.y;
-      }
-    }
-  }
-#pragma unroll
-  for (int kk = 0; kk < KLD; ++kk) {
-    const int it = tid + kk * NT;
-    const int c = it >> LGM, n = it & (M - 1);
-    if (NLD % NT == 0 || it < NLD) {
-      if (PRO == PRO_CLAMP && c < nrows) {
-        const long long gi = (row0 + c) * (long long)(2 * M) + 2 * n;
-        v[kk].x = spatial_clamp(v[kk].x, eps, sedits, gi);
-        v[kk].y = spatial_clamp(v[kk].y, eps, sedits, gi + 1);
-      }
-      buf[n * P + c] = v[kk];
-    }
-  }
-  __syncthreads();
-  sfft<T, -1, M, LGTW, NT>(buf, p, tid);
-  constexpr int HZ = M + 1;
-  constexpr int NST = HZ * TW, KST = (NST + NT - 1) / NT;
-#pragma unroll
-  for (int kk = 0; kk < KST; ++kk) {
-    const int it = tid + kk * NT;
-    if (it >= NST) break;
-    const int c = it / HZ;
-    const int k = it - c * HZ;
-    if (c >= nrows) continue;
-    const int k1 = (k == M) ? 0 : k;
-    const int k2 = (k == 0) ? 0 : M - k;
-    const V A = buf[k1 * P + c];
-    const V B = cconj(buf[k2 * P + c]);
-    const V w = post[k];
-    const V s = cadd(A, B);
-    const V d = csub(A, B);
-    const V t = cmul(mkc<T>(-w.y, w.x), d);
-    V X;
-    X.x = T(0.5) * (s.x - t.x);
-    X.y = T(0.5) * (s.y - t.y);
-    spec[(row0 + c) * (long long)z.Hzp + k] = X;
-  }
-}
-
-// C2R along z (even Nz = 2M) for TW rows + 1/N + violation; see k_zinv.
-template <typename T, int M, int LGTW, int NT>
-__global__ void __launch_bounds__(NT) ks_zinv(const c2<T> *__restrict__ spec, T *__restrict__ e, T eps, T factor,
-                                             LoopCtl *ctl, ZArgs z, AxisPlan p, const c2<T> *__restrict__ post) {
-  using V = c2<T>;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  V *buf = reinterpret_cast<V *>(smem_raw);
-  constexpr int TW = 1 << LGTW, P = TW + 1, LGM = ilog2(M), HZ = M + 1;
-  const int tid = threadIdx.x;
-  const long long row0 = (long long)blockIdx.x * TW;
-  const int nrows = (int)min((long long)TW, z.rows - row0);
-  {
-    constexpr int NLD = HZ * TW, KLD = (NLD + NT - 1) / NT;
-    V v[KLD];
-#pragma unroll
-    for (int kk = 0; kk < KLD; ++kk) {
-      const int it = tid + kk * NT;
-      const int c = it / HZ;
-      const int k = it - c * HZ;
-      v[kk] = mkc<T>(T(0), T(0));
-      if (it < NLD && c < nrows) v[kk] = spec[(row0 + c) * (long long)z.Hzp + k];
-    }
-#pragma unroll
-    for (int kk = 0; kk < KLD; ++kk) {
-      const int it = tid + kk * NT;
-      const int c = it / HZ;
-      const int k = it - c * HZ;
-      if (it < NLD) buf[k * P + c] = v[kk];
-    }
-  }
-  __syncthreads();
-  {
-    constexpr int HALF = M / 2;
-    constexpr int NPR = (HALF + 1) * TW, KPR = (NPR + NT - 1) / NT;
-#pragma unroll
-    for (int kk = 0; kk < KPR; ++kk) {
-      const int it = tid + kk * NT;
-      if (it >= NPR) break;
-      const int c = it / (HALF + 1);
-      const int k = it - c * (HALF + 1);
-      if (k == 0) {
-        const T x0 = buf[c].x, xm = buf[M * P + c].x;
-        buf[c] = mkc<T>(x0 + xm, x0 - xm);
-      } else {
-        const int km = M - k;
-        const V Xk = buf[k * P + c];
-        const V Xm = buf[km * P + c];
-        const V w = post[k];
-        const V s1 = cadd(Xk, cconj(Xm));
-        const V d1 = csub(Xk, cconj(Xm));
-        const V t1 = cmul(mkc<T>(w.y, w.x), d1);
-        buf[k * P + c] = cadd(s1, t1);
-        if (km != k) {
-          const V s2 = cadd(Xm, cconj(Xk));
-          const V d2 = csub(Xm, cconj(Xk));
-          const V t2 = cmul(mkc<T>(-w.y, w.x), d2);
-          buf[km * P + c] = csub(s2, t2);
-        }
-      }
-    }
-  }
-  __syncthreads();
-  sfft<T, +1, M, LGTW, NT>(buf, p, tid);
-  T vmax = T(0);
-  constexpr int NST = M * TW, KST = (NST + NT - 1) / NT;
-#pragma unroll
-  for (int kk = 0; kk < KST; ++kk) {
-    const int it = tid + kk * NT;
-    const int c = it >> LGM, n = it & (M - 1);
-    if ((NST % NT == 0 || it < NST) && c < nrows) {
-      const V v = buf[n * P + c];
-      V o;
-      o.x = v.x * factor;
-      o.y = v.y * factor;
-      *reinterpret_cast<V *>(e + (row0 + c) * (long long)(2 * M) + 2 * n) = o;
-      const T a0 = fabs(o.x), a1 = fabs(o.y);
-      if (a0 > eps) vmax = max(vmax, a0 - eps);
-      if (a1 > eps) vmax = max(vmax, a1 - eps);
-    }
-  }
-  block_max_to_ctl<T>(vmax, ctl);
-}
-
-// C2C along a strided axis of length L for TW columns; see k_strided.
-template <typename T, int MODE, int L, int LGTW, int NT>
-__global__ void __launch_bounds__(NT) ks_strided(c2<T> *__restrict__ spec, SArgs s, AxisPlan p, T delta,
-                                                T *__restrict__ fedits, long long H) {
-  using V = c2<T>;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  V *buf = reinterpret_cast<V *>(smem_raw);
-  constexpr int TW = 1 << LGTW, P = TW + 1, N = L * TW, K = (N + NT - 1) / NT;
-  const int tid = threadIdx.x;
+  const int c = threadIdx.x & (TW - 1);
+  const int t = threadIdx.x >> LGTW;
   const long long tile = blockIdx.x;
   const long long per_b = (long long)s.Q * s.tpq;
   const long long bb = tile / per_b;
@@ -250,45 +213,163 @@ __global__ void __launch_bounds__(NT) ks_strided(c2<T> *__restrict__ spec, SArgs
   const int q = rem / s.tpq;
   const int kb = rem - q * s.tpq;
   const int kz0 = kb * TW;
-  const int ncol = min(TW, s.Hz - kz0);
-  const long long base = bb * (long long)L * s.Wtot + (long long)q * s.Hzp + kz0;
-  {
-    V v[K];
+  const bool live = c < s.Hz - kz0;
+  const V *src = spec + bb * (long long)L * s.Wtot + (long long)q * s.Hzp + kz0 + c;
+  constexpr int D0 = (MODE == MODE_INV) ? +1 : -1;
+  V v[E];
 #pragma unroll
-    for (int kk = 0; kk < K; ++kk) {
-      const int it = tid + kk * NT;
-      const int l = it >> LGTW, c = it & (TW - 1);
-      v[kk] = mkc<T>(T(0), T(0));
-      if ((N % NT == 0 || it < N) && c < ncol) v[kk] = spec[base + (long long)l * s.Wtot + c];
-    }
-#pragma unroll
-    for (int kk = 0; kk < K; ++kk) {
-      const int it = tid + kk * NT;
-      if (N % NT == 0 || it < N) buf[(it >> LGTW) * P + (it & (TW - 1))] = v[kk];
-    }
-  }
-  __syncthreads();
-  if (MODE == MODE_INV) sfft<T, +1, L, LGTW, NT>(buf, p, tid);
-  else sfft<T, -1, L, LGTW, NT>(buf, p, tid);
+  for (int i = 0; i < E; ++i)
+    v[i] = live ? src[(long long)first_pos<L, D0>(t, i) * s.Wtot] : mkc<T>(T(0), T(0));
+  RRun<T, D0, L, ColLayout<P>, 0>::run(v, buf, t, c, p);
   if (MODE == MODE_FCI) {
+    if (live) {
 #pragma unroll
-    for (int kk = 0; kk < K; ++kk) {
-      const int it = tid + kk * NT;
-      const int l = it >> LGTW, c = it & (TW - 1);
-      if ((N % NT == 0 || it < N) && c < ncol) {
+      for (int i = 0; i < E; ++i) {
+        const int l = last_pos<L, -1>(t, i);
         const long long k = ((bb * L + l) * (long long)s.Q + q) * s.Hz + kz0 + c;
-        buf[l * P + c] = freq_clamp<T>(buf[l * P + c], delta, fedits, k, H);
+        v[i] = freq_clamp<T>(v[i], delta, fedits, k, H);
       }
     }
+    // The inverse's first stage reads the positions the forward's last
+    // stage wrote, so the same registers continue.  A barrier separates the
+    // forward's last shared reads from the inverse's first shared writes.
     __syncthreads();
-    sfft<T, +1, L, LGTW, NT>(buf, p, tid);
+    RRun<T, +1, L, ColLayout<P>, 0>::run(v, buf, t, c, p);
   }
+  constexpr int DL = (MODE == MODE_FWD) ? -1 : +1;
+  V *dst = spec + bb * (long long)L * s.Wtot + (long long)q * s.Hzp + kz0 + c;
+  if (live) {
 #pragma unroll
-  for (int kk = 0; kk < K; ++kk) {
-    const int it = tid + kk * NT;
-    const int l = it >> LGTW, c = it & (TW - 1);
-    if ((N % NT == 0 || it < N) && c < ncol) spec[base + (long long)l * s.Wtot + c] = buf[l * P + c];
+    for (int i = 0; i < E; ++i) dst[(long long)last_pos<L, DL>(t, i) * s.Wtot] = v[i];
   }
+}
+
+// ---------------------------------------------------------------------------
+// R2C along z (Nz = 2M): TC = M/8 threads per row x TW rows (t fastest
+// across lanes: each load is a run of consecutive complex values of one row,
+// and a half warp holds a single row).
+template <typename T, int PRO, int M, int LGTW>
+__global__ void __launch_bounds__((M / 8) << LGTW) ks_zfwd(const T *__restrict__ a, const T *__restrict__ b,
+                                                          T *__restrict__ sedits, T eps,
+                                                          c2<T> *__restrict__ spec, ZArgs z, AxisPlan p,
+                                                          const c2<T> *__restrict__ post) {
+  using V = c2<T>;
+  constexpr int E = 8, TC = M / E;
+  using LY = RowLayout<row_pitch(M)>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  V *buf = reinterpret_cast<V *>(smem_raw);
+  const int t = threadIdx.x % TC;
+  const int c = threadIdx.x / TC;
+  const long long row = (long long)blockIdx.x * (1 << LGTW) + c;
+  const bool live = row < z.rows;
+  const long long rbase = row * (long long)(2 * M);
+  V v[E];
+#pragma unroll
+  for (int i = 0; i < E; ++i) {
+    v[i] = mkc<T>(T(0), T(0));
+    if (live) {
+      const long long gi = rbase + 2 * first_pos<M, -1, 8>(t, i);
+      v[i] = *reinterpret_cast<const V *>(a + gi);
+      if (PRO == PRO_DIFF) {
+        const V w = *reinterpret_cast<const V *>(b + gi);
+        v[i].x -= w.x;
+        v[i].y -= w.y;
+      }
+    }
+  }
+  if (PRO == PRO_CLAMP && live) {
+#pragma unroll
+    for (int i = 0; i < E; ++i) {
+      const long long gi = rbase + 2 * first_pos<M, -1, 8>(t, i);
+      v[i].x = spatial_clamp(v[i].x, eps, sedits, gi);
+      v[i].y = spatial_clamp(v[i].y, eps, sedits, gi + 1);
+    }
+  }
+  RRun<T, -1, M, LY, 0, 8>::run(v, buf, t, c, p);
+  // Z in natural order to shared memory, then the real-to-complex split of
+  // row c: X[k] = (Z[k] + conj Z[M-k])/2 - i W^k (Z[k] - conj Z[M-k])/2.
+  if (rp_nst(M, 8) > 1) __syncthreads();
+#pragma unroll
+  for (int i = 0; i < E; ++i) buf[LY::idx(last_pos<M, -1, 8>(t, i), c)] = v[i];
+  __syncthreads();
+  if (!live) return;
+  V *out = spec + row * (long long)z.Hzp;
+  for (int k = t; k <= M; k += TC) {
+    const int k1 = (k == M) ? 0 : k;
+    const int k2 = (k == 0) ? 0 : M - k;
+    const V A = buf[LY::idx(k1, c)];
+    const V B = cconj(buf[LY::idx(k2, c)]);
+    const V w = post[k];
+    const V sm = cadd(A, B);
+    const V d = csub(A, B);
+    const V tt = cmul(mkc<T>(-w.y, w.x), d);
+    V X;
+    X.x = T(0.5) * (sm.x - tt.x);
+    X.y = T(0.5) * (sm.y - tt.y);
+    out[k] = X;
+  }
+}
+
+// C2R along z (Nz = 2M) + normalisation + violation max.  Each thread reads
+// X[k] and X[M-k] for its first-stage positions straight from global memory
+// (the row is read by the block, so the second read mostly hits L1) and
+// forms Z[k] = (X[k] + conj X[M-k]) + i W^-k (X[k] - conj X[M-k]) in
+// registers (imaginary parts of X[0] and X[M] ignored).
+template <typename T, int M, int LGTW>
+__global__ void __launch_bounds__((M / 8) << LGTW) ks_zinv(const c2<T> *__restrict__ spec, T *__restrict__ e,
+                                                          T eps, T factor, LoopCtl *ctl, ZArgs z, AxisPlan p,
+                                                          const c2<T> *__restrict__ post) {
+  using V = c2<T>;
+  constexpr int E = 8, TC = M / E;
+  using LY = RowLayout<row_pitch(M)>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  V *buf = reinterpret_cast<V *>(smem_raw);
+  const int t = threadIdx.x % TC;
+  const int c = threadIdx.x / TC;
+  const long long row = (long long)blockIdx.x * (1 << LGTW) + c;
+  const bool live = row < z.rows;
+  const V *in = spec + row * (long long)z.Hzp;
+  V v[E];
+  if (live) {
+    V xa[E], xb[E];
+#pragma unroll
+    for (int i = 0; i < E; ++i) {
+      const int k = first_pos<M, +1, 8>(t, i);
+      xa[i] = in[k];
+      xb[i] = in[M - k];
+    }
+#pragma unroll
+    for (int i = 0; i < E; ++i) {
+      const int k = first_pos<M, +1, 8>(t, i);
+      if (k == 0) {
+        v[i] = mkc<T>(xa[i].x + xb[i].x, xa[i].x - xb[i].x);
+      } else {
+        const V w = post[k];
+        const V s1 = cadd(xa[i], cconj(xb[i]));
+        const V d1 = csub(xa[i], cconj(xb[i]));
+        v[i] = cadd(s1, cmul(mkc<T>(w.y, w.x), d1));
+      }
+    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < E; ++i) v[i] = mkc<T>(T(0), T(0));
+  }
+  RRun<T, +1, M, LY, 0, 8>::run(v, buf, t, c, p);
+  T vmax = T(0);
+  if (live) {
+    T *out = e + row * (long long)(2 * M);
+#pragma unroll
+    for (int i = 0; i < E; ++i) {
+      V o;
+      o.x = v[i].x * factor;
+      o.y = v[i].y * factor;
+      *reinterpret_cast<V *>(out + 2 * last_pos<M, +1, 8>(t, i)) = o;
+      const T a0 = fabs(o.x), a1 = fabs(o.y);
+      if (a0 > eps) vmax = max(vmax, a0 - eps);
+      if (a1 > eps) vmax = max(vmax, a1 - eps);
+    }
+  }
+  block_max_to_ctl<T>(vmax, ctl);
 }
 
 }  // namespace ffcz

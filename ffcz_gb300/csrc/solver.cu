@@ -67,6 +67,7 @@ struct ffcz_solver {
   size_t nblk_max = 0;
   // plans
   AxisPlan pz{}, py{}, px{};
+  AxisPlan pz_s{}, py_s{}, px_s{};  // plans of the compile-time-sized kernels
   size_t post_off = 0;  // offset (complex entries) of the R2C split twiddles
   ZArgs za{};
   SArgs sy{}, sx{};
@@ -153,9 +154,10 @@ int select_kernels(ffcz_solver *s) {
     ZinvFn<T> fi;
     bool ok = static_zinv<T>(s->M, fi, g);
     for (int pro = 0; pro < 3 && ok; ++pro) ok = static_zfwd<T>(s->M, pro, f[pro], g);
-    if (ok) {
+    if (ok && s->pz_s.nst > 0) {
       for (int pro = 0; pro < 3; ++pro) s->kzf[pro] = (void *)f[pro];
       s->kzi = (void *)fi;
+      s->pz = s->pz_s;
       s->za.TW = g.TW;
       s->za.log2TW = __builtin_ctz(g.TW);
       s->za.P = g.TW + 1;
@@ -165,12 +167,14 @@ int select_kernels(ffcz_solver *s) {
       s->static_z = 1;
     }
   }
-  auto strided = [&](int L, int Q, long long B, SArgs &sa, Launch &ln, void **k, int &flag) {
+  auto strided = [&](int L, int Q, long long B, SArgs &sa, Launch &ln, void **k, int &flag, AxisPlan &pl,
+                     const AxisPlan &ps) {
     StridedFn<T> f[3];
-    bool ok = true;
+    bool ok = ps.nst > 0;
     for (int m = 0; m < 3 && ok; ++m) ok = static_strided<T>(L, m, f[m], g);
     if (!ok) return;
     for (int m = 0; m < 3; ++m) k[m] = (void *)f[m];
+    pl = ps;
     sa.TW = g.TW;
     sa.log2TW = __builtin_ctz(g.TW);
     sa.P = g.TW + 1;
@@ -180,8 +184,8 @@ int select_kernels(ffcz_solver *s) {
     ln.grid = (unsigned)(B * Q * (long long)sa.tpq);
     flag = 1;
   };
-  if (s->has_y) strided((int)s->ny, 1, (long long)s->nx, s->sy, s->ly, s->ky, s->static_y);
-  if (s->has_x) strided((int)s->nx, (int)s->ny, 1, s->sx, s->lx, s->kx, s->static_x);
+  if (s->has_y) strided((int)s->ny, 1, (long long)s->nx, s->sy, s->ly, s->ky, s->static_y, s->py, s->py_s);
+  if (s->has_x) strided((int)s->nx, (int)s->ny, 1, s->sx, s->lx, s->kx, s->static_x, s->px, s->px_s);
   return FFCZ_OK;
 }
 
@@ -204,6 +208,13 @@ int plan_solver(ffcz_solver *s) {
     return fail(FFCZ_ERR_UNSUPPORTED, "Ny = " + std::to_string(s->ny) + " has an unsupported prime factor");
   if (s->has_x && !build_axis_plan((int)s->nx, s->px, table))
     return fail(FFCZ_ERR_UNSUPPORTED, "Nx = " + std::to_string(s->nx) + " has an unsupported prime factor");
+  const bool fp64 = sizeof(T) == 8;
+  const bool zs = s->even && static_length(s->M, fp64);
+  const bool ys = s->has_y && static_length((int)s->ny, fp64);
+  const bool xs = s->has_x && static_length((int)s->nx, fp64);
+  if (zs) build_static_plan(s->M, 8, s->pz_s, table);
+  if (ys) build_static_plan((int)s->ny, 16, s->py_s, table);
+  if (xs) build_static_plan((int)s->nx, 16, s->px_s, table);
   s->post_off = table.size();
   if (s->even)
     for (int k = 0; k <= s->M; ++k) {
@@ -215,9 +226,8 @@ int plan_solver(ffcz_solver *s) {
   for (size_t i = 0; i < table.size(); ++i) tw[i] = mkc<T>((T)table[i].real(), (T)table[i].imag());
   FFCZ_CUDA(cudaMalloc(&s->d_tw, tw.size() * es2));
   FFCZ_CUDA(cudaMemcpy(s->d_tw, tw.data(), tw.size() * es2, cudaMemcpyHostToDevice));
-  s->pz.tw = s->d_tw;
-  s->py.tw = s->d_tw;
-  s->px.tw = s->d_tw;
+  s->pz.tw = s->py.tw = s->px.tw = s->d_tw;
+  s->pz_s.tw = s->py_s.tw = s->px_s.tw = s->d_tw;
   // z passes
   {
     const int rows_smem = s->even ? s->M + 1 : (int)s->nz;

@@ -1,18 +1,47 @@
-// Instantiations of the compile-time-sized pass kernels for power-of-two
-// lengths 16..1024 (FP32) and 16..512 (FP64), and their lookup.
+// Instantiations of the register-resident pass kernels (FP32 lengths
+// 16..4096, FP64 16..2048), their lookup, and their twiddle tables.
+#include <cmath>
+
 #include "passes_static.cuh"
 #include "static_kernels.h"
 
 namespace ffcz {
 
+bool static_length(int L, bool fp64) {
+  return L >= 16 && (L & (L - 1)) == 0 && L <= (fp64 ? 2048 : 4096);
+}
+
+void build_static_plan(int L, int cap, AxisPlan &p, std::vector<std::complex<double>> &table) {
+  p.L = L;
+  p.nst = rp_nst(L, cap);
+  p.tw = nullptr;
+  for (int dir : {-1, +1}) {
+    long long Ns = 1;
+    for (int s = 0; s < rp_nst(L, cap); ++s) {
+      const int R = rp_rad(L, dir, s, cap);
+      p.twoff[(dir < 0 ? 0 : kInvBase) + s] = (int)table.size();
+      if (Ns > 1)
+        for (long long k = 0; k < Ns; ++k)
+          for (int r = 1; r < R; ++r) {
+            const long long d = Ns * R, a = (r * k) % d;
+            const double th = -2.0 * M_PI * (double)a / (double)d;
+            table.push_back({std::cos(th), std::sin(th)});
+          }
+      Ns *= R;
+    }
+  }
+}
+
 namespace {
 
-template <typename T, int L>
+template <typename T, int L, int CAP = 16>
 struct Cfg {
-  static constexpr int LGTW = sizeof(T) == 4 ? (L <= 512 ? 4 : 3) : (L <= 256 ? 3 : 3);
-  static constexpr int TW = 1 << LGTW;
-  static constexpr int NT0 = L * TW / 8;
-  static constexpr int NT = NT0 < 64 ? 64 : (NT0 > 1024 ? 1024 : NT0);
+  static constexpr int TC = L / rp_elems(L, CAP);
+  static constexpr int TWMAX = sizeof(T) == 4 ? 16 : 8;
+  static constexpr int TW0 = 512 / TC;
+  static constexpr int TW = TW0 < 1 ? 1 : (TW0 > TWMAX ? TWMAX : TW0);
+  static constexpr int LGTW = ilog2(TW);
+  static constexpr int NT = TC * TW;
 };
 
 template <typename F>
@@ -24,32 +53,32 @@ int set_smem(F fn, size_t smem) {
 
 template <typename T, int M>
 bool zfwd_for(int pro, ZfwdFn<T> &fn, StaticGeom &g) {
-  using C = Cfg<T, M>;
-  if (pro == PRO_PLAIN) fn = ks_zfwd<T, PRO_PLAIN, M, C::LGTW, C::NT>;
-  else if (pro == PRO_DIFF) fn = ks_zfwd<T, PRO_DIFF, M, C::LGTW, C::NT>;
-  else fn = ks_zfwd<T, PRO_CLAMP, M, C::LGTW, C::NT>;
+  using C = Cfg<T, M, 8>;
+  if (pro == PRO_PLAIN) fn = ks_zfwd<T, PRO_PLAIN, M, C::LGTW>;
+  else if (pro == PRO_DIFF) fn = ks_zfwd<T, PRO_DIFF, M, C::LGTW>;
+  else fn = ks_zfwd<T, PRO_CLAMP, M, C::LGTW>;
   g.TW = C::TW;
   g.threads = C::NT;
-  g.smem = (size_t)(M + 1) * (C::TW + 1) * sizeof(c2<T>);
+  g.smem = (size_t)C::TW * row_pitch(M) * sizeof(c2<T>);
   return set_smem(fn, g.smem) == FFCZ_OK;
 }
 
 template <typename T, int M>
 bool zinv_for(ZinvFn<T> &fn, StaticGeom &g) {
-  using C = Cfg<T, M>;
-  fn = ks_zinv<T, M, C::LGTW, C::NT>;
+  using C = Cfg<T, M, 8>;
+  fn = ks_zinv<T, M, C::LGTW>;
   g.TW = C::TW;
   g.threads = C::NT;
-  g.smem = (size_t)(M + 1) * (C::TW + 1) * sizeof(c2<T>);
+  g.smem = (size_t)C::TW * row_pitch(M) * sizeof(c2<T>);
   return set_smem(fn, g.smem) == FFCZ_OK;
 }
 
 template <typename T, int L>
 bool strided_for(int mode, StridedFn<T> &fn, StaticGeom &g) {
   using C = Cfg<T, L>;
-  if (mode == MODE_FWD) fn = ks_strided<T, MODE_FWD, L, C::LGTW, C::NT>;
-  else if (mode == MODE_INV) fn = ks_strided<T, MODE_INV, L, C::LGTW, C::NT>;
-  else fn = ks_strided<T, MODE_FCI, L, C::LGTW, C::NT>;
+  if (mode == MODE_FWD) fn = ks_strided<T, MODE_FWD, L, C::LGTW>;
+  else if (mode == MODE_INV) fn = ks_strided<T, MODE_INV, L, C::LGTW>;
+  else fn = ks_strided<T, MODE_FCI, L, C::LGTW>;
   g.TW = C::TW;
   g.threads = C::NT;
   g.smem = (size_t)L * (C::TW + 1) * sizeof(c2<T>);
@@ -58,62 +87,41 @@ bool strided_for(int mode, StridedFn<T> &fn, StaticGeom &g) {
 
 }  // namespace
 
-#define CASES_F32(X) X(16) X(32) X(64) X(128) X(256) X(512) X(1024)
-#define CASES_F64(X) X(16) X(32) X(64) X(128) X(256) X(512)
+#define CASES_F32(X) X(16) X(32) X(64) X(128) X(256) X(512) X(1024) X(2048) X(4096)
+#define CASES_F64(X) X(16) X(32) X(64) X(128) X(256) X(512) X(1024) X(2048)
 
-template <>
-bool static_zfwd<float>(int M, int pro, ZfwdFn<float> &fn, StaticGeom &g) {
-  switch (M) {
-#define X(n) case n: return zfwd_for<float, n>(pro, fn, g);
-    CASES_F32(X)
-#undef X
-    default: return false;
+#define DEFINE_LOOKUPS(T, CASES)                                                  \
+  template <>                                                                     \
+  bool static_zfwd<T>(int M, int pro, ZfwdFn<T> &fn, StaticGeom &g) {             \
+    switch (M) {                                                                  \
+      CASES(ZF)                                                                   \
+      default: return false;                                                      \
+    }                                                                             \
+  }                                                                               \
+  template <>                                                                     \
+  bool static_zinv<T>(int M, ZinvFn<T> &fn, StaticGeom &g) {                      \
+    switch (M) {                                                                  \
+      CASES(ZI)                                                                   \
+      default: return false;                                                      \
+    }                                                                             \
+  }                                                                               \
+  template <>                                                                     \
+  bool static_strided<T>(int L, int mode, StridedFn<T> &fn, StaticGeom &g) {      \
+    switch (L) {                                                                  \
+      CASES(ST)                                                                   \
+      default: return false;                                                      \
+    }                                                                             \
   }
-}
-template <>
-bool static_zfwd<double>(int M, int pro, ZfwdFn<double> &fn, StaticGeom &g) {
-  switch (M) {
-#define X(n) case n: return zfwd_for<double, n>(pro, fn, g);
-    CASES_F64(X)
-#undef X
-    default: return false;
-  }
-}
-template <>
-bool static_zinv<float>(int M, ZinvFn<float> &fn, StaticGeom &g) {
-  switch (M) {
-#define X(n) case n: return zinv_for<float, n>(fn, g);
-    CASES_F32(X)
-#undef X
-    default: return false;
-  }
-}
-template <>
-bool static_zinv<double>(int M, ZinvFn<double> &fn, StaticGeom &g) {
-  switch (M) {
-#define X(n) case n: return zinv_for<double, n>(fn, g);
-    CASES_F64(X)
-#undef X
-    default: return false;
-  }
-}
-template <>
-bool static_strided<float>(int L, int mode, StridedFn<float> &fn, StaticGeom &g) {
-  switch (L) {
-#define X(n) case n: return strided_for<float, n>(mode, fn, g);
-    CASES_F32(X)
-#undef X
-    default: return false;
-  }
-}
-template <>
-bool static_strided<double>(int L, int mode, StridedFn<double> &fn, StaticGeom &g) {
-  switch (L) {
-#define X(n) case n: return strided_for<double, n>(mode, fn, g);
-    CASES_F64(X)
-#undef X
-    default: return false;
-  }
-}
+
+#define ZF(n) case n: return zfwd_for<TT, n>(pro, fn, g);
+#define ZI(n) case n: return zinv_for<TT, n>(fn, g);
+#define ST(n) case n: return strided_for<TT, n>(mode, fn, g);
+
+#define TT float
+DEFINE_LOOKUPS(float, CASES_F32)
+#undef TT
+#define TT double
+DEFINE_LOOKUPS(double, CASES_F64)
+#undef TT
 
 }  // namespace ffcz

@@ -1,5 +1,9 @@
-// Lookup of the compile-time-sized pass kernels (passes_static.cuh).
+// Lookup of the compile-time-sized register-resident pass kernels
+// (passes_static.cuh) and construction of their twiddle tables.
 #pragma once
+
+#include <complex>
+#include <vector>
 
 #include "passes.cuh"
 
@@ -18,8 +22,16 @@ struct StaticGeom {
   size_t smem = 0;   // dynamic shared memory bytes
 };
 
-// Kernel for a power-of-two length, or false when none is compiled in.
-// z passes: M = Nz/2 (even Nz only); pro is PRO_PLAIN/PRO_DIFF/PRO_CLAMP.
+// True when a compile-time kernel exists for this length (power of two,
+// 16..4096 for FP32, 16..2048 for FP64).
+bool static_length(int L, bool fp64);
+// Appends the forward and inverse stage twiddles of length L to `table`
+// and fills p.twoff (forward at [s], inverse at [12 + s]); p.tw left null.
+// cap = 16 for the strided passes' stage lists, 8 for the z passes'.
+void build_static_plan(int L, int cap, AxisPlan &p, std::vector<std::complex<double>> &table);
+
+// Kernel for a length static_length() accepts (false otherwise).
+// z passes: M = Nz/2; pro is PRO_PLAIN/PRO_DIFF/PRO_CLAMP.
 template <typename T> bool static_zfwd(int M, int pro, ZfwdFn<T> &fn, StaticGeom &g);
 template <typename T> bool static_zinv(int M, ZinvFn<T> &fn, StaticGeom &g);
 template <typename T> bool static_strided(int L, int mode, StridedFn<T> &fn, StaticGeom &g);
