@@ -46,6 +46,11 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "Input GB/s (project+encode) on 1 GB300, mixed-prec vs plain FP32, bounds met"
 PEAKS = ROOT / "MEASURED_PEAKS.json"
+# DRAM bytes read + written per launch of each pass, from one
+# `ncu --set full` capture of the same workload (profiles/passes_plain256_ncu.md;
+# cold-cache replays, writes still dirty in L2 at kernel exit not counted).
+TRAFFIC = {"plain256": {"zfwd_r2c": 169.0e6, "y_fwd": 89.3e6, "x_fwd_clamp_inv": 91.5e6, "y_inv": 89.3e6,
+                        "zinv_c2r_viol": 98.2e6}}
 
 
 def parse():
@@ -330,7 +335,8 @@ def run_ours(args):
         "e2e": {"value": N * dt.itemsize * args.steps * world / t_e2e / 1e9, "unit": "GB/s",
                 "h2d_bytes_per_step": 2 * N * dt.itemsize, "d2h_bytes_per_step": d2h},
         "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "peak_source": f"{peak_kind} hbm_gbs", "traffic": None,
+                     "frac": achieved / peak, "peak_source": f"{peak_kind} hbm_gbs",
+                     "traffic": TRAFFIC.get(args.workload, {}).get(names[dom]),
                      "algorithmic_bytes_per_launch": by_dom, "avg_launch_ms": ms_dom},
         "passes": {names[i]: {"ms": round(m, 5), "GB/s": round(b / (m / 1e3) / 1e9, 1)} for i, (m, b) in avg.items()},
         "gpu_launches": launches,

@@ -20,11 +20,17 @@
 #include <cuda_runtime.h>
 #include <cufft.h>
 
+// The reference header reaches <cstring>, <algorithm> and friends through
+// <cub/cub.cuh>; code written against it (projection_example.cu uses
+// std::strcmp) relies on that, so they are included here explicitly.
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
+#include <cstring>
 #include <iostream>
+#include <memory>
 #include <stdexcept>
 #include <string>
 #include <type_traits>
