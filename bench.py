@@ -56,13 +56,15 @@ TRAFFIC = {"plain256": {"zfwd_r2c": 169.0e6, "y_fwd": 89.3e6, "x_fwd_clamp_inv":
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="plain256")
     ap.add_argument("--zstd-level", type=int, default=20)
     ap.add_argument("--zstd-mode", default="single", choices=["single", "chunked"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--zstd-threads", type=int, default=0,
+                    help="host threads of the ZSTD pool (default: cores - 2, at least 1)")
     ap.add_argument("--loop", default="graph", choices=["graph", "host"],
                     help="iteration driver; 'host' runs the same kernels outside a graph (for ncu)")
     return ap.parse_args()
@@ -245,7 +247,8 @@ def run_ours(args):
     s.set_profiling(True)
     s.initialize_all_abs_device(dx, fld.eps, fld.delta)
 
-    pool = ThreadPoolExecutor(max_workers=os.cpu_count())
+    nzt = args.zstd_threads or max(1, (os.cpu_count() or 2) - 2)
+    pool = ThreadPoolExecutor(max_workers=nzt)
 
     def zstd_jobs(res):
         return [pool.submit(F.zstd_compress, r.bitstream, args.zstd_level, zmode) for r in res if r is not None]
@@ -253,14 +256,14 @@ def run_ours(args):
     def step_device():
         s.reset_edit_accumulators()
         s.solve_all_abs_pair_device(dx, dxp, max_iter, 1e-7)
-        res = s.encode(-1)  # Huffman bitstreams; ZSTD runs on the pool
+        res = s.encode(args.zstd_level, F.FFCZ_ZSTD_NONE)  # Huffman bitstreams; ZSTD on the pool
         return s.launch_count(), res, zstd_jobs(res)
 
     def step_e2e():
         s.reset_edit_accumulators()
         s.initialize_all_abs(x_h.numpy(), fld.eps, fld.delta)
         s.solve_all_abs(e0_h.numpy(), max_iter, 1e-7)
-        res = s.encode(-1)
+        res = s.encode(args.zstd_level, F.FFCZ_ZSTD_NONE)
         return res, zstd_jobs(res)
 
     for _ in range(args.warmup):
@@ -276,6 +279,23 @@ def run_ours(args):
     serial = s.encode(args.zstd_level, zmode)
     assert [r.compressed_data for r in serial if r is not None] == comp1
     torch.cuda.synchronize()
+    # where the host-side time of one step goes
+    tb = [time.perf_counter()]
+    s.reset_edit_accumulators()
+    tb.append(time.perf_counter())
+    s.solve_all_abs_pair_device(dx, dxp, max_iter, 1e-7)
+    tb.append(time.perf_counter())
+    res_b = s.encode(args.zstd_level, F.FFCZ_ZSTD_NONE)
+    tb.append(time.perf_counter())
+    s.pass_times()
+    tb.append(time.perf_counter())
+    jobs_b = zstd_jobs(res_b)
+    tb.append(time.perf_counter())
+    for f in jobs_b:
+        f.result()
+    tb.append(time.perf_counter())
+    breakdown = dict(zip(["reset", "solve", "huffman", "pass_times", "submit", "zstd_wait"],
+                         [round(1e3 * (b - a), 2) for a, b in zip(tb, tb[1:])]))
     clocks = Clocks()
     barrier(world)
     torch.cuda.synchronize()
@@ -284,12 +304,14 @@ def run_ours(args):
     pass_ms = {}
     ev0.record()
     jobs = []
+    t_host0 = time.perf_counter()
     for _ in range(args.steps):
         n, out, j = step_device()
         jobs += j
         launches += n
         for i, (ms, by) in enumerate(s.pass_times()):
             pass_ms.setdefault(i, []).append((ms, by))
+    t_serial = (time.perf_counter() - t_host0) / args.steps
     comp = [f.result() for f in jobs]
     ev1.record()
     torch.cuda.synchronize()
@@ -341,6 +363,9 @@ def run_ours(args):
         "passes": {names[i]: {"ms": round(m, 5), "GB/s": round(b / (m / 1e3) / 1e9, 1)} for i, (m, b) in avg.items()},
         "gpu_launches": launches,
         "step_latency_ms": 1e3 * step_latency,
+        "serial_ms_per_step": 1e3 * t_serial,
+        "serial_breakdown_ms": breakdown,
+        "zstd_threads": nzt,
         "active_edits": {"freq": counts[0], "spatial": counts[1]},
         "compressed_bytes": comp_bytes,
         "clocks": clk,

@@ -17,7 +17,6 @@ from __future__ import annotations
 
 import ctypes as C
 import os
-from dataclasses import dataclass, field
 from pathlib import Path
 
 import numpy as np
@@ -29,7 +28,7 @@ FFCZ_OK = 0
 FFCZ_F32, FFCZ_F64 = 0, 1
 FFCZ_PACK_CORRECT, FFCZ_PACK_REFERENCE = 0, 1
 FFCZ_LOOP_GRAPH, FFCZ_LOOP_HOST = 0, 1
-FFCZ_ZSTD_SINGLE, FFCZ_ZSTD_CHUNKED = 0, 1
+FFCZ_ZSTD_SINGLE, FFCZ_ZSTD_CHUNKED, FFCZ_ZSTD_NONE = 0, 1, 2
 ERRORS = {-1: "INVALID", -2: "CUDA", -3: "UNSUPPORTED", -4: "NOT_INITIALIZED", -5: "ZSTD",
           -6: "CAPACITY", -7: "CODE_TOO_LONG", -8: "EMPTY", -9: "IO"}
 
@@ -108,6 +107,7 @@ SIGNATURES = {
     "ffcz_huff_result_compressed": [_p, _p, _sz],
     "ffcz_huff_result_bitstream": [_p, _p, _sz],
     "ffcz_huff_result_codes": [_p, _p, _p, _p, _sz],
+    "ffcz_huff_result_view": [_p, _i, _PP, _SP],
     "ffcz_huff_decompress_u16": [_p, _sz, _p, _p, _p, _sz, _sz, _sz, _p, _SP],
     "ffcz_huff_decompress_u8": [_p, _sz, _p, _p, _p, _sz, _sz, _sz, _p, _SP],
     "ffcz_solver_encode": [_p, _i, _i, C.POINTER(C.c_void_p * 4)],
@@ -337,45 +337,66 @@ class ProjectionSolver:
         return v.value
 
     def encode(self, zstd_level: int = 20, zstd_mode: int = FFCZ_ZSTD_SINGLE) -> list:
-        """The four streams of projection_example.cu:230-246 (None where skipped)."""
+        """The four streams of projection_example.cu:230-246 (None where skipped).
+        FFCZ_ZSTD_NONE returns the Huffman bitstreams with empty compressed_data."""
         arr = (C.c_void_p * 4)()
         _check(lib().ffcz_solver_encode(self._h, zstd_level, zstd_mode, C.byref(arr)))
         return [None if not p else _take_result(p) for p in arr]
 
 
 # ---------------------------------------------------------------------------
-@dataclass
 class CompressionResult:
-    """SimpleCudaHuffmanZstdCompressor<T>::CompressionResult (HuffmanZSTDCoder.cuh:240-246)."""
-    compressed_data: bytes
-    code_table: dict = field(repr=False)      # symbol -> (code, length)
-    original_bitstream_size: int
-    num_elements: int
-    bitstream: bytes = field(repr=False, default=b"")
+    """SimpleCudaHuffmanZstdCompressor<T>::CompressionResult (HuffmanZSTDCoder.cuh:240-246).
+
+    ``compressed_data`` (bytes), ``original_bitstream_size``, ``num_elements``;
+    the code table as arrays (``symbols``, ``codes``, ``lengths``, ascending
+    symbols) and as the reference's map ``code_table`` (built on first use)."""
+
+    def __init__(self, compressed_data, symbols, codes, lengths, original_bitstream_size, num_elements,
+                 bitstream=b""):
+        self.compressed_data = compressed_data
+        self.symbols, self.codes, self.lengths = symbols, codes, lengths
+        self.original_bitstream_size = original_bitstream_size
+        self.num_elements = num_elements
+        self.bitstream = bitstream
+        self._table = None
+
+    @property
+    def code_table(self) -> dict:
+        if self._table is None:
+            self._table = dict(zip(self.symbols.tolist(), zip(self.codes.tolist(), self.lengths.tolist())))
+        return self._table
 
     def arrays(self):
-        syms = np.array(sorted(self.code_table), dtype=np.uint32)
-        codes = np.array([self.code_table[s][0] for s in syms], dtype=np.uint32)
-        lens = np.array([self.code_table[s][1] for s in syms], dtype=np.int32)
-        return syms, codes, lens
+        return self.symbols, self.codes, self.lengths
+
+    def __repr__(self):
+        return (f"CompressionResult(compressed={len(self.compressed_data)} B, bitstream="
+                f"{self.original_bitstream_size} B, elements={self.num_elements}, symbols={self.symbols.size})")
+
+
+def _view(p, which):
+    ptr, n = C.c_void_p(), C.c_size_t()
+    _check(lib().ffcz_huff_result_view(p, which, C.byref(ptr), C.byref(n)))
+    return ptr.value, n.value
 
 
 def _take_result(p: int) -> CompressionResult:
-    L = lib()
-    comp, bits, nel, nsym = (C.c_size_t() for _ in range(4))
-    _check(L.ffcz_huff_result_sizes(p, C.byref(comp), C.byref(bits), C.byref(nel), C.byref(nsym)))
-    cbuf = np.empty(max(comp.value, 1), np.uint8)
-    bbuf = np.empty(max(bits.value, 1), np.uint8)
-    _check(L.ffcz_huff_result_compressed(p, _np_ptr(cbuf), cbuf.size))
-    _check(L.ffcz_huff_result_bitstream(p, _np_ptr(bbuf), bbuf.size))
-    k = max(nsym.value, 1)
-    syms, codes, lens = np.empty(k, np.uint32), np.empty(k, np.uint32), np.empty(k, np.int32)
-    if nsym.value:
-        _check(L.ffcz_huff_result_codes(p, _np_ptr(syms), _np_ptr(codes), _np_ptr(lens), k))
-    table = {int(syms[i]): (int(codes[i]), int(lens[i])) for i in range(nsym.value)}
-    r = CompressionResult(bytes(cbuf[: comp.value]), table, bits.value, nel.value, bytes(bbuf[: bits.value]))
-    L.ffcz_huff_result_free(p)
-    return r
+    """Copies a native result into Python objects and frees it."""
+    try:
+        cp, cn = _view(p, 0)
+        bp, bn = _view(p, 1)
+        bits = C.string_at(bp, bn) if bn else b""
+        comp = C.string_at(cp, cn) if cn else b""
+        arrs = []
+        for which, dt in ((2, np.uint32), (3, np.uint32), (4, np.int32)):
+            ap, an = _view(p, which)
+            arrs.append(np.frombuffer(C.string_at(ap, an * 4), dt) if an else np.zeros(0, dt))
+        nel = C.c_size_t()
+        _check(lib().ffcz_huff_result_sizes(p, None, None, C.byref(nel), None))
+        return CompressionResult(comp, *arrs, bn, nel.value, bits)
+    finally:
+        lib().ffcz_huff_result_free(p)
 
 
 def cuda_huffman_zstd_compress(data, zstd_level: int = 3) -> CompressionResult:
@@ -410,13 +431,18 @@ def zstd_compress(data: bytes, level: int, mode: int = FFCZ_ZSTD_SINGLE) -> byte
     return bytes(dst[: n.value])
 
 
-def cuda_huffman_zstd_decompress(compressed: bytes, code_table: dict, num_elements: int,
+def cuda_huffman_zstd_decompress(compressed: bytes, code_table, num_elements: int,
                                  original_bitstream_size: int, dtype=np.uint16) -> np.ndarray:
-    """cudaHuffmanZstdDecompress<T> (HuffmanZSTDCoder.cuh:462-470)."""
+    """cudaHuffmanZstdDecompress<T> (HuffmanZSTDCoder.cuh:462-470).  code_table:
+    {symbol: (code, length)} or a (symbols, codes, lengths) array triple."""
     dtype = np.dtype(dtype)
-    syms = np.array(sorted(code_table), dtype=np.uint32)
-    codes = np.array([code_table[s][0] for s in syms], dtype=np.uint32)
-    lens = np.array([code_table[s][1] for s in syms], dtype=np.int32)
+    if isinstance(code_table, dict):
+        syms = np.array(sorted(code_table), dtype=np.uint32)
+        codes = np.array([code_table[s][0] for s in syms], dtype=np.uint32)
+        lens = np.array([code_table[s][1] for s in syms], dtype=np.int32)
+    else:
+        syms, codes, lens = (np.ascontiguousarray(a, dt) for a, dt in
+                             zip(code_table, (np.uint32, np.uint32, np.int32)))
     comp = np.frombuffer(compressed, np.uint8) if len(compressed) else np.zeros(1, np.uint8)
     out = np.empty(max(num_elements, 1), dtype)
     n = C.c_size_t()

@@ -340,8 +340,8 @@ int huff_encode_device(HuffWorkspace &ws, const void *d_data, size_t n, int symb
 }
 
 int huff_zstd(ffcz_huff_result &res, int level, int mode) {
-  if (level < 0) {
-    res.compressed = res.bitstream;
+  if (mode == FFCZ_ZSTD_NONE) {
+    res.compressed.clear();
     return FFCZ_OK;
   }
   return zstd_compress(res.bitstream.data(), res.bitstream.size(), level, mode == FFCZ_ZSTD_CHUNKED,
@@ -405,6 +405,7 @@ int ffcz_huff_compress_u8(const uint8_t *h_data, size_t n, int zstd_level, ffcz_
 int ffcz_huff_compress_device(const void *d_data, size_t n, int symbol_bytes, int zstd_level, int zstd_mode,
                               void *stream, ffcz_huff_result **out) {
   if (symbol_bytes != 1 && symbol_bytes != 2) return fail(FFCZ_ERR_INVALID, "symbol_bytes must be 1 or 2");
+  if (zstd_mode < FFCZ_ZSTD_SINGLE || zstd_mode > FFCZ_ZSTD_NONE) return fail(FFCZ_ERR_INVALID, "unknown ZSTD mode");
   return global_encode(d_data, n, symbol_bytes, false, zstd_level, zstd_mode, (cudaStream_t)stream, out);
 }
 void ffcz_huff_result_free(ffcz_huff_result *r) { delete r; }
@@ -414,6 +415,7 @@ size_t ffcz_zstd_bound(size_t n) { return zstd_bound(n); }
 int ffcz_zstd_compress(const uint8_t *src, size_t n, int level, int mode, uint8_t *dst, size_t cap,
                        size_t *out_len) {
   if ((!src && n) || !dst || !out_len) return fail(FFCZ_ERR_INVALID, "NULL argument");
+  if (mode != FFCZ_ZSTD_SINGLE && mode != FFCZ_ZSTD_CHUNKED) return fail(FFCZ_ERR_INVALID, "unknown ZSTD mode");
   std::vector<uint8_t> out;
   FFCZ_TRY(zstd_compress(src, n, level, mode == FFCZ_ZSTD_CHUNKED, out));
   *out_len = out.size();
@@ -437,6 +439,19 @@ int ffcz_huff_result_compressed(const ffcz_huff_result *r, uint8_t *dst, size_t 
   if (!r->compressed.empty()) std::memcpy(dst, r->compressed.data(), r->compressed.size());
   return FFCZ_OK;
 }
+int ffcz_huff_result_view(const ffcz_huff_result *r, int which, const void **ptr, size_t *count) {
+  if (!r || !ptr || !count) return fail(FFCZ_ERR_INVALID, "NULL argument");
+  switch (which) {
+    case 0: *ptr = r->compressed.data(); *count = r->compressed.size(); break;
+    case 1: *ptr = r->bitstream.data(); *count = r->bitstream.size(); break;
+    case 2: *ptr = r->symbols.data(); *count = r->symbols.size(); break;
+    case 3: *ptr = r->codes.data(); *count = r->codes.size(); break;
+    case 4: *ptr = r->lengths.data(); *count = r->lengths.size(); break;
+    default: return fail(FFCZ_ERR_INVALID, "unknown buffer");
+  }
+  return FFCZ_OK;
+}
+
 int ffcz_huff_result_bitstream(const ffcz_huff_result *r, uint8_t *dst, size_t cap) {
   if (!r || (!dst && !r->bitstream.empty())) return fail(FFCZ_ERR_INVALID, "NULL argument");
   if (cap < r->bitstream.size()) return fail(FFCZ_ERR_CAPACITY, "destination too small");

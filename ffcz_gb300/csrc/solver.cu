@@ -862,6 +862,7 @@ int ffcz_solver_encode(ffcz_solver *s, int zstd_level, int zstd_mode, ffcz_huff_
   if (!out4) return fail(FFCZ_ERR_INVALID, "out4 is NULL");
   for (int i = 0; i < 4; ++i) out4[i] = nullptr;
   if (!s->extracted) return fail(FFCZ_ERR_INVALID, "extract before encode");
+  if (zstd_mode < FFCZ_ZSTD_SINGLE || zstd_mode > FFCZ_ZSTD_NONE) return fail(FFCZ_ERR_INVALID, "unknown ZSTD mode");
   const size_t cf = s->h_ctl->count[0], cs = s->h_ctl->count[1];
   struct Job { const void *d; size_t n; int sb; };
   Job jobs[4] = {{s->d_fquant, cf, 2}, {s->d_fpack, cf ? (2 * s->H + 7) / 8 : 0, 1},
@@ -875,6 +876,7 @@ int ffcz_solver_encode(ffcz_solver *s, int zstd_level, int zstd_mode, ffcz_huff_
     FFCZ_TRY(huff_encode_device(s->huff, jobs[i].d, jobs[i].n, jobs[i].sb, s->stream, *res[i]));
     launches += s->huff.launches;
     ffcz_huff_result *r = res[i].get();
+    if (zstd_mode == FFCZ_ZSTD_NONE) continue;
     z.push_back(std::async(std::launch::async, [r, zstd_level, zstd_mode] { return huff_zstd(*r, zstd_level, zstd_mode); }));
   }
   int rc = FFCZ_OK;

@@ -186,6 +186,7 @@ typedef struct ffcz_huff_result ffcz_huff_result;
 #define FFCZ_ZSTD_SINGLE 0   /* one ZSTD_compress call (reference :359-375) */
 #define FFCZ_ZSTD_CHUNKED 1  /* independent frames over host threads; the  */
                              /* concatenation decodes with ZSTD_decompress */
+#define FFCZ_ZSTD_NONE 2     /* Huffman bitstream only (no ZSTD stage)     */
 
 /* compress(data, level) for T = uint16_t / uint8_t from HOST data --
  * HuffmanZSTDCoder.cuh:248-376.  Histogram, code lengths, bit offsets and
@@ -198,7 +199,6 @@ int ffcz_huff_compress_u8(const uint8_t *h_data, size_t n, int zstd_level,
 int ffcz_huff_compress_device(const void *d_data, size_t n, int symbol_bytes,
                               int zstd_level, int zstd_mode, void *stream,
                               ffcz_huff_result **out);
-/* Huffman bitstream only, no ZSTD (ZSTD level < 0 means the same). */
 void ffcz_huff_result_free(ffcz_huff_result *r);
 /* CompressionResult fields (:240-246). */
 int ffcz_huff_result_sizes(const ffcz_huff_result *r, size_t *compressed_bytes,
@@ -212,6 +212,11 @@ int ffcz_huff_result_bitstream(const ffcz_huff_result *r, uint8_t *dst,
 /* Code table as three parallel arrays in ascending symbol order. */
 int ffcz_huff_result_codes(const ffcz_huff_result *r, uint32_t *symbols,
                            uint32_t *codes, int32_t *lengths, size_t cap);
+/* Read-only view of a result's buffers, valid until the result is freed:
+ * which = 0 compressed bytes, 1 bitstream bytes, 2 symbols (uint32),
+ * 3 codes (uint32), 4 lengths (int32); *count = elements. */
+int ffcz_huff_result_view(const ffcz_huff_result *r, int which,
+                          const void **ptr, size_t *count);
 
 /* The ZSTD stage alone (HuffmanZSTDCoder.cuh:359-375) on host bytes, so
  * that callers can run it on their own threads, overlapped with the GPU
