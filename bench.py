@@ -82,21 +82,15 @@ def dist_init(n):
 
 
 def barrier(world):
-    if world > 1:
-        import torch.distributed as dist
+    from ffcz_gb300 import replicas
 
-        dist.barrier()
+    replicas.barrier()
 
 
 def max_over_ranks(v, world):
-    if world == 1:
-        return v
-    import torch
-    import torch.distributed as dist
+    from ffcz_gb300 import replicas
 
-    t = torch.tensor([v], dtype=torch.float64, device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    return float(t.item())
+    return replicas.max_over_ranks(v, device="cuda" if world > 1 else None)
 
 
 class Clocks:
@@ -322,6 +316,14 @@ def run_ours(args):
     comp_bytes = sum(len(c) for c in comp[-len(j):]) if j else 0
     its = s.iterations
     counts = s.active_counts()
+    # FP64 check of both bounds on the corrected field x^ = x + e
+    from oracle import ffcz_oracle as O  # checker only, outside the timed region
+
+    e_fin = s.get_results()
+    bchk = O.check_bounds(np.zeros(1), e_fin.astype(np.float64), fld.eps, fld.delta)
+    bounds = {"spatial_max_over_E": bchk["spatial_max"] / fld.eps, "freq_max_over_Delta": bchk["freq_max"] / fld.delta,
+              "met": bool(bchk["spatial_excess"] <= 1e-7 and bchk["freq_excess"] <= 0.0),
+              "rule": "reference schedule: spatial within E + tol (1e-7), frequency within Delta"}
 
     # e2e through the reference-facing API with host buffers
     for _ in range(max(1, args.warmup // 2)):
@@ -367,6 +369,7 @@ def run_ours(args):
         "serial_breakdown_ms": breakdown,
         "zstd_threads": nzt,
         "active_edits": {"freq": counts[0], "spatial": counts[1]},
+        "bounds_fp64": bounds,
         "compressed_bytes": comp_bytes,
         "clocks": clk,
     }
