@@ -16,7 +16,10 @@ from pathlib import Path
 PKG = Path(__file__).resolve().parent
 ROOT = PKG.parent
 CSRC = PKG / "csrc"
-OUT = PKG / "_build"
+# FFCZ_BUILD_DIR / FFCZ_NVCC_FLAGS build variants (other tile or twiddle
+# settings) next to the default library without touching it.
+OUT = Path(os.environ.get("FFCZ_BUILD_DIR", str(PKG / "_build")))
+EXTRA = os.environ.get("FFCZ_NVCC_FLAGS", "").split()
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 LIB_SOURCES = ["solver.cu", "static_kernels.cu", "huffman.cu", "legacy_kernels.cu", "noalloc.cu", "fft_plan.cpp",
                "huffman_host.cpp", "capi_misc.cpp"]
@@ -30,7 +33,7 @@ def nvcc() -> str:
 
 
 def _flags(src: Path) -> list[str]:
-    common = ["-std=c++17", "-O3", "-Xcompiler", "-fPIC", f"-I{ROOT / 'include'}", f"-I{CSRC}"]
+    common = ["-std=c++17", "-O3", "-Xcompiler", "-fPIC", f"-I{ROOT / 'include'}", f"-I{CSRC}"] + EXTRA
     if src.suffix == ".cu":
         return common + ARCH + ["-lineinfo", "-Xptxas", "-warn-spills"]
     return common
@@ -55,7 +58,7 @@ def _stale(target: Path, deps: list[Path]) -> bool:
 
 def build(verbose: bool = False, force: bool = False) -> Path:
     """Compiles libffcz.so and the fftz CLI; returns the library path."""
-    OUT.mkdir(exist_ok=True)
+    OUT.mkdir(parents=True, exist_ok=True)
     headers = list(CSRC.glob("*.cuh")) + list(CSRC.glob("*.h")) + list((ROOT / "include").glob("*"))
     jobs = []
     objs = []

@@ -25,6 +25,11 @@ namespace ffcz {
 
 constexpr int kInvBase = 12;
 
+// Twiddles of the strided passes' stages are stored R per k (entry 0
+// unused) so that a butterfly's R-1 twiddles are 16-byte aligned and read in
+// pairs: there a warp's lanes share few twiddle rows.  The z passes' lanes
+// each need a different row, and their tables keep R-1 per k.
+
 __host__ __device__ constexpr int ilog2(int n) { return n <= 1 ? 0 : 1 + ilog2(n >> 1); }
 
 // Stage lists.  Strided passes (CAP 16): 16:[16] 32:[8,4] 64:[8,8]
@@ -102,7 +107,7 @@ template <int DIR, typename V> struct Dft<16, DIR, V> {
 
 // Butterflies of one stage on the thread's registers: v[m*R + r] is input
 // r of butterfly m (j = t + m*TC) and becomes output r.
-template <typename T, int DIR, int R, int LGNS, int L, int E>
+template <typename T, int DIR, int R, int LGNS, int L, int E, bool VEC>
 __device__ __forceinline__ void rstage(c2<T> (&v)[E], int t, const c2<T> *__restrict__ tw) {
   using V = c2<T>;
   constexpr int TC = L / E, NS = 1 << LGNS;
@@ -110,11 +115,29 @@ __device__ __forceinline__ void rstage(c2<T> (&v)[E], int t, const c2<T> *__rest
   for (int m = 0; m < E / R; ++m) {
     if (NS > 1) {
       const int j = t + m * TC;
-      const V *w = tw + (j & (NS - 1)) * (R - 1);
+      if constexpr (VEC) {
+        const V *w = tw + (j & (NS - 1)) * R;
+        V ww[R];
+        if (sizeof(T) == 4) {
 #pragma unroll
-      for (int r = 1; r < R; ++r) {
-        const V ww = w[r - 1];
-        v[m * R + r] = (DIR < 0) ? cmul(v[m * R + r], ww) : cmulc(v[m * R + r], ww);
+          for (int r = 0; r < R; r += 2) {
+            const float4 q = *reinterpret_cast<const float4 *>(w + r);
+            ww[r] = mkc<T>((T)q.x, (T)q.y);
+            ww[r + 1] = mkc<T>((T)q.z, (T)q.w);
+          }
+        } else {
+#pragma unroll
+          for (int r = 1; r < R; ++r) ww[r] = w[r];
+        }
+#pragma unroll
+        for (int r = 1; r < R; ++r) v[m * R + r] = (DIR < 0) ? cmul(v[m * R + r], ww[r]) : cmulc(v[m * R + r], ww[r]);
+      } else {
+        const V *w = tw + (j & (NS - 1)) * (R - 1);
+#pragma unroll
+        for (int r = 1; r < R; ++r) {
+          const V ww = w[r - 1];
+          v[m * R + r] = (DIR < 0) ? cmul(v[m * R + r], ww) : cmulc(v[m * R + r], ww);
+        }
       }
     }
     Dft<R, DIR, V>::run(&v[m * R]);
@@ -155,7 +178,7 @@ struct RRun {
     if constexpr (S < rp_nst(L, CAP)) {
       constexpr int R = rp_rad(L, DIR, S, CAP), LG = rp_lgns(L, DIR, S, CAP);
       const c2<T> *tw = (const c2<T> *)p.tw + p.twoff[(DIR < 0 ? 0 : kInvBase) + S];
-      rstage<T, DIR, R, LG, L, E>(v, t, tw);
+      rstage<T, DIR, R, LG, L, E, CAP == 16>(v, t, tw);
       if constexpr (S + 1 < rp_nst(L, CAP)) {
         constexpr int R2 = rp_rad(L, DIR, S + 1, CAP);
 #pragma unroll

@@ -19,10 +19,13 @@ void build_static_plan(int L, int cap, AxisPlan &p, std::vector<std::complex<dou
     long long Ns = 1;
     for (int s = 0; s < rp_nst(L, cap); ++s) {
       const int R = rp_rad(L, dir, s, cap);
+      // strided lists (cap 16): R entries per k from a 16-byte aligned start
+      const bool vec = cap == 16;
+      while (vec && table.size() % 2) table.push_back({1.0, 0.0});
       p.twoff[(dir < 0 ? 0 : kInvBase) + s] = (int)table.size();
       if (Ns > 1)
         for (long long k = 0; k < Ns; ++k)
-          for (int r = 1; r < R; ++r) {
+          for (int r = vec ? 0 : 1; r < R; ++r) {
             const long long d = Ns * R, a = (r * k) % d;
             const double th = -2.0 * M_PI * (double)a / (double)d;
             table.push_back({std::cos(th), std::sin(th)});
@@ -34,11 +37,17 @@ void build_static_plan(int L, int cap, AxisPlan &p, std::vector<std::complex<dou
 
 namespace {
 
+#ifndef FFCZ_TILE_THREADS
+#define FFCZ_TILE_THREADS 512
+#endif
+
 template <typename T, int L, int CAP = 16>
 struct Cfg {
   static constexpr int TC = L / rp_elems(L, CAP);
   static constexpr int TWMAX = sizeof(T) == 4 ? 16 : 8;
-  static constexpr int TW0 = 512 / TC;
+  // radix-16 lists hold 16 values per thread (~80-100 registers): at most
+  // 512 threads; radix-8 lists (~64 registers) may use FFCZ_TILE_THREADS
+  static constexpr int TW0 = (rp_elems(L, CAP) == 16 ? 512 : FFCZ_TILE_THREADS) / TC;
   static constexpr int TW = TW0 < 1 ? 1 : (TW0 > TWMAX ? TWMAX : TW0);
   static constexpr int LGTW = ilog2(TW);
   static constexpr int NT = TC * TW;
