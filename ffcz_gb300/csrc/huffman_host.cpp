@@ -131,6 +131,11 @@ struct Zstd {
   size_t (*decompress)(void *, size_t, const void *, size_t) = nullptr;
   unsigned (*isError)(size_t) = nullptr;
   const char *(*getErrorName)(size_t) = nullptr;
+  // optional: a context kept per thread keeps level-20 match tables (tens of
+  // MB) mapped between calls; ZSTD_compressCCtx writes ZSTD_compress's bytes
+  void *(*createCCtx)() = nullptr;
+  size_t (*freeCCtx)(void *) = nullptr;
+  size_t (*compressCCtx)(void *, void *, size_t, const void *, size_t, int) = nullptr;
   bool ok = false;
   std::string why;
 };
@@ -149,6 +154,10 @@ Zstd &zstd() {
     z.decompress = (size_t(*)(void *, size_t, const void *, size_t))dlsym(h, "ZSTD_decompress");
     z.isError = (unsigned (*)(size_t))dlsym(h, "ZSTD_isError");
     z.getErrorName = (const char *(*)(size_t))dlsym(h, "ZSTD_getErrorName");
+    z.createCCtx = (void *(*)())dlsym(h, "ZSTD_createCCtx");
+    z.freeCCtx = (size_t(*)(void *))dlsym(h, "ZSTD_freeCCtx");
+    z.compressCCtx = (size_t(*)(void *, void *, size_t, const void *, size_t, int))dlsym(h, "ZSTD_compressCCtx");
+    if (!z.createCCtx || !z.freeCCtx || !z.compressCCtx) z.createCCtx = nullptr;
     z.ok = z.compressBound && z.compress && z.decompress && z.isError && z.getErrorName;
     if (!z.ok) z.why = "libzstd.so.1 lacks a required symbol";
   });
@@ -162,11 +171,23 @@ bool zstd_available(std::string *why) {
   return z.ok;
 }
 
+namespace {
+struct ThreadCCtx {
+  void *ctx = nullptr;
+  ~ThreadCCtx() {
+    if (ctx) zstd().freeCCtx(ctx);
+  }
+};
+}  // namespace
+
 static int compress_one(const uint8_t *src, size_t n, int level, std::vector<uint8_t> &out) {
   Zstd &z = zstd();
   const size_t bound = z.compressBound(n);
   out.resize(bound);
-  const size_t r = z.compress(out.data(), bound, src, n, level);
+  thread_local ThreadCCtx tc;
+  if (z.createCCtx && !tc.ctx) tc.ctx = z.createCCtx();
+  const size_t r = tc.ctx ? z.compressCCtx(tc.ctx, out.data(), bound, src, n, level)
+                          : z.compress(out.data(), bound, src, n, level);
   if (z.isError(r)) return fail(FFCZ_ERR_ZSTD, std::string("ZSTD compression failed: ") + z.getErrorName(r));
   out.resize(r);
   return FFCZ_OK;

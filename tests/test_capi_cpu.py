@@ -92,3 +92,22 @@ def test_solver_create_without_gpu_fails_cleanly():
     with pytest.raises(F.FFCzError) as ei:
         F.ProjectionSolver(8, 8, 8)
     assert ei.value.code == -2
+
+
+def test_zstd_stage_bytes_equal_zstd_compress():
+    """The native ZSTD stage reuses one compression context per thread; its
+    bytes must stay ZSTD_compress's for every size and level, in any order,
+    from any thread (HuffmanZSTDCoder.cuh:359-365)."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    rng = np.random.default_rng(7)
+    cases = []
+    for n, level in ((0, 3), (1, 20), (1000, 1), (70_000, 20), (300_000, 3), (5_000, 19), (300_000, 20)):
+        # skewed bytes, like a Huffman bitstream of a peaked histogram
+        cases.append((rng.geometric(0.2, n).astype(np.uint8).tobytes(), level))
+    expect = [O.zstd_compress(d, lv) for d, lv in cases]
+    assert [F.zstd_compress(d, lv) for d, lv in cases] == expect
+    assert [F.zstd_compress(d, lv) for d, lv in reversed(cases)] == expect[::-1]
+    with ThreadPoolExecutor(3) as pool:
+        got = list(pool.map(lambda c: F.zstd_compress(*c), cases * 2))
+    assert got == expect * 2
