@@ -117,6 +117,11 @@ SIGNATURES = {
                                       C.POINTER(C.c_double)],
     "ffcz_read_raw": [C.c_char_p, _p, _sz, _sz],
     "ffcz_write_raw": [C.c_char_p, _p, _sz, _sz],
+    "ffcz_batch_create": [_PP, _i, _PP],
+    "ffcz_batch_destroy": [_p],
+    "ffcz_batch_set_stream": [_p, _p],
+    "ffcz_batch_reset_edit_accumulators": [_p],
+    "ffcz_batch_solve_pair_device": [_p, _PP, _PP, _i, _d],
     "ffcz_write_map": [C.c_char_p, _p, _p, _p, _sz],
     "ffcz_read_map": [C.c_char_p, _p, _p, _p, _sz, _SP],
     "ffcz_last_error": [],
@@ -373,6 +378,58 @@ class CompressionResult:
     def __repr__(self):
         return (f"CompressionResult(compressed={len(self.compressed_data)} B, bitstream="
                 f"{self.original_bitstream_size} B, elements={self.num_elements}, symbols={self.symbols.size})")
+
+
+class Batch:
+    """Many fields of uneven shapes corrected in one graph launch (no
+    counterpart in the reference, whose CLI corrects one field per run).
+
+    ``solvers`` are initialised ProjectionSolver handles, one per field; the
+    batch keeps them alive.  After :meth:`solve_pair_device` each field's
+    results are read through its own solver, and equal what
+    ``solver.solve_all_abs_pair_device`` gives, bit for bit: every field runs
+    its own device-side loop and retires when it converges."""
+
+    def __init__(self, solvers):
+        self.solvers = list(solvers)
+        arr = (C.c_void_p * len(self.solvers))(*[s._h.value for s in self.solvers])
+        h = C.c_void_p()
+        _check(lib().ffcz_batch_create(arr, len(self.solvers), C.byref(h)))
+        self._h = h
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) and self._h.value:
+            lib().ffcz_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def set_stream(self, stream) -> None:
+        ptr = 0 if stream is None else (stream if isinstance(stream, int) else stream.cuda_stream)
+        _check(lib().ffcz_batch_set_stream(self._h, C.c_void_p(ptr)))
+
+    def reset_edit_accumulators(self) -> None:
+        _check(lib().ffcz_batch_reset_edit_accumulators(self._h))
+
+    def solve_pair_device(self, d_xs, d_xprimes, max_iterations: int = 100, tol: float = 1e-7) -> list[int]:
+        """Returns each field's iteration count."""
+        n = len(self.solvers)
+        if len(d_xs) != n or len(d_xprimes) != n:
+            raise ValueError(f"expected {n} fields")
+        a = (C.c_void_p * n)(*[_dev_ptr(t) for t in d_xs])
+        b = (C.c_void_p * n)(*[_dev_ptr(t) for t in d_xprimes])
+        _check(lib().ffcz_batch_solve_pair_device(self._h, a, b, int(max_iterations), float(tol)))
+        return [s._iters() for s in self.solvers]
 
 
 def _view(p, which):

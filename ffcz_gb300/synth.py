@@ -112,6 +112,44 @@ def workload(name: str) -> tuple[Field, int]:
     return make_field(shape, alpha, seed, fe, fd, dtype, noise, spikes), max_iter
 
 
+# Batched form: groups of (count, shape, alpha, first seed); every field has
+# f_Delta = 1e-3 and a log-uniform spatial bound E_i = range_i * 10^(-5 + 2 u_i),
+# u_i = default_rng(seed_i + 2000).random(); x' = 2E round(x / 2E).
+BATCHES = {
+    "batch48": [(16, (1800, 3600), 2.0, 10), (16, (100, 500, 500), 11 / 3, 30), (16, (128, 128, 128), 5 / 3, 50)],
+    # the same three shape families at a size the oracle finishes in seconds
+    "batch6_small": [(2, (90, 180), 2.0, 10), (2, (10, 50, 50), 11 / 3, 30), (2, (32, 32, 32), 5 / 3, 50)],
+}
+
+
+def batch_field(shape, alpha: float, seed: int) -> Field:
+    u = float(np.random.default_rng(seed + 2000).random())
+    return make_field(shape, alpha, seed, 10.0 ** (-5.0 + 2.0 * u), 1e-3, np.float32)
+
+
+def batch_specs(name: str) -> list[tuple]:
+    return [(shape, alpha, seed0 + i) for count, shape, alpha, seed0 in BATCHES[name] for i in range(count)]
+
+
+def batch_workload(name: str, workers: int = 0) -> tuple[list[Field], int]:
+    """The fields of a named batch (max_iter 100).  With workers > 1 they are
+    generated in spawned processes (safe next to a CUDA context)."""
+    specs = batch_specs(name)
+    if workers > 1:
+        import multiprocessing as mp
+        from concurrent.futures import ProcessPoolExecutor
+
+        with ProcessPoolExecutor(workers, mp_context=mp.get_context("spawn")) as pool:
+            fields = list(pool.map(_batch_field_star, specs))
+    else:
+        fields = [batch_field(*sp) for sp in specs]
+    return fields, 100
+
+
+def _batch_field_star(spec):
+    return batch_field(*spec)
+
+
 def stress_delta(field: Field, c: float) -> float:
     """Delta = c * E * sqrt(N/6): a frequency bound near the noise level of
     the quantisation error, which makes the projections iterate."""

@@ -177,6 +177,38 @@ int ffcz_get_pass_times(ffcz_solver *s, double *ms, double *bytes, int cap,
                         int *npass);
 
 /* ======================================================================== *
+ * Batched form: many fields of uneven shapes in one graph launch           *
+ * ======================================================================== */
+/* No counterpart in the reference, whose CLI corrects one field per process
+ * (projection_example.cu:160-246).  A batch groups solver handles, each
+ * created for its own field shape and initialised (ffcz_init_all_abs*) with
+ * its own eps and delta.  ffcz_batch_solve_pair_device runs, for every
+ * field at once, what ffcz_solve_all_abs_pair_device runs for one: the
+ * projection loop of each field is a device-side while loop of its own
+ * inside one CUDA graph, so a field retires when it converges (or reaches
+ * max_iter) while the others keep iterating, and its compaction follows in
+ * the same graph.  Each field's results equal those of
+ * ffcz_solve_all_abs_pair_device on its own handle, bit for bit, and are
+ * read through that handle's getters and ffcz_solver_encode.
+ *   solvers : nfields distinct handles on the current device; the batch
+ *             keeps the pointers (destroy the batch before them).
+ *   d_orig[f], d_decomp[f] : device arrays of field f (16-byte aligned).
+ * The call runs on the batch's stream (ffcz_batch_set_stream; legacy
+ * default stream otherwise) and returns after it finished.  The graph is
+ * built on the first call and reused while the arguments stay the same. */
+typedef struct ffcz_batch ffcz_batch;
+int ffcz_batch_create(ffcz_solver *const *solvers, int nfields,
+                      ffcz_batch **out);
+int ffcz_batch_destroy(ffcz_batch *b);
+int ffcz_batch_set_stream(ffcz_batch *b, void *stream);
+/* ffcz_reset_edit_accumulators of every field, on the batch's stream, with
+ * one synchronisation. */
+int ffcz_batch_reset_edit_accumulators(ffcz_batch *b);
+int ffcz_batch_solve_pair_device(ffcz_batch *b, const void *const *d_orig,
+                                 const void *const *d_decomp, int max_iter,
+                                 double tol);
+
+/* ======================================================================== *
  * Huffman + ZSTD coder (replaces SimpleCudaHuffmanZstdCompressor<T>,       *
  * HuffmanZSTDCoder.cuh:236-451, cudaHuffmanZstdCompress/Decompress :454-470)*
  * ======================================================================== */
