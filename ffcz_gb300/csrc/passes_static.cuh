@@ -1,9 +1,9 @@
 // Compile-time-sized, register-resident pass kernels for power-of-two axis
-// lengths L = 16 .. 4096.
+// lengths L = 16 .. 4096 and a table of 2^a 3^b 5^c lengths.
 //
 // Each column (strided passes) or row (z passes) of length L is handled by
-// TC = L/E threads holding E elements each (E = the largest radix of the
-// stage list).  A stage of radix R runs E/R butterflies per thread in
+// TC = L/E threads holding E elements each (E = a multiple of every radix of
+// the stage list).  A stage of radix R runs E/R butterflies per thread in
 // registers; butterfly j = t + m*TC reads Stockham positions j + r*L/R and
 // writes (j/Ns)*Ns*R + j%Ns + r*Ns.  Stages exchange data through shared
 // memory, but the first stage reads its inputs straight from HBM into
@@ -25,22 +25,47 @@ namespace ffcz {
 
 constexpr int kInvBase = 12;
 
-// Twiddles of the strided passes' stages are stored R per k (entry 0
-// unused) so that a butterfly's R-1 twiddles are 16-byte aligned and read in
-// pairs: there a warp's lanes share few twiddle rows.  The z passes' lanes
-// each need a different row, and their tables keep R-1 per k.
-
 __host__ __device__ constexpr int ilog2(int n) { return n <= 1 ? 0 : 1 + ilog2(n >> 1); }
 
-// Stage lists.  Strided passes (CAP 16): 16:[16] 32:[8,4] 64:[8,8]
-// 128:[16,8] 256:[16,16] 512:[8,8,8] 1024:[16,8,8] 2048:[16,16,8]
+// Stage lists of the non-power-of-two lengths (the same for every pass),
+// packed as E | nst << 8 | r0 << 16 | r1 << 24 | r2 << 32 | r3 << 40
+// (forward order; every radix divides E; composite radices are prime-factor
+// butterflies).  0: no list.
+__host__ __device__ constexpr unsigned long long mx_pack(int E, int r0, int r1 = 0, int r2 = 0, int r3 = 0) {
+  return (unsigned long long)E | (unsigned long long)((r1 ? 1 : 0) + (r2 ? 1 : 0) + (r3 ? 1 : 0) + 1) << 8 |
+         (unsigned long long)r0 << 16 | (unsigned long long)r1 << 24 | (unsigned long long)r2 << 32 |
+         (unsigned long long)r3 << 40;
+}
+__host__ __device__ constexpr unsigned long long mx_list(int L) {
+  return L == 96 ? mx_pack(12, 12, 4, 2)
+       : L == 100 ? mx_pack(10, 10, 10)
+       : L == 192 ? mx_pack(12, 12, 4, 4)
+       : L == 200 ? mx_pack(20, 20, 10)
+       : L == 250 ? mx_pack(10, 10, 5, 5)
+       : L == 384 ? mx_pack(24, 24, 8, 2)
+       : L == 400 ? mx_pack(20, 20, 20)
+       : L == 500 ? mx_pack(10, 10, 10, 5)
+       : L == 768 ? mx_pack(24, 24, 8, 4)
+       : L == 900 ? mx_pack(30, 30, 30)
+       : L == 1000 ? mx_pack(10, 10, 10, 10)
+       : L == 1800 ? mx_pack(30, 30, 30, 2)
+       : 0;
+}
+__host__ __device__ constexpr int mx_E(int L) { return (int)(mx_list(L) & 0xff); }
+__host__ __device__ constexpr int mx_nst(int L) { return (int)((mx_list(L) >> 8) & 0xff); }
+__host__ __device__ constexpr int mx_r(int L, int s) { return (int)((mx_list(L) >> (16 + 8 * s)) & 0xff); }
+
+// Power-of-two stage lists.  Strided passes (CAP 16): 16:[16] 32:[8,4]
+// 64:[8,8] 128:[16,8] 256:[16,16] 512:[8,8,8] 1024:[16,8,8] 2048:[16,16,8]
 // 4096:[16,16,16].  z passes (CAP 8, 16+ threads per row): radix-8 stages
 // then one radix 4 or 2 stage for the remainder.
 __host__ __device__ constexpr int rp_nst(int L, int cap = 16) {
-  return cap == 8 ? (ilog2(L) / 3 + (ilog2(L) % 3 ? 1 : 0)) : (L == 16 ? 1 : (L <= 256 ? 2 : 3));
+  return mx_list(L) ? mx_nst(L)
+       : cap == 8 ? (ilog2(L) / 3 + (ilog2(L) % 3 ? 1 : 0)) : (L == 16 ? 1 : (L <= 256 ? 2 : 3));
 }
 __host__ __device__ constexpr int rp_radix(int L, int s, int cap = 16) {
-  return cap == 8 ? (s < ilog2(L) / 3 ? 8 : (ilog2(L) % 3 == 2 ? 4 : 2))
+  return mx_list(L) ? mx_r(L, s)
+       : cap == 8 ? (s < ilog2(L) / 3 ? 8 : (ilog2(L) % 3 == 2 ? 4 : 2))
        : L == 16 ? 16
        : L == 32 ? (s == 0 ? 8 : 4)
        : L == 64 ? 8
@@ -52,16 +77,35 @@ __host__ __device__ constexpr int rp_radix(int L, int s, int cap = 16) {
        : 16;
 }
 __host__ __device__ constexpr int rp_elems(int L, int cap = 16) {
-  return cap == 8 ? 8 : ((L == 32 || L == 64 || L == 512) ? 8 : 16);
+  return mx_list(L) ? mx_E(L) : cap == 8 ? 8 : ((L == 32 || L == 64 || L == 512) ? 8 : 16);
 }
 // radix of stage s in direction DIR (inverse = reversed list)
 __host__ __device__ constexpr int rp_rad(int L, int dir, int s, int cap = 16) {
   return dir < 0 ? rp_radix(L, s, cap) : rp_radix(L, rp_nst(L, cap) - 1 - s, cap);
 }
-// log2 of the span Ns before stage s in direction dir
-__host__ __device__ constexpr int rp_lgns(int L, int dir, int s, int cap = 16) {
-  return s == 0 ? 0 : rp_lgns(L, dir, s - 1, cap) + ilog2(rp_rad(L, dir, s - 1, cap));
+// span Ns before stage s in direction dir
+__host__ __device__ constexpr int rp_ns(int L, int dir, int s, int cap = 16) {
+  return s == 0 ? 1 : rp_ns(L, dir, s - 1, cap) * rp_rad(L, dir, s - 1, cap);
 }
+// Strided passes' even radices store R twiddles per k (entry 0 unused) so
+// that a butterfly's R-1 twiddles are 16-byte aligned and read in pairs:
+// there a warp's lanes share few twiddle rows.  Odd radices and the z
+// passes (whose lanes each need a different row) keep R-1 per k.
+__host__ __device__ constexpr bool tw_paired(int cap, int R) { return cap == 16 && R % 2 == 0; }
+
+// Prime-factor butterfly of length N1*N2 (coprime): input n = (N2 n1 + N1 n2)
+// mod N, N2 transforms of length N1, N1 of length N2, output at
+// k = (k1 e1 + k2 e2) mod N with e1 = 1 mod N1, 0 mod N2 and e2 = 0 mod N1,
+// 1 mod N2 -- no twiddles between the two layers (Good-Thomas).
+__host__ __device__ constexpr int crt_unit(int a, int b) {  // x = 0 mod b, x = 1 mod a
+  int x = 0;
+  while ((x * b) % a != 1) ++x;
+  return x * b;
+}
+template <int N1, int N2, int DIR, typename V>
+struct DftPfa {
+  __device__ __forceinline__ static void run(V *v);
+};
 
 // Radix 16 = 4 x 4 with the w16 twiddles between the two radix-4 layers.
 template <int DIR, typename V> struct Dft<16, DIR, V> {
@@ -105,18 +149,48 @@ template <int DIR, typename V> struct Dft<16, DIR, V> {
   }
 };
 
+template <int N1, int N2, int DIR, typename V>
+__device__ __forceinline__ void DftPfa<N1, N2, DIR, V>::run(V *v) {
+  constexpr int N = N1 * N2, E1 = crt_unit(N1, N2), E2 = crt_unit(N2, N1);
+  V a[N2][N1];
+#pragma unroll
+  for (int n2 = 0; n2 < N2; ++n2)
+#pragma unroll
+    for (int n1 = 0; n1 < N1; ++n1) a[n2][n1] = v[(N2 * n1 + N1 * n2) % N];
+#pragma unroll
+  for (int n2 = 0; n2 < N2; ++n2) Dft<N1, DIR, V>::run(a[n2]);
+  V b[N1][N2];
+#pragma unroll
+  for (int k1 = 0; k1 < N1; ++k1)
+#pragma unroll
+    for (int n2 = 0; n2 < N2; ++n2) b[k1][n2] = a[n2][k1];
+#pragma unroll
+  for (int k1 = 0; k1 < N1; ++k1) Dft<N2, DIR, V>::run(b[k1]);
+#pragma unroll
+  for (int k1 = 0; k1 < N1; ++k1)
+#pragma unroll
+    for (int k2 = 0; k2 < N2; ++k2) v[(k1 * E1 + k2 * E2) % N] = b[k1][k2];
+}
+template <int DIR, typename V> struct Dft<6, DIR, V> : DftPfa<2, 3, DIR, V> {};
+template <int DIR, typename V> struct Dft<10, DIR, V> : DftPfa<2, 5, DIR, V> {};
+template <int DIR, typename V> struct Dft<12, DIR, V> : DftPfa<4, 3, DIR, V> {};
+template <int DIR, typename V> struct Dft<15, DIR, V> : DftPfa<3, 5, DIR, V> {};
+template <int DIR, typename V> struct Dft<20, DIR, V> : DftPfa<4, 5, DIR, V> {};
+template <int DIR, typename V> struct Dft<24, DIR, V> : DftPfa<8, 3, DIR, V> {};
+template <int DIR, typename V> struct Dft<30, DIR, V> : DftPfa<2, 15, DIR, V> {};
+
 // Butterflies of one stage on the thread's registers: v[m*R + r] is input
 // r of butterfly m (j = t + m*TC) and becomes output r.
-template <typename T, int DIR, int R, int LGNS, int L, int E, bool VEC>
+template <typename T, int DIR, int R, int NS, int L, int E, bool VEC>
 __device__ __forceinline__ void rstage(c2<T> (&v)[E], int t, const c2<T> *__restrict__ tw) {
   using V = c2<T>;
-  constexpr int TC = L / E, NS = 1 << LGNS;
+  constexpr int TC = L / E;
 #pragma unroll
   for (int m = 0; m < E / R; ++m) {
     if (NS > 1) {
       const int j = t + m * TC;
       if constexpr (VEC) {
-        const V *w = tw + (j & (NS - 1)) * R;
+        const V *w = tw + (j % NS) * R;
         V ww[R];
         if (sizeof(T) == 4) {
 #pragma unroll
@@ -132,7 +206,7 @@ __device__ __forceinline__ void rstage(c2<T> (&v)[E], int t, const c2<T> *__rest
 #pragma unroll
         for (int r = 1; r < R; ++r) v[m * R + r] = (DIR < 0) ? cmul(v[m * R + r], ww[r]) : cmulc(v[m * R + r], ww[r]);
       } else {
-        const V *w = tw + (j & (NS - 1)) * (R - 1);
+        const V *w = tw + (j % NS) * (R - 1);
 #pragma unroll
         for (int r = 1; r < R; ++r) {
           const V ww = w[r - 1];
@@ -162,10 +236,10 @@ template <int L, int E, int R>
 __device__ __forceinline__ int in_pos(int t, int m, int r) {
   return t + m * (L / E) + r * (L / R);
 }
-template <int L, int E, int R, int LGNS>
+template <int L, int E, int R, int NS>
 __device__ __forceinline__ int out_pos(int t, int m, int r) {
   const int j = t + m * (L / E);
-  return ((j >> LGNS) << (LGNS + ilog2(R))) + (j & ((1 << LGNS) - 1)) + (r << LGNS);
+  return (j / NS) * NS * R + j % NS + r * NS;
 }
 
 // Runs stages S..end of direction DIR; v holds stage S's inputs.  Between
@@ -176,9 +250,9 @@ struct RRun {
   static constexpr int E = rp_elems(L, CAP);
   static __device__ __forceinline__ void run(c2<T> (&v)[E], c2<T> *buf, int t, int c, const AxisPlan &p) {
     if constexpr (S < rp_nst(L, CAP)) {
-      constexpr int R = rp_rad(L, DIR, S, CAP), LG = rp_lgns(L, DIR, S, CAP);
+      constexpr int R = rp_rad(L, DIR, S, CAP), LG = rp_ns(L, DIR, S, CAP);
       const c2<T> *tw = (const c2<T> *)p.tw + p.twoff[(DIR < 0 ? 0 : kInvBase) + S];
-      rstage<T, DIR, R, LG, L, E, CAP == 16>(v, t, tw);
+      rstage<T, DIR, R, LG, L, E, tw_paired(CAP, R)>(v, t, tw);
       if constexpr (S + 1 < rp_nst(L, CAP)) {
         constexpr int R2 = rp_rad(L, DIR, S + 1, CAP);
 #pragma unroll
@@ -201,7 +275,7 @@ struct RRun {
 template <int L, int DIR, int CAP = 16>
 __device__ __forceinline__ int last_pos(int t, int i) {
   constexpr int S = rp_nst(L, CAP) - 1, E = rp_elems(L, CAP), R = rp_rad(L, DIR, S, CAP),
-                LG = rp_lgns(L, DIR, S, CAP);
+                LG = rp_ns(L, DIR, S, CAP);
   return out_pos<L, E, R, LG>(t, i / R, i % R);
 }
 // Position of v[i] as input of the first stage of direction DIR.
@@ -211,16 +285,19 @@ __device__ __forceinline__ int first_pos(int t, int i) {
   return in_pos<L, E, R>(t, i / R, i % R);
 }
 
-// Resident blocks the 256-thread FP32 strided tiles are compiled for (three
-// per SM fit their 35 KB tiles and keep 24 warps resident); others: one.
-__host__ __device__ constexpr int strided_minb(int es, int nt) { return (es == 4 && nt == 256) ? 3 : 1; }
+// Resident blocks the 256-thread FP32 radix-16 strided tiles are compiled
+// for (three per SM fit their 35 KB tiles and keep 24 warps resident);
+// others: one.
+__host__ __device__ constexpr int strided_minb(int es, int nt, int E) {
+  return (es == 4 && nt == 256 && E == 16) ? 3 : 1;
+}
 
 // ---------------------------------------------------------------------------
 // Strided C2C pass.  Block = TC threads per column x TW columns (c fastest
 // across lanes, so each row access is TW contiguous complex values).
 template <typename T, int MODE, int L, int LGTW>
 __global__ void __launch_bounds__((L / rp_elems(L)) << LGTW,
-                                  strided_minb(sizeof(T), (L / rp_elems(L)) << LGTW)) ks_strided(c2<T> *__restrict__ spec, SArgs s,
+                                  strided_minb(sizeof(T), (L / rp_elems(L)) << LGTW, rp_elems(L))) ks_strided(c2<T> *__restrict__ spec, SArgs s,
                                                                         AxisPlan p, T delta,
                                                                         T *__restrict__ fedits, long long H) {
   using V = c2<T>;
@@ -268,16 +345,15 @@ __global__ void __launch_bounds__((L / rp_elems(L)) << LGTW,
 }
 
 // ---------------------------------------------------------------------------
-// R2C along z (Nz = 2M): TC = M/8 threads per row x TW rows (t fastest
-// across lanes: each load is a run of consecutive complex values of one row,
-// and a half warp holds a single row).
+// R2C along z (Nz = 2M): TC = M/E threads per row x TW rows (t fastest
+// across lanes: each load is a run of consecutive complex values of one row).
 template <typename T, int PRO, int M, int LGTW>
-__global__ void __launch_bounds__((M / 8) << LGTW) ks_zfwd(const T *__restrict__ a, const T *__restrict__ b,
+__global__ void __launch_bounds__((M / rp_elems(M, 8)) << LGTW) ks_zfwd(const T *__restrict__ a, const T *__restrict__ b,
                                                           T *__restrict__ sedits, T eps,
                                                           c2<T> *__restrict__ spec, ZArgs z, AxisPlan p,
                                                           const c2<T> *__restrict__ post) {
   using V = c2<T>;
-  constexpr int E = 8, TC = M / E;
+  constexpr int E = rp_elems(M, 8), TC = M / E;
   using LY = RowLayout<row_pitch(M)>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   V *buf = reinterpret_cast<V *>(smem_raw);
@@ -339,11 +415,11 @@ __global__ void __launch_bounds__((M / 8) << LGTW) ks_zfwd(const T *__restrict__
 // forms Z[k] = (X[k] + conj X[M-k]) + i W^-k (X[k] - conj X[M-k]) in
 // registers (imaginary parts of X[0] and X[M] ignored).
 template <typename T, int M, int LGTW>
-__global__ void __launch_bounds__((M / 8) << LGTW) ks_zinv(const c2<T> *__restrict__ spec, T *__restrict__ e,
+__global__ void __launch_bounds__((M / rp_elems(M, 8)) << LGTW) ks_zinv(const c2<T> *__restrict__ spec, T *__restrict__ e,
                                                           T eps, T factor, LoopCtl *ctl, ZArgs z, AxisPlan p,
                                                           const c2<T> *__restrict__ post) {
   using V = c2<T>;
-  constexpr int E = 8, TC = M / E;
+  constexpr int E = rp_elems(M, 8), TC = M / E;
   using LY = RowLayout<row_pitch(M)>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   V *buf = reinterpret_cast<V *>(smem_raw);

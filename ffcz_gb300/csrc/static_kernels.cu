@@ -1,5 +1,6 @@
 // Instantiations of the register-resident pass kernels (FP32 lengths
-// 16..4096, FP64 16..2048), their lookup, and their twiddle tables.
+// 16..4096, FP64 16..2048, and the 2^a 3^b 5^c lengths with a stage list),
+// their lookup, and their twiddle tables.
 #include <cmath>
 
 #include "passes_static.cuh"
@@ -8,6 +9,7 @@
 namespace ffcz {
 
 bool static_length(int L, bool fp64) {
+  if (mx_list(L)) return mx_E(L) <= (fp64 ? 12 : 30);
   return L >= 16 && (L & (L - 1)) == 0 && L <= (fp64 ? 2048 : 4096);
 }
 
@@ -19,8 +21,8 @@ void build_static_plan(int L, int cap, AxisPlan &p, std::vector<std::complex<dou
     long long Ns = 1;
     for (int s = 0; s < rp_nst(L, cap); ++s) {
       const int R = rp_rad(L, dir, s, cap);
-      // strided lists (cap 16): R entries per k from a 16-byte aligned start
-      const bool vec = cap == 16;
+      // paired stages: R entries per k from a 16-byte aligned start
+      const bool vec = tw_paired(cap, R);
       while (vec && table.size() % 2) table.push_back({1.0, 0.0});
       p.twoff[(dir < 0 ? 0 : kInvBase) + s] = (int)table.size();
       if (Ns > 1)
@@ -43,13 +45,16 @@ namespace {
 
 template <typename T, int L, int CAP = 16>
 struct Cfg {
-  static constexpr int TC = L / rp_elems(L, CAP);
+  static constexpr int E = rp_elems(L, CAP);
+  static constexpr int TC = L / E;
   static constexpr int TWMAX = sizeof(T) == 4 ? 16 : 8;
-  // radix-16 lists hold 16 values per thread (~80-100 registers): at most
-  // 512 threads; radix-8 lists (~64 registers) may use FFCZ_TILE_THREADS
-  static constexpr int TW0 = (rp_elems(L, CAP) == 16 ? 512 : FFCZ_TILE_THREADS) / TC;
-  static constexpr int TW = TW0 < 1 ? 1 : (TW0 > TWMAX ? TWMAX : TW0);
-  static constexpr int LGTW = ilog2(TW);
+  // 16 values per thread take ~80-100 registers: at most 512 threads; 20-30
+  // values (~130-170 registers): 256; 8-12 values may use FFCZ_TILE_THREADS
+  static constexpr int BUDGET = E > 16 ? 256 : E == 16 ? 512 : FFCZ_TILE_THREADS;
+  static constexpr int TW0 = BUDGET / TC;
+  static constexpr int TW1 = TW0 < 1 ? 1 : (TW0 > TWMAX ? TWMAX : TW0);
+  static constexpr int LGTW = ilog2(TW1);  // tile widths are powers of two
+  static constexpr int TW = 1 << LGTW;
   static constexpr int NT = TC * TW;
 };
 
@@ -96,8 +101,10 @@ bool strided_for(int mode, StridedFn<T> &fn, StaticGeom &g) {
 
 }  // namespace
 
-#define CASES_F32(X) X(16) X(32) X(64) X(128) X(256) X(512) X(1024) X(2048) X(4096)
-#define CASES_F64(X) X(16) X(32) X(64) X(128) X(256) X(512) X(1024) X(2048)
+#define CASES_F32(X)                                                                                      \
+  X(16) X(32) X(64) X(128) X(256) X(512) X(1024) X(2048) X(4096) X(96) X(100) X(192) X(200) X(250) X(384)  \
+  X(400) X(500) X(768) X(900) X(1000) X(1800)
+#define CASES_F64(X) X(16) X(32) X(64) X(128) X(256) X(512) X(1024) X(2048) X(96) X(100) X(192) X(250) X(500) X(1000)
 
 #define DEFINE_LOOKUPS(T, CASES)                                                  \
   template <>                                                                     \

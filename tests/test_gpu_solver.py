@@ -19,7 +19,11 @@ TOL_E = 2e-5
 TOL_EDIT = 2e-5
 
 SHAPES = [(16, 24, 10), (8, 8, 8), (1, 1, 17), (1, 1, 64), (1, 30, 50), (5, 7, 9), (12, 10, 14), (3, 1, 40),
-          (2, 3, 1), (20, 35, 49), (64, 64, 64), (4, 6, 250), (11, 13, 34), (1, 1, 1), (1, 2, 2)]
+          (2, 3, 1), (20, 35, 49), (64, 64, 64), (4, 6, 250), (11, 13, 34), (1, 1, 1), (1, 2, 2),
+          (2, 96, 192), (500, 2, 6), (1, 900, 1800), (100, 3, 200)]
+# axes with a compile-time mixed-radix stage list (100, 250, 500, 900, 1800, 96, 384, ...)
+MIXED = [(4, 100, 200), (3, 250, 500), (2, 96, 192), (2, 384, 768), (2, 400, 1000), (1, 900, 1800),
+         (100, 3, 10), (500, 2, 6), (1800, 2, 4), (3, 1000, 2000), (2, 200, 400), (2, 192, 384)]
 
 
 def rand_e0(shape, seed, scale=1.0, dtype=np.float32):
@@ -59,7 +63,9 @@ def test_frequency_clamp_one_pass(cuda, shape):
 
 
 @pytest.mark.parametrize("shape,c", [((64, 64, 64), 1.0), ((64, 64, 64), 3.0), ((32, 48, 20), 2.0),
-                                     ((1, 90, 100), 1.5), ((1, 1, 4096), 1.0), ((25, 20, 16), 2.0)])
+                                     ((1, 90, 100), 1.5), ((1, 1, 4096), 1.0), ((25, 20, 16), 2.0),
+                                     ((4, 100, 200), 2.0), ((3, 250, 500), 1.5), ((2, 384, 768), 1.0),
+                                     ((100, 6, 10), 2.0), ((1, 1800, 3600), 1.0)])
 def test_loop_parity(cuda, shape, c):
     """Stress bounds (several iterations): iterations, e and both edit
     accumulators agree with the FP32-rounded oracle."""
@@ -77,10 +83,12 @@ def test_loop_parity(cuda, shape, c):
         fscale = float(np.abs(np.fft.rfftn(e0.reshape(fld.shape).astype(np.float64))).max())
         assert np.abs(s.get_freq_edits_full() - ref["freq_edits"]).max() <= TOL_EDIT * fscale * max(1, it)
         assert np.abs(s.get_spatial_edits_full() - ref["spatial_edits"]).max() <= TOL_E * escale * max(1, it)
-        # FP64 check of the bounds the reference schedule guarantees
+        # FP64 check of the bounds the reference schedule guarantees: |e| <= E
+        # + tol; x^ = x + e stored in float32 adds up to half an ulp of |x^|
         b = O.check_bounds(fld.x, fld.x + e.reshape(fld.shape), fld.eps, delta)
+        half_ulp = 0.5 * float(np.spacing(np.float32(np.abs(fld.x).max() + fld.eps)))
         if ref["converged"]:
-            assert b["spatial_excess"] <= 1e-7 + 1e-6 * fld.eps
+            assert b["spatial_excess"] <= 1e-7 + half_ulp + 1e-6 * fld.eps
 
 
 @pytest.mark.parametrize("dtype", [np.float32, np.float64])
@@ -231,15 +239,19 @@ def test_launch_count_reported(cuda):
         assert s.launch_count() == 2 + 6 * it
 
 
-@pytest.mark.parametrize("shape", [(64, 64, 64), (32, 48, 20), (16, 1024, 32), (8, 16, 2048), (40, 512, 256)])
+@pytest.mark.parametrize("shape", [(64, 64, 64), (32, 48, 20), (16, 1024, 32), (8, 16, 2048), (40, 512, 256)]
+                         + MIXED)
 @pytest.mark.parametrize("dtype", [np.float32, np.float64])
 def test_static_kernels_match_generic(cuda, shape, dtype, monkeypatch):
-    """Compile-time-sized pass kernels (power-of-two axes) against the
-    runtime-planned engine on the same input."""
+    """Compile-time-sized pass kernels (power-of-two and mixed-radix axes)
+    against the runtime-planned engine on the same input."""
     fld = synth.make_field(shape, 11 / 3, 13, 1e-3, 1e-3, dtype, noise=0.3)
     delta = synth.stress_delta(fld, 1.5)
     e0 = (fld.xp.astype(np.float64) - fld.x.astype(np.float64)).astype(dtype)
     out = []
+    if dtype == np.float64 and max(shape) > 1024 and max(shape) & (max(shape) - 1):
+        # FP64 axes above 1024 exist only as compile-time lengths (2048)
+        pytest.skip("FP64 axis length above the runtime-planned engine's 1024")
     for generic in ("0", "1"):
         monkeypatch.setenv("FFCZ_GENERIC_KERNELS", generic)
         with F.ProjectionSolver(*shape, dtype=dtype) as s:
