@@ -126,8 +126,12 @@ class Clocks:
 
 
 def load_workload(name):
+    """A named single field, or "batch:i" for field i of a named batch."""
     from ffcz_gb300 import synth
 
+    if ":" in name:
+        batch, i = name.split(":")
+        return synth.batch_field(*synth.batch_specs(batch)[int(i)]), 100
     fld, max_iter = synth.workload(name)
     return fld, max_iter
 

@@ -285,9 +285,10 @@ __device__ __forceinline__ int first_pos(int t, int i) {
   return in_pos<L, E, R>(t, i / R, i % R);
 }
 
-// Resident blocks the 256-thread FP32 radix-16 strided tiles are compiled
-// for (three per SM fit their 35 KB tiles and keep 24 warps resident);
-// others: one.
+// Resident blocks the FP32 strided tiles are compiled for: three for the
+// 256-thread radix-16 tiles (35 KB tiles, 24 warps resident); others: one
+// (two blocks of the 30-value lists would cap them at 128 registers, and
+// their spills cost more than the occupancy gains: 63 vs 48 us at 1800).
 __host__ __device__ constexpr int strided_minb(int es, int nt, int E) {
   return (es == 4 && nt == 256 && E == 16) ? 3 : 1;
 }

@@ -1,0 +1,104 @@
+// Instantiation helpers of the register-resident pass kernels: tile
+// geometry per length (Cfg), the typed lookups and the length lists.  Each
+// element type is instantiated in its own translation unit.
+#pragma once
+
+#include "passes_static.cuh"
+#include "static_kernels.h"
+
+namespace ffcz {
+
+#ifndef FFCZ_TILE_THREADS
+#define FFCZ_TILE_THREADS 512
+#endif
+
+template <typename T, int L, int CAP = 16>
+struct Cfg {
+  static constexpr int E = rp_elems(L, CAP);
+  static constexpr int TC = L / E;
+  static constexpr int TWMAX = sizeof(T) == 4 ? 16 : 8;
+  // 16 values per thread take ~80-100 registers: at most 512 threads; 20-30
+  // values (~130-170 registers): 256; 8-12 values may use FFCZ_TILE_THREADS
+  static constexpr int BUDGET = E > 16 ? 256 : E == 16 ? 512 : FFCZ_TILE_THREADS;
+  static constexpr int TW0 = BUDGET / TC;
+  static constexpr int TW1 = TW0 < 1 ? 1 : (TW0 > TWMAX ? TWMAX : TW0);
+  static constexpr int LGTW = ilog2(TW1);  // tile widths are powers of two
+  static constexpr int TW = 1 << LGTW;
+  static constexpr int NT = TC * TW;
+};
+
+template <typename F>
+int set_smem(F fn, size_t smem) {
+  if (smem > 48 * 1024)
+    FFCZ_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  return FFCZ_OK;
+}
+
+template <typename T, int M>
+bool zfwd_for(int pro, ZfwdFn<T> &fn, StaticGeom &g) {
+  using C = Cfg<T, M, 8>;
+  if (pro == PRO_PLAIN) fn = ks_zfwd<T, PRO_PLAIN, M, C::LGTW>;
+  else if (pro == PRO_DIFF) fn = ks_zfwd<T, PRO_DIFF, M, C::LGTW>;
+  else fn = ks_zfwd<T, PRO_CLAMP, M, C::LGTW>;
+  g.TW = C::TW;
+  g.threads = C::NT;
+  g.smem = (size_t)C::TW * row_pitch(M) * sizeof(c2<T>);
+  return set_smem(fn, g.smem) == FFCZ_OK;
+}
+
+template <typename T, int M>
+bool zinv_for(ZinvFn<T> &fn, StaticGeom &g) {
+  using C = Cfg<T, M, 8>;
+  fn = ks_zinv<T, M, C::LGTW>;
+  g.TW = C::TW;
+  g.threads = C::NT;
+  g.smem = (size_t)C::TW * row_pitch(M) * sizeof(c2<T>);
+  return set_smem(fn, g.smem) == FFCZ_OK;
+}
+
+template <typename T, int L>
+bool strided_for(int mode, StridedFn<T> &fn, StaticGeom &g) {
+  using C = Cfg<T, L>;
+  if (mode == MODE_FWD) fn = ks_strided<T, MODE_FWD, L, C::LGTW>;
+  else if (mode == MODE_INV) fn = ks_strided<T, MODE_INV, L, C::LGTW>;
+  else fn = ks_strided<T, MODE_FCI, L, C::LGTW>;
+  g.TW = C::TW;
+  g.threads = C::NT;
+  g.smem = (size_t)L * (C::TW + 1) * sizeof(c2<T>);
+  return set_smem(fn, g.smem) == FFCZ_OK;
+}
+
+#define CASES_F32(X)                                                                                      \
+  X(16) X(32) X(64) X(128) X(256) X(512) X(1024) X(2048) X(4096) X(96) X(100) X(192) X(200) X(250) X(384)  \
+  X(400) X(500) X(768) X(900) X(1000) X(1800)
+#define CASES_F64(X) X(16) X(32) X(64) X(128) X(256) X(512) X(1024) X(2048) X(96) X(100) X(192) X(250) X(500) X(1000)
+
+#define DEFINE_LOOKUPS(T, CASES)                                                  \
+  template <>                                                                     \
+  bool static_zfwd<T>(int M, int pro, ZfwdFn<T> &fn, StaticGeom &g) {             \
+    switch (M) {                                                                  \
+      CASES(ZF)                                                                   \
+      default: return false;                                                      \
+    }                                                                             \
+  }                                                                               \
+  template <>                                                                     \
+  bool static_zinv<T>(int M, ZinvFn<T> &fn, StaticGeom &g) {                      \
+    switch (M) {                                                                  \
+      CASES(ZI)                                                                   \
+      default: return false;                                                      \
+    }                                                                             \
+  }                                                                               \
+  template <>                                                                     \
+  bool static_strided<T>(int L, int mode, StridedFn<T> &fn, StaticGeom &g) {      \
+    switch (L) {                                                                  \
+      CASES(ST)                                                                   \
+      default: return false;                                                      \
+    }                                                                             \
+  }
+
+#define ZF(n) case n: return zfwd_for<TT, n>(pro, fn, g);
+#define ZI(n) case n: return zinv_for<TT, n>(fn, g);
+#define ST(n) case n: return strided_for<TT, n>(mode, fn, g);
+
+
+}  // namespace ffcz
