@@ -218,19 +218,50 @@ __device__ __forceinline__ void rstage(c2<T> (&v)[E], int t, const c2<T> *__rest
   }
 }
 
-// Shared-memory layouts of a tile of positions x columns.  Strided passes
-// (lanes along columns): element (pos, c) at pos*P + c, P = TW + 1.  z passes
-// (lanes along positions): row-major with one pad slot every 16 positions,
-// so that the stride-R output positions of a stage fall in distinct banks.
-template <int P>
+// Shared-memory layouts of a tile of positions x columns, chosen per length
+// from a bank model of every stage exchange (64-bit accesses served in
+// 128-byte wavefronts) and kept where they measured faster: the mixed-radix
+// z passes' pads cut their modelled wavefronts from 2.4-4.6x to 1.3-1.4x of
+// the minimum (z forward at 250: 100 -> 91 us, z inverse 84 -> 66 us).
+//
+// Strided passes (lanes along columns): element (pos, c) at
+// pos*P + c + pos/B.  z passes (lanes along positions): row-major with pitch
+// RP and one pad slot every B positions.  FP64 tiles keep P = TW + 1 and
+// B = 16 for z.
+__host__ __device__ constexpr int sl_p(int L, int TW, int es) {
+  return es != 4 ? TW + 1
+       : mx_list(L) ? (((L == 500 || L == 900) && TW == 8) ? 12 : ((L == 1800 || L == 1000) && TW == 4) ? 6 : TW + 1)
+       : TW + 1;
+}
+// (P = TW, B = 16/TW models better for the power-of-two tiles of 8 and fewer
+// columns but measured slower: 348 vs 284 us for the y pass at 512^3.)
+__host__ __device__ constexpr int sl_b(int L, int TW, int es) { return 0; }
+// elements of a strided tile
+__host__ __device__ constexpr int sl_size(int L, int TW, int es) {
+  return (L - 1) * sl_p(L, TW, es) + TW + (sl_b(L, TW, es) ? (L - 1) / sl_b(L, TW, es) : 0);
+}
+__host__ __device__ constexpr int zl_b(int M, int es) {
+  return (es == 4 && mx_list(M))
+             ? (M == 250 ? 0 : M == 500 ? 100 : M == 1800 ? 60 : M == 900 ? 90 : M == 100 ? 10 : M == 1000 ? 100
+                : M == 96 ? 8 : M == 192 ? 8 : M == 384 ? 16 : M == 768 ? 16 : M == 200 ? 40 : M == 400 ? 20 : 16)
+             : 16;
+}
+__host__ __device__ constexpr int row_pitch(int M, int es) {
+  return (es == 4 && mx_list(M))
+             ? (M == 250 ? 265 : M == 500 ? 514 : M == 1800 ? 1836 : M == 900 ? 926 : M == 100 ? 122
+                : M == 1000 ? 1012 : M == 96 ? 116 : M == 192 ? 232 : M == 384 ? 424 : M == 768 ? 817
+                : M == 200 ? 218 : M == 400 ? 436 : M + M / 16 + 1)
+             : M + M / 16 + 1;
+}
+template <int P, int B>
 struct ColLayout {
-  static __device__ __forceinline__ int idx(int pos, int c) { return pos * P + c; }
+  static __device__ __forceinline__ int idx(int pos, int c) { return pos * P + c + (B ? pos / B : 0); }
 };
-template <int RP>
+template <int RP, int B>
 struct RowLayout {
-  static __device__ __forceinline__ int idx(int pos, int c) { return c * RP + pos + (pos >> 4); }
+  static_assert(B == 0 || RP > 0, "pitch");
+  static __device__ __forceinline__ int idx(int pos, int c) { return c * RP + pos + (B ? pos / B : 0); }
 };
-__host__ __device__ constexpr int row_pitch(int M) { return M + (M >> 4) + 1; }
 
 template <int L, int E, int R>
 __device__ __forceinline__ int in_pos(int t, int m, int r) {
@@ -302,7 +333,8 @@ __global__ void __launch_bounds__((L / rp_elems(L)) << LGTW,
                                                                         AxisPlan p, T delta,
                                                                         T *__restrict__ fedits, long long H) {
   using V = c2<T>;
-  constexpr int E = rp_elems(L), TW = 1 << LGTW, P = TW + 1;
+  constexpr int E = rp_elems(L), TW = 1 << LGTW;
+  using LY = ColLayout<sl_p(L, TW, sizeof(T)), sl_b(L, TW, sizeof(T))>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   V *buf = reinterpret_cast<V *>(smem_raw);
   const int c = threadIdx.x & (TW - 1);
@@ -321,7 +353,7 @@ __global__ void __launch_bounds__((L / rp_elems(L)) << LGTW,
 #pragma unroll
   for (int i = 0; i < E; ++i)
     v[i] = live ? src[(long long)first_pos<L, D0>(t, i) * s.Wtot] : mkc<T>(T(0), T(0));
-  RRun<T, D0, L, ColLayout<P>, 0>::run(v, buf, t, c, p);
+  RRun<T, D0, L, LY, 0>::run(v, buf, t, c, p);
   if (MODE == MODE_FCI) {
     if (live) {
 #pragma unroll
@@ -335,7 +367,7 @@ __global__ void __launch_bounds__((L / rp_elems(L)) << LGTW,
     // stage wrote, so the same registers continue.  A barrier separates the
     // forward's last shared reads from the inverse's first shared writes.
     __syncthreads();
-    RRun<T, +1, L, ColLayout<P>, 0>::run(v, buf, t, c, p);
+    RRun<T, +1, L, LY, 0>::run(v, buf, t, c, p);
   }
   constexpr int DL = (MODE == MODE_FWD) ? -1 : +1;
   V *dst = spec + bb * (long long)L * s.Wtot + (long long)q * s.Hzp + kz0 + c;
@@ -355,7 +387,7 @@ __global__ void __launch_bounds__((M / rp_elems(M, 8)) << LGTW) ks_zfwd(const T 
                                                           const c2<T> *__restrict__ post) {
   using V = c2<T>;
   constexpr int E = rp_elems(M, 8), TC = M / E;
-  using LY = RowLayout<row_pitch(M)>;
+  using LY = RowLayout<row_pitch(M, sizeof(T)), zl_b(M, sizeof(T))>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   V *buf = reinterpret_cast<V *>(smem_raw);
   const int t = threadIdx.x % TC;
@@ -421,7 +453,7 @@ __global__ void __launch_bounds__((M / rp_elems(M, 8)) << LGTW) ks_zinv(const c2
                                                           const c2<T> *__restrict__ post) {
   using V = c2<T>;
   constexpr int E = rp_elems(M, 8), TC = M / E;
-  using LY = RowLayout<row_pitch(M)>;
+  using LY = RowLayout<row_pitch(M, sizeof(T)), zl_b(M, sizeof(T))>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   V *buf = reinterpret_cast<V *>(smem_raw);
   const int t = threadIdx.x % TC;

@@ -42,7 +42,7 @@ bool zfwd_for(int pro, ZfwdFn<T> &fn, StaticGeom &g) {
   else fn = ks_zfwd<T, PRO_CLAMP, M, C::LGTW>;
   g.TW = C::TW;
   g.threads = C::NT;
-  g.smem = (size_t)C::TW * row_pitch(M) * sizeof(c2<T>);
+  g.smem = (size_t)C::TW * row_pitch(M, sizeof(T)) * sizeof(c2<T>);
   return set_smem(fn, g.smem) == FFCZ_OK;
 }
 
@@ -52,7 +52,7 @@ bool zinv_for(ZinvFn<T> &fn, StaticGeom &g) {
   fn = ks_zinv<T, M, C::LGTW>;
   g.TW = C::TW;
   g.threads = C::NT;
-  g.smem = (size_t)C::TW * row_pitch(M) * sizeof(c2<T>);
+  g.smem = (size_t)C::TW * row_pitch(M, sizeof(T)) * sizeof(c2<T>);
   return set_smem(fn, g.smem) == FFCZ_OK;
 }
 
@@ -64,7 +64,7 @@ bool strided_for(int mode, StridedFn<T> &fn, StaticGeom &g) {
   else fn = ks_strided<T, MODE_FCI, L, C::LGTW>;
   g.TW = C::TW;
   g.threads = C::NT;
-  g.smem = (size_t)L * (C::TW + 1) * sizeof(c2<T>);
+  g.smem = (size_t)sl_size(L, C::TW, sizeof(T)) * sizeof(c2<T>);
   return set_smem(fn, g.smem) == FFCZ_OK;
 }
 
