@@ -122,6 +122,11 @@ SIGNATURES = {
     "ffcz_batch_set_stream": [_p, _p],
     "ffcz_batch_reset_edit_accumulators": [_p],
     "ffcz_batch_solve_pair_device": [_p, _PP, _PP, _i, _d],
+    "ffcz_huff_decode_device": [_p, _sz, _p, _p, _p, _sz, _sz, _i, _p, _SP, _p],
+    "ffcz_huff_zstd_decompress_device": [_p, _sz, _p, _p, _p, _sz, _sz, _sz, _i, _p, _SP, _p],
+    "ffcz_huff_result_create": [_p, _sz, _p, _sz, _p, _p, _p, _sz, _sz, _PP],
+    "ffcz_reconstruct_device": [_p, _p, _p, _sz, _p, _d, _d, _p, _sz, _p, _d, _d, _p],
+    "ffcz_solver_decode": [_p, _p, _PP, _d, _d, _d, _d, _p],
     "ffcz_write_map": [C.c_char_p, _p, _p, _p, _sz],
     "ffcz_read_map": [C.c_char_p, _p, _p, _p, _sz, _SP],
     "ffcz_last_error": [],
@@ -341,6 +346,28 @@ class ProjectionSolver:
         _check(lib().ffcz_get_launch_count(self._h, C.byref(v)))
         return v.value
 
+    def reconstruct_device(self, d_xprime, d_out, freq=None, spatial=None) -> None:
+        """x^ = x' + (C2R(F)/N + S) from decoded streams on the device.
+        freq / spatial: (d_quant, count, d_pack, min, max) or None."""
+        fq, nf, fp, fmn, fmx = freq if freq else (0, 0, 0, 0.0, 0.0)
+        sq, ns, sp, smn, smx = spatial if spatial else (0, 0, 0, 0.0, 0.0)
+        _check(lib().ffcz_reconstruct_device(self._h, _dev_ptr(d_xprime), _dev_ptr(fq) or None, nf,
+                                             _dev_ptr(fp) or None, fmn, fmx, _dev_ptr(sq) or None, ns,
+                                             _dev_ptr(sp) or None, smn, smx, _dev_ptr(d_out)))
+
+    def decode_device(self, d_xprime, streams, minmax, d_out) -> None:
+        """The decoder: the four CompressionResults of :meth:`encode` (None
+        where empty) and :meth:`minmax`'s values -> x^ in d_out (device)."""
+        handles = [None if r is None else r.native() for r in streams]
+        arr = (C.c_void_p * 4)(*[h.value if h is not None else None for h in handles])
+        try:
+            _check(lib().ffcz_solver_decode(self._h, _dev_ptr(d_xprime), arr, *[float(v) for v in minmax],
+                                            _dev_ptr(d_out)))
+        finally:
+            for h in handles:
+                if h is not None:
+                    lib().ffcz_huff_result_free(h)
+
     def encode(self, zstd_level: int = 20, zstd_mode: int = FFCZ_ZSTD_SINGLE) -> list:
         """The four streams of projection_example.cu:230-246 (None where skipped).
         FFCZ_ZSTD_NONE returns the Huffman bitstreams with empty compressed_data."""
@@ -374,6 +401,23 @@ class CompressionResult:
 
     def arrays(self):
         return self.symbols, self.codes, self.lengths
+
+    def native(self) -> C.c_void_p:
+        """A C-ABI result handle of this result (caller frees it with
+        ffcz_huff_result_free); the bitstream is recovered from the ZSTD
+        frame when this result does not hold it."""
+        syms, codes, lens = (np.ascontiguousarray(a, dt) for a, dt in
+                             zip((self.symbols, self.codes, self.lengths), (np.uint32, np.uint32, np.int32)))
+        comp = np.frombuffer(self.compressed_data, np.uint8) if len(self.compressed_data) else None
+        bits = np.frombuffer(self.bitstream, np.uint8) if len(self.bitstream) else None
+        h = C.c_void_p()
+        _check(lib().ffcz_huff_result_create(None if comp is None else _np_ptr(comp), len(self.compressed_data),
+                                             None if bits is None else _np_ptr(bits), self.original_bitstream_size,
+                                             _np_ptr(syms) if syms.size else None,
+                                             _np_ptr(codes) if codes.size else None,
+                                             _np_ptr(lens) if lens.size else None, syms.size, self.num_elements,
+                                             C.byref(h)))
+        return h
 
     def __repr__(self):
         return (f"CompressionResult(compressed={len(self.compressed_data)} B, bitstream="
@@ -486,6 +530,44 @@ def zstd_compress(data: bytes, level: int, mode: int = FFCZ_ZSTD_SINGLE) -> byte
     n = C.c_size_t()
     _check(lib().ffcz_zstd_compress(_np_ptr(src), len(data), int(level), int(mode), _np_ptr(dst), cap, C.byref(n)))
     return bytes(dst[: n.value])
+
+
+def _table_arrays(code_table):
+    if isinstance(code_table, dict):
+        syms = np.array(sorted(code_table), dtype=np.uint32)
+        codes = np.array([code_table[s][0] for s in syms], dtype=np.uint32)
+        lens = np.array([code_table[s][1] for s in syms], dtype=np.int32)
+        return syms, codes, lens
+    return tuple(np.ascontiguousarray(a, dt) for a, dt in zip(code_table, (np.uint32, np.uint32, np.int32)))
+
+
+def huff_decode_device(d_bits, nbytes: int, code_table, num_elements: int, dtype, d_out, stream=None) -> int:
+    """GPU prefix decode of a device-resident Huffman bitstream (the host
+    decoder's rules); returns the number of symbols written to d_out."""
+    syms, codes, lens = _table_arrays(code_table)
+    n = C.c_size_t()
+    ptr = 0 if stream is None else (stream if isinstance(stream, int) else stream.cuda_stream)
+    _check(lib().ffcz_huff_decode_device(_dev_ptr(d_bits), nbytes, _np_ptr(syms) if syms.size else None,
+                                         _np_ptr(codes) if codes.size else None,
+                                         _np_ptr(lens) if lens.size else None, syms.size, num_elements,
+                                         np.dtype(dtype).itemsize, _dev_ptr(d_out), C.byref(n), C.c_void_p(ptr)))
+    return n.value
+
+
+def huff_zstd_decompress_device(compressed: bytes, code_table, num_elements: int, original_bitstream_size: int,
+                                dtype, d_out, stream=None) -> int:
+    """ZSTD on the host, then the GPU decode into d_out; returns the count."""
+    syms, codes, lens = _table_arrays(code_table)
+    comp = np.frombuffer(compressed, np.uint8) if len(compressed) else np.zeros(1, np.uint8)
+    n = C.c_size_t()
+    ptr = 0 if stream is None else (stream if isinstance(stream, int) else stream.cuda_stream)
+    _check(lib().ffcz_huff_zstd_decompress_device(_np_ptr(comp), len(compressed),
+                                                  _np_ptr(syms) if syms.size else None,
+                                                  _np_ptr(codes) if codes.size else None,
+                                                  _np_ptr(lens) if lens.size else None, syms.size, num_elements,
+                                                  original_bitstream_size, np.dtype(dtype).itemsize,
+                                                  _dev_ptr(d_out), C.byref(n), C.c_void_p(ptr)))
+    return n.value
 
 
 def cuda_huffman_zstd_decompress(compressed: bytes, code_table, num_elements: int,

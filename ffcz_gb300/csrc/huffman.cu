@@ -424,6 +424,30 @@ int ffcz_zstd_compress(const uint8_t *src, size_t n, int level, int mode, uint8_
   return FFCZ_OK;
 }
 
+int ffcz_huff_result_create(const uint8_t *compressed, size_t comp_len, const uint8_t *bitstream,
+                            size_t bitstream_bytes, const uint32_t *symbols, const uint32_t *codes,
+                            const int32_t *lengths, size_t num_symbols, size_t num_elements,
+                            ffcz_huff_result **out) {
+  if (!out) return fail(FFCZ_ERR_INVALID, "out is NULL");
+  *out = nullptr;
+  if ((!compressed && comp_len) || (num_symbols && (!symbols || !codes || !lengths)))
+    return fail(FFCZ_ERR_INVALID, "NULL argument");
+  std::unique_ptr<ffcz_huff_result> r(new ffcz_huff_result());
+  r->compressed.assign(compressed, compressed + comp_len);
+  if (bitstream) {
+    r->bitstream.assign(bitstream, bitstream + bitstream_bytes);
+  } else {
+    FFCZ_TRY(zstd_decompress(compressed, comp_len, bitstream_bytes, r->bitstream));
+    r->bitstream.resize(bitstream_bytes, 0);
+  }
+  r->symbols.assign(symbols, symbols + num_symbols);
+  r->codes.assign(codes, codes + num_symbols);
+  r->lengths.assign(lengths, lengths + num_symbols);
+  r->num_elements = num_elements;
+  *out = r.release();
+  return FFCZ_OK;
+}
+
 int ffcz_huff_result_sizes(const ffcz_huff_result *r, size_t *compressed_bytes, size_t *bitstream_bytes,
                            size_t *num_elements, size_t *num_symbols) {
   if (!r) return fail(FFCZ_ERR_INVALID, "result is NULL");

@@ -14,6 +14,7 @@
 #include "huffman.cuh"
 #include "passes.cuh"
 #include "static_kernels.h"
+#include "decode.cuh"
 
 using namespace ffcz;
 
@@ -65,6 +66,7 @@ struct ffcz_solver {
   unsigned *d_blk_cnt = nullptr;
   void *d_blk_mn = nullptr, *d_blk_mx = nullptr, *d_mnmx = nullptr;
   size_t nblk_max = 0;
+  unsigned long long *d_up_blk = nullptr;  // decoder: set flags per chunk (lazy)
   // plans
   AxisPlan pz{}, py{}, px{};
   AxisPlan pz_s{}, py_s{}, px_s{};  // plans of the compile-time-sized kernels
@@ -514,6 +516,7 @@ void free_all(ffcz_solver *s) {
                   s->d_blk_mn, s->d_blk_mx, s->d_mnmx};
   for (void *p : bufs)
     if (p) cudaFree(p);
+  if (s->d_up_blk) cudaFree(s->d_up_blk);
   if (s->h_ctl) cudaFreeHost(s->h_ctl);
   if (s->cap) cudaStreamDestroy(s->cap);
   for (cudaEvent_t e : s->ev)
@@ -534,6 +537,70 @@ int copy_out(const void *src, size_t bytes, void *dst, size_t cap_bytes, cudaStr
   if (cap_bytes < bytes) return fail(FFCZ_ERR_CAPACITY, "destination too small");
   FFCZ_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, st));
   FFCZ_CUDA(cudaStreamSynchronize(st));
+  return FFCZ_OK;
+}
+
+// Flag pack + codes of one edit array -> dequantised values (spectrum or
+// dense), on the solver's stream.  The pack is copied into the solver's
+// zero-padded pack buffer (whole 32-bit words) unless it already is it.
+template <typename T>
+int unpack_edits(ffcz_solver *s, const uint16_t *quant, size_t count, const uint8_t *pack, size_t n, double mn,
+                 double mx, uint8_t *pack_buf, size_t pack_alloc, T *dense, c2<T> *spec) {
+  cudaStream_t st = s->stream;
+  if (pack != pack_buf) {
+    FFCZ_CUDA(cudaMemsetAsync(pack_buf, 0, pack_alloc, st));
+    FFCZ_CUDA(cudaMemcpyAsync(pack_buf, pack, (n + 7) / 8, cudaMemcpyDeviceToDevice, st));
+  }
+  const size_t nblk = ceil_div(n, (size_t)UP_CHUNK);
+  if (!s->d_up_blk) FFCZ_CUDA(cudaMalloc(&s->d_up_blk, (s->nblk_max + 1) * sizeof(unsigned long long)));
+  const unsigned *words = reinterpret_cast<const unsigned *>(pack_buf);
+  k_unpack_count<<<(unsigned)nblk, UP_THREADS, 0, st>>>(words, (long long)n, s->d_up_blk);
+  k_unpack_scan<<<1, 1024, 0, st>>>(s->d_up_blk, (long long)nblk);
+  k_unpack_scatter<T><<<(unsigned)nblk, UP_THREADS, 0, st>>>(words, (long long)n, s->d_up_blk, quant,
+                                                             (long long)count, (T)mn, (T)mx, dense, spec,
+                                                             (long long)s->H, s->Hz, s->Hzp);
+  FFCZ_CUDA(cudaGetLastError());
+  return FFCZ_OK;
+}
+
+// x^ = x' + (C2R(frequency edits)/N + spatial edits).  The frequency edits
+// go straight into the half spectrum, the inverse passes of the solver's
+// plan run over it (x, y, then the C2R along z with the 1/N factor into the
+// e buffer), and the spatial edits are unpacked into the spatial-edit
+// accumulator before the final sum.
+template <typename T>
+int reconstruct(ffcz_solver *s, const void *d_decomp, const uint16_t *fq, size_t nf, const uint8_t *fpack,
+                double fmin, double fmax, const uint16_t *sq, size_t ns, const uint8_t *spack, double smin,
+                double smax, void *d_out) {
+  cudaStream_t st = s->stream;
+  const long long H = (long long)s->H;
+  c2<T> *spec = (c2<T> *)s->d_spec;
+  FFCZ_CUDA(cudaMemsetAsync(s->d_spec, 0, (size_t)s->rows * s->Hzp * 2 * s->es, st));
+  if (nf) FFCZ_TRY(unpack_edits<T>(s, fq, nf, fpack, 2 * s->H, fmin, fmax, s->d_fpack, s->fpack_bytes, nullptr, spec));
+  const T delta = (T)s->delta;
+  if (s->fused == 2) {
+    ((StridedFn<T>)s->kx[MODE_INV])<<<s->lx.grid, s->lx.threads, s->lx.smem, st>>>(spec, s->sx, s->px, delta,
+                                                                                   tp<T>(s->d_fedits), H);
+    if (s->has_y)
+      ((StridedFn<T>)s->ky[MODE_INV])<<<s->ly.grid, s->ly.threads, s->ly.smem, st>>>(spec, s->sy, s->py, delta,
+                                                                                     tp<T>(s->d_fedits), H);
+  } else if (s->fused == 1) {
+    ((StridedFn<T>)s->ky[MODE_INV])<<<s->ly.grid, s->ly.threads, s->ly.smem, st>>>(spec, s->sy, s->py, delta,
+                                                                                   tp<T>(s->d_fedits), H);
+  }
+  const c2<T> *post = (const c2<T> *)s->d_tw + s->post_off;
+  const T factor = T(1) / static_cast<T>(s->N);
+  ((ZinvFn<T>)s->kzi)<<<s->lz_i.grid, s->lz_i.threads, s->lz_i.smem, st>>>(spec, tp<T>(s->d_e), (T)s->eps, factor,
+                                                                          s->d_ctl, s->za, s->pz, post);
+  FFCZ_CUDA(cudaMemsetAsync(s->d_sedits, 0, s->N * s->es, st));
+  if (ns) FFCZ_TRY(unpack_edits<T>(s, sq, ns, spack, s->N, smin, smax, s->d_spack, s->spack_bytes, tp<T>(s->d_sedits),
+                                   nullptr));
+  const unsigned g = (unsigned)std::min<size_t>(ceil_div(s->N, 256), 152 * 16);
+  k_recon_sum<T><<<g, 256, 0, st>>>((const T *)d_decomp, tp<T>(s->d_e), tp<T>(s->d_sedits), (T *)d_out,
+                                    (long long)s->N);
+  FFCZ_CUDA(cudaGetLastError());
+  FFCZ_CUDA(cudaStreamSynchronize(st));
+  s->extracted = false;
   return FFCZ_OK;
 }
 
@@ -881,6 +948,47 @@ int ffcz_get_pass_times(ffcz_solver *s, double *ms, double *bytes, int cap, int 
     else bytes[i] = 4.0 * H * es;
   }
   return FFCZ_OK;
+}
+
+int ffcz_reconstruct_device(ffcz_solver *s, const void *d_decomp, const uint16_t *d_freq_quant, size_t n_freq,
+                            const uint8_t *d_freq_pack, double freq_min, double freq_max,
+                            const uint16_t *d_spatial_quant, size_t n_spatial, const uint8_t *d_spatial_pack,
+                            double spatial_min, double spatial_max, void *d_out) {
+  FFCZ_TRY(check_solver(s));
+  FFCZ_TRY(check_dev_ptr(d_decomp, "decompressed data"));
+  FFCZ_TRY(check_dev_ptr(d_out, "output"));
+  if (n_freq > 2 * s->H || n_spatial > s->N) return fail(FFCZ_ERR_INVALID, "more edits than elements");
+  if ((n_freq && (!d_freq_quant || !d_freq_pack)) || (n_spatial && (!d_spatial_quant || !d_spatial_pack)))
+    return fail(FFCZ_ERR_INVALID, "edit stream is NULL");
+  return DISPATCH(s, reconstruct, s, d_decomp, d_freq_quant, n_freq, d_freq_pack, freq_min, freq_max,
+                  d_spatial_quant, n_spatial, d_spatial_pack, spatial_min, spatial_max, d_out);
+}
+
+int ffcz_solver_decode(ffcz_solver *s, const void *d_decomp, ffcz_huff_result *const *in4, double freq_min,
+                       double freq_max, double spatial_min, double spatial_max, void *d_out) {
+  FFCZ_TRY(check_solver(s));
+  if (!in4) return fail(FFCZ_ERR_INVALID, "in4 is NULL");
+  const size_t nf = in4[0] ? in4[0]->num_elements : 0, ns = in4[2] ? in4[2]->num_elements : 0;
+  const size_t fpb = (2 * s->H + 7) / 8, spb = (s->N + 7) / 8;
+  if ((nf && (!in4[1] || in4[1]->num_elements != fpb)) || (ns && (!in4[3] || in4[3]->num_elements != spb)))
+    return fail(FFCZ_ERR_INVALID, "an edit stream needs its flag pack of ceil(n/8) bytes");
+  if (nf > 2 * s->H || ns > s->N) return fail(FFCZ_ERR_INVALID, "more edits than elements");
+  struct Job { const ffcz_huff_result *r; int sb; void *dst; size_t n; };
+  const Job jobs[4] = {{in4[0], 2, s->d_fquant, nf}, {in4[1], 1, s->d_fpack, nf ? fpb : 0},
+                       {in4[2], 2, s->d_squant, ns}, {in4[3], 1, s->d_spack, ns ? spb : 0}};
+  FFCZ_CUDA(cudaMemsetAsync(s->d_fpack, 0, s->fpack_bytes, s->stream));
+  FFCZ_CUDA(cudaMemsetAsync(s->d_spack, 0, s->spack_bytes, s->stream));
+  for (const Job &j : jobs) {
+    if (!j.n) continue;
+    const ffcz_huff_result *r = j.r;
+    size_t got = 0;
+    FFCZ_TRY(huff_decode_bits(r->bitstream.data(), r->bitstream.size(), cudaMemcpyHostToDevice, r->symbols.data(),
+                              r->codes.data(), r->lengths.data(), r->symbols.size(), j.n, j.sb, j.dst, &got,
+                              s->stream));
+    if (got != j.n) return fail(FFCZ_ERR_INVALID, "a stream decodes to fewer symbols than it declares");
+  }
+  return ffcz_reconstruct_device(s, d_decomp, (const uint16_t *)s->d_fquant, nf, s->d_fpack, freq_min, freq_max,
+                                 (const uint16_t *)s->d_squant, ns, s->d_spack, spatial_min, spatial_max, d_out);
 }
 
 int ffcz_solver_encode(ffcz_solver *s, int zstd_level, int zstd_mode, ffcz_huff_result **out4) {

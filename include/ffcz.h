@@ -280,6 +280,66 @@ int ffcz_solver_encode(ffcz_solver *s, int zstd_level, int zstd_mode,
                        ffcz_huff_result **out4);
 
 /* ======================================================================== *
+ * Decoder side (no counterpart in the reference beyond the host decode of  *
+ * HuffmanZSTDCoder.cuh:378-450 and the commented-out reconstruction of     *
+ * projection_algorithm_impl.cuh:912-985)                                   *
+ * ======================================================================== */
+/* GPU prefix decode of a Huffman bitstream with the rules of the host
+ * decoder above (same output, symbol for symbol): d_bits is DEVICE memory of
+ * nbytes; up to num_elements symbols (symbol_bytes 1 or 2) go to d_out
+ * (device); *decoded receives the count.  Runs on `stream`, returns after
+ * it finished. */
+int ffcz_huff_decode_device(const uint8_t *d_bits, size_t nbytes,
+                            const uint32_t *symbols, const uint32_t *codes,
+                            const int32_t *lengths, size_t num_symbols,
+                            size_t num_elements, int symbol_bytes, void *d_out,
+                            size_t *decoded, void *stream);
+/* ZSTD_decompress on the host, then the GPU decode into d_out (device). */
+int ffcz_huff_zstd_decompress_device(const uint8_t *comp, size_t comp_len,
+                                     const uint32_t *symbols,
+                                     const uint32_t *codes,
+                                     const int32_t *lengths,
+                                     size_t num_symbols, size_t num_elements,
+                                     size_t bitstream_bytes, int symbol_bytes,
+                                     void *d_out, size_t *decoded,
+                                     void *stream);
+/* A coder result rebuilt from its stored parts (ZSTD frame, code table,
+ * counts) for decoding.  bitstream: the Huffman bitstream when at hand;
+ * NULL: recovered here from `compressed` (ZSTD_decompress into
+ * bitstream_bytes bytes). */
+int ffcz_huff_result_create(const uint8_t *compressed, size_t comp_len,
+                            const uint8_t *bitstream, size_t bitstream_bytes,
+                            const uint32_t *symbols, const uint32_t *codes,
+                            const int32_t *lengths, size_t num_symbols,
+                            size_t num_elements, ffcz_huff_result **out);
+/* Reconstruction of the corrected field from decoded edit streams:
+ *   x^ = x' + (C2R(F)/N + S)
+ * F = the frequency edits (planar Re | Im over the half spectrum), S = the
+ * spatial edits, each rebuilt from its flag pack (LSB-first, FFCZ_PACK_CORRECT
+ * layout) and its uint16 codes dequantised as q/65535*(max-min)+min in T
+ * (the inverse of projection_algorithm.cu:447-455, following :638).  All
+ * arrays are device memory; d_decomp = x', d_out = x^ (N values of the
+ * solver's dtype; may alias neither input).  Uses the solver's spectrum,
+ * e and spatial-edit buffers (a previous solve's results are overwritten;
+ * afterwards ffcz_get_spatial_edits_full returns the dequantised spatial
+ * edits).  Returns after the solver's stream finished. */
+int ffcz_reconstruct_device(ffcz_solver *s, const void *d_decomp,
+                            const uint16_t *d_freq_quant, size_t n_freq,
+                            const uint8_t *d_freq_pack, double freq_min,
+                            double freq_max, const uint16_t *d_spatial_quant,
+                            size_t n_spatial, const uint8_t *d_spatial_pack,
+                            double spatial_min, double spatial_max,
+                            void *d_out);
+/* The whole decoder from the four coder results ffcz_solver_encode returns
+ * (frequency codes, frequency flag pack, spatial codes, spatial flag pack;
+ * NULL for an empty pair): GPU Huffman decode of each stream, then
+ * ffcz_reconstruct_device.  min/max are ffcz_get_minmax's values. */
+int ffcz_solver_decode(ffcz_solver *s, const void *d_decomp,
+                       ffcz_huff_result *const *in4, double freq_min,
+                       double freq_max, double spatial_min,
+                       double spatial_max, void *d_out);
+
+/* ======================================================================== *
  * Allocation-free compaction                                               *
  * ======================================================================== */
 /* No counterpart in the reference.  The compaction of one edit accumulator

@@ -235,6 +235,38 @@ def huffman_decode(bits: bytes, book: dict, num_elements: int) -> np.ndarray:
     return out[:k]
 
 
+# ---------------------------------------------------------------- decoder
+def dequantize(quant: np.ndarray, mn: float, mx: float, dtype=np.float32) -> np.ndarray:
+    """Inverse of the quantiser in the order of projection_algorithm.cu:638:
+    q / 65535 * (max - min) + min, every operation rounded to T."""
+    T = np.dtype(dtype).type
+    q = np.asarray(quant).astype(T)
+    return (q / T(65535)) * (T(mx) - T(mn)) + T(mn)
+
+
+def unpack_edits(quant: np.ndarray, pack: bytes, n: int, mn: float, mx: float, dtype=np.float32) -> np.ndarray:
+    """Dense edit array of n values: the r-th set flag of the LSB-first pack
+    (ascending index) receives dequantize(quant[r]); zero elsewhere."""
+    flags = np.unpackbits(np.frombuffer(pack, np.uint8), bitorder="little")[:n].astype(bool)
+    out = np.zeros(n, dtype)
+    idx = np.flatnonzero(flags)
+    k = min(idx.size, len(quant))
+    out[idx[:k]] = dequantize(np.asarray(quant)[:k], mn, mx, dtype)
+    return out
+
+
+def reconstruct(xprime: np.ndarray, shape, freq_edits: np.ndarray, spatial_edits: np.ndarray) -> np.ndarray:
+    """x^ = x' + C2R(F)/N + S in FP64: F the planar half-spectrum edits
+    (Re | Im), C2R the unnormalised inverse real transform (imaginary parts of
+    the self-conjugate bins of the last axis ignored)."""
+    shape = tuple(int(v) for v in shape)
+    H = shape[0] * shape[1] * (shape[2] // 2 + 1)
+    fe = np.asarray(freq_edits, np.float64)
+    F = (fe[:H] + 1j * fe[H:]).reshape(shape[0], shape[1], shape[2] // 2 + 1)
+    e = _irfftn(F, s=shape)
+    return np.asarray(xprime, np.float64).reshape(shape) + e + np.asarray(spatial_edits, np.float64).reshape(shape)
+
+
 # --------------------------------------------------------------------- ZSTD
 _z = None
 

@@ -110,3 +110,27 @@ def test_generator_deterministic(shape):
     assert abs(float(a.x.astype(np.float64).std()) - 1.0) < 1e-3
     # x' = 2E round(x/2E) + U(-0.3E, 0.3E): |x' - x| <= 1.3 E
     assert np.abs(a.xp.astype(np.float64) - a.x).max() <= 1.3 * a.eps * (1 + 1e-5)
+
+
+def test_reconstruction_formula_recovers_the_corrected_field():
+    """x' + C2R(accumulated frequency edits)/N + accumulated spatial edits
+    equals x + e of the FP64 loop (the projections are linear in e)."""
+    from ffcz_gb300 import synth
+
+    shape = (10, 12, 14)
+    fld = synth.make_field(shape, 11 / 3, 8, 1e-3, 1e-3, np.float64, noise=0.3)
+    delta = synth.stress_delta(fld, 1.0)
+    e0 = fld.xp - fld.x
+    r = O.solve_all_abs(e0, shape, fld.eps, delta, 100, 1e-7, np.float64)
+    assert r["iterations"] > 1 and np.any(r["freq_edits"]) and np.any(r["spatial_edits"])
+    xhat = O.reconstruct(fld.xp, shape, r["freq_edits"], r["spatial_edits"])
+    assert np.abs(xhat - (fld.x + r["e"])).max() <= 1e-12 * max(1.0, np.abs(fld.x).max())
+
+
+def test_dequantize_inverts_the_quantiser():
+    v = np.random.default_rng(1).uniform(-3, 5, 1000).astype(np.float32)
+    mn, mx = float(v.min()), float(v.max())
+    q = np.array([O.quantize(x, mn, mx) for x in v])
+    d = O.dequantize(q, mn, mx, np.float32)
+    assert d.dtype == np.float32
+    assert np.abs(d.astype(np.float64) - v).max() <= (mx - mn) / 65535 * 1.01
