@@ -127,6 +127,9 @@ SIGNATURES = {
     "ffcz_huff_result_create": [_p, _sz, _p, _sz, _p, _p, _p, _sz, _sz, _PP],
     "ffcz_reconstruct_device": [_p, _p, _p, _sz, _p, _d, _d, _p, _sz, _p, _d, _d, _p],
     "ffcz_solver_decode": [_p, _p, _PP, _d, _d, _d, _d, _p],
+    "ffcz_solver_container_header": [_p, _p],
+    "ffcz_container_write": [C.c_char_p, _p, _PP],
+    "ffcz_container_read": [C.c_char_p, _p, _PP],
     "ffcz_write_map": [C.c_char_p, _p, _p, _p, _sz],
     "ffcz_read_map": [C.c_char_p, _p, _p, _p, _sz, _SP],
     "ffcz_last_error": [],
@@ -355,6 +358,11 @@ class ProjectionSolver:
                                              _dev_ptr(fp) or None, fmn, fmx, _dev_ptr(sq) or None, ns,
                                              _dev_ptr(sp) or None, smn, smx, _dev_ptr(d_out)))
 
+    def container_header(self) -> "ContainerHeader":
+        h = ContainerHeader()
+        _check(lib().ffcz_solver_container_header(self._h, C.byref(h)))
+        return h
+
     def decode_device(self, d_xprime, streams, minmax, d_out) -> None:
         """The decoder: the four CompressionResults of :meth:`encode` (None
         where empty) and :meth:`minmax`'s values -> x^ in d_out (device)."""
@@ -498,6 +506,42 @@ def _take_result(p: int) -> CompressionResult:
         return CompressionResult(comp, *arrs, bn, nel.value, bits)
     finally:
         lib().ffcz_huff_result_free(p)
+
+
+class ContainerHeader(C.Structure):
+    """ffcz_container_header: what the decoder needs besides x' and the streams."""
+    _fields_ = [("dtype", C.c_uint32), ("pack_mode", C.c_uint32), ("nx", C.c_uint64), ("ny", C.c_uint64),
+                ("nz", C.c_uint64), ("eps", C.c_double), ("delta", C.c_double), ("freq_min", C.c_double),
+                ("freq_max", C.c_double), ("spatial_min", C.c_double), ("spatial_max", C.c_double),
+                ("iterations", C.c_uint32)]
+
+    @property
+    def shape(self):
+        return (self.nx, self.ny, self.nz)
+
+    @property
+    def minmax(self):
+        return (self.freq_min, self.freq_max, self.spatial_min, self.spatial_max)
+
+
+def write_container(path, header: ContainerHeader, streams) -> None:
+    """Writes the .ffcz container (header + the four coder results)."""
+    handles = [None if r is None else r.native() for r in streams]
+    arr = (C.c_void_p * 4)(*[h.value if h is not None else None for h in handles])
+    try:
+        _check(lib().ffcz_container_write(str(path).encode(), C.byref(header), arr))
+    finally:
+        for h in handles:
+            if h is not None:
+                lib().ffcz_huff_result_free(h)
+
+
+def read_container(path):
+    """(ContainerHeader, [four CompressionResult or None]) of a .ffcz file."""
+    h = ContainerHeader()
+    arr = (C.c_void_p * 4)()
+    _check(lib().ffcz_container_read(str(path).encode(), C.byref(h), arr))
+    return h, [None if not p else _take_result(p) for p in arr]
 
 
 def cuda_huffman_zstd_compress(data, zstd_level: int = 3) -> CompressionResult:

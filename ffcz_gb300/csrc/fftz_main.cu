@@ -1,19 +1,25 @@
 // fftz: command-line driver with the flags and output lines of
 // projection_example.cu:1-279, running the GB300 solver and encoder.
 //
-//   fftz -i x.bin -e x'.bin [-z out] [-o out] (-1 n | -2 ny nz | -3 nx ny nz)
-//        [-f|-d] -M ABS|REL eps -F ABS|REL delta
+//   fftz -i x.bin -e x'.bin [-z out.ffcz] [-o xhat.bin] (-1 n | -2 ny nz |
+//        -3 nx ny nz) [-f|-d] -M ABS|REL eps -F ABS|REL delta
+//   fftz -e x'.bin -z in.ffcz -o xhat.bin          (decompression)
 //
 // As in the reference: bounds are absolute whatever ABS/REL says
 // (:124-137), eps/delta are parsed as float (:129, :136), -1/-2/-3 must be
-// followed by another argument (:111-114), -z/-o are accepted but nothing is
-// written (:255-256), max_iterations = 100 and tolerance = 1e-7 (:199-200),
-// the four streams are Huffman+ZSTD coded at level 20 (:233-246), and the
-// printed "Compression time" is 3*(getter time) + solve time (:250).
+// followed by another argument (:111-114), max_iterations = 100 and
+// tolerance = 1e-7 (:199-200), the four streams are Huffman+ZSTD coded at
+// level 20 (:233-246), and the printed "Compression time" is 3*(getter
+// time) + solve time (:250).  Where the reference parses -z/-o but writes
+// nothing (:255-256), this driver writes the .ffcz container to -z and the
+// decoder's reconstruction x^ = x' + C2R(F)/N + S to -o; without -i it
+// decompresses (-z container + -e x' -> -o).
 #include <chrono>
 #include <cstdio>
 #include <cstring>
 #include <iostream>
+#include <memory>
+#include <stdexcept>
 #include <string>
 #include <vector>
 
@@ -101,6 +107,51 @@ void Parsing(int argc, char *argv[]) {
     parseError("Input files of original data (-i) and base decompressed data (-e) are mandatory");
 }
 
+void check(int rc) {
+  if (rc != FFCZ_OK) throw std::runtime_error(ffcz_last_error());
+}
+
+struct Streams {
+  ffcz_huff_result *r[4] = {nullptr, nullptr, nullptr, nullptr};
+  ~Streams() {
+    for (ffcz_huff_result *p : r) ffcz_huff_result_free(p);
+  }
+};
+
+// GPU decode of the four streams + reconstruction with x' on a solver of
+// the header's shape.
+template <typename T>
+std::vector<T> decode(const ffcz_container_header &h, const Streams &st, const std::vector<T> &xp) {
+  ffcz_solver *s = nullptr;
+  check(ffcz_solver_create(h.nx, h.ny, h.nz, sizeof(T) == 4 ? FFCZ_F32 : FFCZ_F64, &s));
+  std::unique_ptr<ffcz_solver, int (*)(ffcz_solver *)> guard(s, ffcz_solver_destroy);
+  const size_t n = xp.size();
+  T *d_xp = nullptr, *d_out = nullptr;
+  CHECK_CUDA(cudaMalloc(&d_xp, n * sizeof(T)));
+  CHECK_CUDA(cudaMalloc(&d_out, n * sizeof(T)));
+  CHECK_CUDA(cudaMemcpy(d_xp, xp.data(), n * sizeof(T), cudaMemcpyHostToDevice));
+  const int rc = ffcz_solver_decode(s, d_xp, st.r, h.freq_min, h.freq_max, h.spatial_min, h.spatial_max, d_out);
+  std::vector<T> out(n);
+  if (rc == FFCZ_OK) CHECK_CUDA(cudaMemcpy(out.data(), d_out, n * sizeof(T), cudaMemcpyDeviceToHost));
+  cudaFree(d_xp);
+  cudaFree(d_out);
+  check(rc);
+  return out;
+}
+
+template <typename T>
+void Decompress(const ffcz_container_header &h, const Streams &st) {
+  const size_t n = (size_t)(h.nx * h.ny * h.nz);
+  std::vector<T> xp(n);
+  readRawArrayBinary(baseDecompFile, xp.data(), n, sizeof(T) == 4 ? DataType::FLOAT : DataType::DOUBLE);
+  const auto t0 = std::chrono::high_resolution_clock::now();
+  std::vector<T> xhat = decode<T>(h, st, xp);
+  const auto t1 = std::chrono::high_resolution_clock::now();
+  if (!decompressedFile.empty()) writeRawArrayBinary(xhat.data(), n, decompressedFile);
+  std::cout << "Decompression time: "
+            << std::chrono::duration_cast<std::chrono::milliseconds>(t1 - t0).count() << " ms" << std::endl;
+}
+
 template <typename T>
 void Run() {
   std::vector<T> x(spatial_size), err(spatial_size);
@@ -124,13 +175,34 @@ void Run() {
   const auto t2 = std::chrono::high_resolution_clock::now();
 
   size_t extra_storage = 0;
-  if (!fq.empty()) {
-    extra_storage += cudaHuffmanZstdCompress(fq, 20).compressed_data.size();
-    extra_storage += cudaHuffmanZstdCompress(fp, 20).compressed_data.size();
-  }
-  if (!sq.empty()) {
-    extra_storage += cudaHuffmanZstdCompress(sq, 20).compressed_data.size();
-    extra_storage += cudaHuffmanZstdCompress(sp, 20).compressed_data.size();
+  if (compressedFile.empty() && decompressedFile.empty()) {
+    if (!fq.empty()) {
+      extra_storage += cudaHuffmanZstdCompress(fq, 20).compressed_data.size();
+      extra_storage += cudaHuffmanZstdCompress(fp, 20).compressed_data.size();
+    }
+    if (!sq.empty()) {
+      extra_storage += cudaHuffmanZstdCompress(sq, 20).compressed_data.size();
+      extra_storage += cudaHuffmanZstdCompress(sp, 20).compressed_data.size();
+    }
+  } else {
+    // the same four streams once, through the C ABI, for the container
+    // and the decoder
+    Streams st;
+    check(ffcz_solver_encode(solver.handle(), 20, FFCZ_ZSTD_SINGLE, st.r));
+    for (ffcz_huff_result *r : st.r) {
+      size_t cb = 0;
+      if (r) check(ffcz_huff_result_sizes(r, &cb, nullptr, nullptr, nullptr));
+      extra_storage += cb;
+    }
+    ffcz_container_header h;
+    check(ffcz_solver_container_header(solver.handle(), &h));
+    if (!compressedFile.empty()) check(ffcz_container_write(compressedFile.c_str(), &h, st.r));
+    if (!decompressedFile.empty()) {
+      std::vector<T> xp(spatial_size);
+      readRawArrayBinary(baseDecompFile, xp.data(), spatial_size, dt);
+      std::vector<T> xhat = decode<T>(h, st, xp);
+      writeRawArrayBinary(xhat.data(), spatial_size, decompressedFile);
+    }
   }
   (void)extra_storage;
   printf("# Active frequency edits: %zu\n", fq.size());
@@ -147,6 +219,14 @@ void Run() {
 int main(int argc, char *argv[]) {
   Parsing(argc, argv);
   try {
+    if (originalFile.empty() && !compressedFile.empty()) {
+      Streams st;
+      ffcz_container_header h;
+      check(ffcz_container_read(compressedFile.c_str(), &h, st.r));
+      if (h.dtype == FFCZ_F64) Decompress<double>(h, st);
+      else Decompress<float>(h, st);
+      return 0;
+    }
     if (isDouble) Run<double>();
     else Run<float>();
   } catch (const std::exception &e) {

@@ -991,6 +991,22 @@ int ffcz_solver_decode(ffcz_solver *s, const void *d_decomp, ffcz_huff_result *c
                                  (const uint16_t *)s->d_squant, ns, s->d_spack, spatial_min, spatial_max, d_out);
 }
 
+int ffcz_solver_container_header(ffcz_solver *s, ffcz_container_header *h) {
+  FFCZ_TRY(check_solver(s));
+  if (!h) return fail(FFCZ_ERR_INVALID, "NULL argument");
+  *h = ffcz_container_header{};
+  h->dtype = (uint32_t)s->dtype;
+  h->pack_mode = (uint32_t)s->pack_mode;
+  h->nx = s->nx;
+  h->ny = s->ny;
+  h->nz = s->nz;
+  h->eps = s->eps;
+  h->delta = s->delta;
+  FFCZ_TRY(ffcz_get_minmax(s, &h->freq_min, &h->freq_max, &h->spatial_min, &h->spatial_max));
+  h->iterations = (uint32_t)s->h_ctl->iterations;
+  return FFCZ_OK;
+}
+
 int ffcz_solver_encode(ffcz_solver *s, int zstd_level, int zstd_mode, ffcz_huff_result **out4) {
   FFCZ_TRY(check_solver(s));
   if (!out4) return fail(FFCZ_ERR_INVALID, "out4 is NULL");

@@ -339,6 +339,31 @@ int ffcz_solver_decode(ffcz_solver *s, const void *d_decomp,
                        double freq_max, double spatial_min,
                        double spatial_max, void *d_out);
 
+/* ---- the .ffcz container ------------------------------------------------ */
+/* The reference's CLI parses -z/-o but writes nothing (projection_example.cu:
+ * 75-86, 255-256).  One file holds what the decoder needs besides x': shape,
+ * dtype, bounds, min/max of both edit arrays and the four coder results
+ * (each with its code table in writeMap's layout, fileIO.cpp:3-33).  Layout
+ * in ffcz_gb300/csrc/container.cpp. */
+typedef struct {
+  uint32_t dtype;       /* FFCZ_F32 / FFCZ_F64 */
+  uint32_t pack_mode;   /* flag-pack mode of the streams */
+  uint64_t nx, ny, nz;
+  double eps, delta;
+  double freq_min, freq_max, spatial_min, spatial_max;
+  uint32_t iterations;
+} ffcz_container_header;
+/* Header of the solver's last solve (shape, dtype, bounds, min/max,
+ * iterations, pack mode). */
+int ffcz_solver_container_header(ffcz_solver *s, ffcz_container_header *h);
+/* in4: ffcz_solver_encode's four results (NULL = absent). */
+int ffcz_container_write(const char *path, const ffcz_container_header *h,
+                         ffcz_huff_result *const *in4);
+/* Reads a container; out4 receives four new results (NULL = absent, caller
+ * frees) with their bitstreams restored, ready for ffcz_solver_decode. */
+int ffcz_container_read(const char *path, ffcz_container_header *h,
+                        ffcz_huff_result **out4);
+
 /* ======================================================================== *
  * Allocation-free compaction                                               *
  * ======================================================================== */

@@ -111,3 +111,33 @@ def test_zstd_stage_bytes_equal_zstd_compress():
     with ThreadPoolExecutor(3) as pool:
         got = list(pool.map(lambda c: F.zstd_compress(*c), cases * 2))
     assert got == expect * 2
+
+
+def test_container_round_trip(tmp_path):
+    """Header fields, code tables, ZSTD frames and the restored bitstreams of
+    a .ffcz container survive write + read (host only)."""
+    rng = np.random.default_rng(3)
+    streams = []
+    for i, (n, dt) in enumerate(((500, np.uint16), (100, np.uint8), None, None)[:2]):
+        sym = rng.geometric(0.2, n).astype(dt)
+        book = O.huffman_codebook(sym)
+        bits, _ = O.huffman_bitstream(sym, book)
+        comp = O.zstd_compress(bits, 3)
+        streams.append(F.CompressionResult(comp, book["symbols"], book["codes"], book["lengths"], len(bits), n, b""))
+    streams += [None, None]
+    h = F.ContainerHeader(dtype=F.FFCZ_F32, pack_mode=0, nx=2, ny=3, nz=40, eps=1e-3, delta=2.5, freq_min=-1.0,
+                          freq_max=1.5, spatial_min=-0.1, spatial_max=0.2, iterations=7)
+    path = tmp_path / "c.ffcz"
+    F.write_container(path, h, streams)
+    h2, got = F.read_container(path)
+    for f, _ in F.ContainerHeader._fields_:
+        assert getattr(h2, f) == getattr(h, f), f
+    assert got[2] is None and got[3] is None
+    for a, b in zip(streams[:2], got[:2]):
+        assert b.compressed_data == a.compressed_data and b.num_elements == a.num_elements
+        assert np.array_equal(b.symbols, a.symbols) and np.array_equal(b.codes, a.codes)
+        assert np.array_equal(b.lengths, a.lengths)
+        assert b.bitstream == O.zstd_decompress(a.compressed_data, a.original_bitstream_size)
+    path.write_bytes(path.read_bytes()[:50])
+    with pytest.raises(F.FFCzError):
+        F.read_container(path)
