@@ -27,6 +27,7 @@ LIB_PATH = _PKG / "_build" / "libffcz.so"
 FFCZ_OK = 0
 FFCZ_F32, FFCZ_F64 = 0, 1
 FFCZ_PACK_CORRECT, FFCZ_PACK_REFERENCE = 0, 1
+FFCZ_MODE_ALL_ABS, FFCZ_MODE_DIRECT, FFCZ_MODE_ALL_PTW, FFCZ_MODE_PARTIAL_PTW = 0, 1, 2, 3
 FFCZ_LOOP_GRAPH, FFCZ_LOOP_HOST = 0, 1
 FFCZ_ZSTD_SINGLE, FFCZ_ZSTD_CHUNKED, FFCZ_ZSTD_NONE = 0, 1, 2
 ERRORS = {-1: "INVALID", -2: "CUDA", -3: "UNSUPPORTED", -4: "NOT_INITIALIZED", -5: "ZSTD",
@@ -130,6 +131,14 @@ SIGNATURES = {
     "ffcz_solver_container_header": [_p, _p],
     "ffcz_container_write": [C.c_char_p, _p, _PP],
     "ffcz_container_read": [C.c_char_p, _p, _PP],
+    "ffcz_init_direct": [_p, _p, _p, _p, _d, _sz],
+    "ffcz_get_orig_spectrum": [_p, _p, _sz],
+    "ffcz_init_all_ptw": [_p, _p, _d, _d],
+    "ffcz_init_all_ptw_device": [_p, _p, _d, _d],
+    "ffcz_init_partial_ptw": [_p, _p, _p, _d, _d, _sz],
+    "ffcz_solve": [_p, _p, _i, _d],
+    "ffcz_solve_all_ptw": [_p, _p, _i, _d],
+    "ffcz_solve_mode_device": [_p, _i, _p, _i, _d],
     "ffcz_write_map": [C.c_char_p, _p, _p, _p, _sz],
     "ffcz_read_map": [C.c_char_p, _p, _p, _p, _sz, _SP],
     "ffcz_last_error": [],
@@ -241,6 +250,53 @@ class ProjectionSolver:
     def solve_all_abs_pair_device(self, d_x, d_xprime, max_iterations: int = 100, tol: float = 1e-7) -> int:
         _check(lib().ffcz_solve_all_abs_pair_device(self._h, _dev_ptr(d_x), _dev_ptr(d_xprime),
                                                      int(max_iterations), float(tol)))
+        return self._iters()
+
+    # -- the other constraint modes (impl:598-738, 772-814, 860-902) --------
+    def _indices(self, idx) -> np.ndarray:
+        return np.ascontiguousarray(idx, dtype=np.uint64).reshape(-1)
+
+    def initialize(self, x, freq_indices, delta_k, spatial_epsilon: float) -> None:
+        """Direct mode: coefficient freq_indices[c] within +-delta_k[c]."""
+        x = self._host(x)
+        idx = self._indices(freq_indices)
+        dk = np.ascontiguousarray(delta_k, dtype=self.dtype).reshape(-1)
+        if dk.size != idx.size:
+            raise ValueError("one delta_k per index")
+        _check(lib().ffcz_init_direct(self._h, _np_ptr(x), _np_ptr(idx) if idx.size else None,
+                                      _np_ptr(dk) if dk.size else None, float(spatial_epsilon), idx.size))
+
+    def initialize_all_ptw(self, x, spatial_epsilon: float, delta_ptw: float) -> None:
+        x = self._host(x)
+        _check(lib().ffcz_init_all_ptw(self._h, _np_ptr(x), float(spatial_epsilon), float(delta_ptw)))
+
+    def initialize_all_ptw_device(self, d_x, spatial_epsilon: float, delta_ptw: float) -> None:
+        _check(lib().ffcz_init_all_ptw_device(self._h, _dev_ptr(d_x), float(spatial_epsilon), float(delta_ptw)))
+
+    def initialize_partial_ptw(self, x, freq_indices, delta_ptw: float, spatial_epsilon: float) -> None:
+        x = self._host(x)
+        idx = self._indices(freq_indices)
+        _check(lib().ffcz_init_partial_ptw(self._h, _np_ptr(x), _np_ptr(idx) if idx.size else None,
+                                           float(delta_ptw), float(spatial_epsilon), idx.size))
+
+    def get_orig_spectrum(self) -> np.ndarray:
+        """The spectrum of x the pointwise modes compare against (H complex)."""
+        out = np.empty(self.H, np.complex64 if self.dtype == np.float32 else np.complex128)
+        _check(lib().ffcz_get_orig_spectrum(self._h, _np_ptr(out), self.H))
+        return out
+
+    def solve(self, e0, max_iterations: int = 100, tol: float = 1e-7) -> int:
+        e0 = self._host(e0)
+        _check(lib().ffcz_solve(self._h, _np_ptr(e0), int(max_iterations), float(tol)))
+        return self._iters()
+
+    def solve_all_ptw(self, e0, max_iterations: int = 100, tol: float = 1e-7) -> int:
+        e0 = self._host(e0)
+        _check(lib().ffcz_solve_all_ptw(self._h, _np_ptr(e0), int(max_iterations), float(tol)))
+        return self._iters()
+
+    def solve_mode_device(self, mode: int, d_e0, max_iterations: int = 100, tol: float = 1e-7) -> int:
+        _check(lib().ffcz_solve_mode_device(self._h, int(mode), _dev_ptr(d_e0), int(max_iterations), float(tol)))
         return self._iters()
 
     def project_all_abs_device(self, d_e0, max_iterations: int = 100, tol: float = 1e-7) -> int:

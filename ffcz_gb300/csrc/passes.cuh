@@ -77,6 +77,58 @@ __device__ __forceinline__ c2<T> freq_clamp(c2<T> v, T delta, T *__restrict__ fe
   return v;
 }
 
+// Frequency projection of every constraint mode, applied where the forward
+// transform's last pass holds coefficient k (flat index) at padded offset p:
+//   CLAMP_ABS    all coefficients, +-delta (projection_algorithm.cu:148-188)
+//   CLAMP_DIRECT +-bound[k], +inf where unconstrained (:93-145)
+//   CLAMP_PTW    pointwise power-spectrum box against the spectrum of x
+//                (:191-333): coefficient 0 by the DC rule, the others (mask
+//                null = all) clamped to +-cd when |orig+err|^2/|orig|^2
+//                leaves [sqrt(1-d), sqrt(1+d)].
+enum { CLAMP_ABS = 0, CLAMP_DIRECT = 1, CLAMP_PTW = 2 };
+
+template <typename T>
+struct ClampArgs {
+  int mode = CLAMP_ABS;
+  int dc = 0;                          // PTW: apply the DC rule at k = 0
+  T delta = T(0);                      // ABS
+  const T *bound = nullptr;            // DIRECT: H bounds
+  const c2<T> *orig = nullptr;         // PTW: spectrum of x, padded layout
+  const unsigned char *mask = nullptr; // PTW: constrained coefficients
+  T sp = T(0), sm = T(0), lo = T(0), hi = T(0), cd = T(0);  // PTW constants
+};
+
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+
+template <typename T>
+__device__ __forceinline__ c2<T> freq_project(c2<T> v, const ClampArgs<T> &ca, T *__restrict__ fedits, long long k,
+                                              long long p, long long H) {
+  if (ca.mode == CLAMP_ABS) return freq_clamp<T>(v, ca.delta, fedits, k, H);
+  if (ca.mode == CLAMP_DIRECT) return freq_clamp<T>(v, ca.bound[k], fedits, k, H);
+  if (k == 0) {
+    if (ca.dc) {
+      const T o = ca.orig[0].x;
+      const T lower = mul_rn(o, ca.lo), upper = mul_rn(o, ca.hi);
+      if (v.x > upper || v.x < lower) {
+        fedits[0] += -v.x;
+        v.x = T(0);
+      }
+    }
+    return v;
+  }
+  if (ca.mask && !ca.mask[k]) return v;
+  const c2<T> o = ca.orig[p];
+  const T om = add_rn(mul_rn(o.x, o.x), mul_rn(o.y, o.y));
+  const T cx = add_rn(o.x, v.x), cy = add_rn(o.y, v.y);
+  const T cm = add_rn(mul_rn(cx, cx), mul_rn(cy, cy));
+  const T ratio = cm / om;
+  if (ratio <= ca.sp && ratio >= ca.sm) return v;
+  return freq_clamp<T>(v, ca.cd, fedits, k, H);
+}
+
 // ---------------------------------------------------------------------------
 // R2C along z for TW consecutive rows.  Even Nz: the row is read as M = Nz/2
 // complex values z[n] = x[2n] + i x[2n+1], transformed with length M, and
@@ -300,7 +352,7 @@ __global__ void __launch_bounds__(sizeof(T) == 4 ? 512 : 256) k_zinv(const c2<T>
 // MODE_FCI: forward, frequency clamp with edit accumulation, inverse.
 template <typename T, int MODE, int EPT>
 __global__ void __launch_bounds__(sizeof(T) == 4 ? 512 : 256) k_strided(c2<T> *__restrict__ spec, SArgs s, AxisPlan p,
-                                                 T delta, T *__restrict__ fedits, long long H) {
+                                                 ClampArgs<T> ca, T *__restrict__ fedits, long long H) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   c2<T> *buf = reinterpret_cast<c2<T> *>(smem_raw);
   const int tid = threadIdx.x, nthr = blockDim.x;
@@ -334,7 +386,7 @@ __global__ void __launch_bounds__(sizeof(T) == 4 ? 512 : 256) k_strided(c2<T> *_
       const int c = it & (TW - 1);
       if (c < ncol) {
         const long long k = ((bb * s.L + l) * (long long)s.Q + q) * s.Hz + kz0 + c;
-        buf[l * P + c] = freq_clamp<T>(buf[l * P + c], delta, fedits, k, H);
+        buf[l * P + c] = freq_project<T>(buf[l * P + c], ca, fedits, k, base + (long long)l * s.Wtot + c, H);
       }
     }
     __syncthreads();
@@ -350,7 +402,7 @@ __global__ void __launch_bounds__(sizeof(T) == 4 ? 512 : 256) k_strided(c2<T> *_
 // Frequency box over the whole half spectrum when no strided axis exists
 // (Nx = Ny = 1).
 template <typename T>
-__global__ void k_clamp_freq(c2<T> *__restrict__ spec, long long rows, int Hz, int Hzp, T delta,
+__global__ void k_clamp_freq(c2<T> *__restrict__ spec, long long rows, int Hz, int Hzp, ClampArgs<T> ca,
                              T *__restrict__ fedits, long long H) {
   const long long total = rows * Hz;
   for (long long it = blockIdx.x * (long long)blockDim.x + threadIdx.x; it < total;
@@ -358,7 +410,7 @@ __global__ void k_clamp_freq(c2<T> *__restrict__ spec, long long rows, int Hz, i
     const long long r = it / Hz;
     const int kz = (int)(it - r * Hz);
     c2<T> *ptr = spec + r * Hzp + kz;
-    *ptr = freq_clamp<T>(*ptr, delta, fedits, it, H);
+    *ptr = freq_project<T>(*ptr, ca, fedits, it, r * Hzp + kz, H);
   }
 }
 

@@ -330,7 +330,7 @@ __host__ __device__ constexpr int strided_minb(int es, int nt, int E) {
 template <typename T, int MODE, int L, int LGTW>
 __global__ void __launch_bounds__((L / rp_elems(L)) << LGTW,
                                   strided_minb(sizeof(T), (L / rp_elems(L)) << LGTW, rp_elems(L))) ks_strided(c2<T> *__restrict__ spec, SArgs s,
-                                                                        AxisPlan p, T delta,
+                                                                        AxisPlan p, ClampArgs<T> ca,
                                                                         T *__restrict__ fedits, long long H) {
   using V = c2<T>;
   constexpr int E = rp_elems(L), TW = 1 << LGTW;
@@ -360,7 +360,8 @@ __global__ void __launch_bounds__((L / rp_elems(L)) << LGTW,
       for (int i = 0; i < E; ++i) {
         const int l = last_pos<L, -1>(t, i);
         const long long k = ((bb * L + l) * (long long)s.Q + q) * s.Hz + kz0 + c;
-        v[i] = freq_clamp<T>(v[i], delta, fedits, k, H);
+        const long long pad = (bb * L + l) * s.Wtot + (long long)q * s.Hzp + kz0 + c;
+        v[i] = freq_project<T>(v[i], ca, fedits, k, pad, H);
       }
     }
     // The inverse's first stage reads the positions the forward's last

@@ -6,6 +6,7 @@
 #include <cmath>
 #include <cstring>
 #include <future>
+#include <limits>
 #include <memory>
 #include <vector>
 
@@ -29,9 +30,14 @@ struct GraphKey {
   double tol = 0, eps = 0, delta = 0;
   cudaStream_t stream = nullptr;
   int profile = 0;
+  int cmode = 0;            // constraint mode (CLAMP_*) and its parameters
+  double delta_ptw = 0;
+  const void *mask = nullptr;
+  int dc = 0;
   bool operator==(const GraphKey &o) const {
     return a == o.a && b == o.b && pro == o.pro && max_iter == o.max_iter && tol == o.tol &&
-           eps == o.eps && delta == o.delta && stream == o.stream && profile == o.profile;
+           eps == o.eps && delta == o.delta && stream == o.stream && profile == o.profile && cmode == o.cmode &&
+           delta_ptw == o.delta_ptw && mask == o.mask && dc == o.dc;
   }
 };
 
@@ -80,7 +86,19 @@ struct ffcz_solver {
   int static_z = 0, static_y = 0, static_x = 0;
   // parameters
   double eps = 0, delta = 0;
-  bool initialized = false;
+  bool initialized = false;  // some initialiser ran (x is on the device)
+  // constraint modes: which initialisers provided their data, and the mode
+  // of the running solve (CLAMP_ABS / CLAMP_DIRECT / CLAMP_PTW)
+  bool abs_ready = false, direct_ready = false, ptw_ready = false;
+  int last_indexed = FFCZ_MODE_DIRECT;  // solve(): direct or partial pointwise
+  int cmode = CLAMP_ABS;
+  double delta_ptw = 0;
+  int ptw_dc = 1;
+  void *d_bound = nullptr;           // direct: H bounds (+inf unconstrained)
+  void *d_orig = nullptr;            // pointwise: spectrum of x (padded)
+  unsigned char *d_mask = nullptr;   // partial pointwise: H flags
+  bool ptw_partial = false;
+  int partial_dc = 0;
   bool extracted = false;
   // graph cache
   cudaGraph_t graph = nullptr;
@@ -277,6 +295,28 @@ int plan_solver(ffcz_solver *s) {
 
 template <typename T> T *tp(void *p) { return (T *)p; }
 
+// Kernel arguments of the running constraint mode; the pointwise constants
+// are computed in T the way projection_algorithm.cu:206-236 does.
+template <typename T>
+ClampArgs<T> clamp_args(const ffcz_solver *s) {
+  ClampArgs<T> ca;
+  ca.mode = s->cmode;
+  ca.delta = (T)s->delta;
+  ca.bound = (const T *)s->d_bound;
+  ca.orig = (const c2<T> *)s->d_orig;
+  if (s->cmode == CLAMP_PTW) {
+    const T d = (T)s->delta_ptw;
+    ca.sp = std::sqrt(T(1) + d);
+    ca.sm = std::sqrt(T(1) - d);
+    ca.lo = T(1) / ca.sp - T(1);
+    ca.hi = T(1) / ca.sm - T(1);
+    ca.cd = std::fmin(T(1) - ca.sm, ca.sp - T(1)) / (T)std::sqrt(2.0f);
+    ca.mask = s->ptw_partial ? s->d_mask : nullptr;
+    ca.dc = s->ptw_dc;
+  }
+  return ca;
+}
+
 // One iteration: [prologue + R2C z] [y fwd] [fused fwd/clamp/inv] [y inv]
 // [C2R z + 1/N + violation] [check].
 template <typename T>
@@ -289,7 +329,8 @@ void launch_iteration(ffcz_solver *s, cudaStream_t st, int pro, const void *a, c
     if (record) cudaEventRecordWithFlags(s->ev[ne++], st, use_graph ? cudaEventRecordExternal : 0);
   };
   mark();
-  const T eps = (T)s->eps, delta = (T)s->delta;
+  const T eps = (T)s->eps;
+  const ClampArgs<T> delta = clamp_args<T>(s);
   const c2<T> *post = (const c2<T> *)s->d_tw + s->post_off;
   c2<T> *spec = (c2<T> *)s->d_spec;
   const T *pa = (const T *)a, *pb = (const T *)b;
@@ -393,6 +434,10 @@ int run_loop_graph(ffcz_solver *s, int pro, const void *a, const void *b, int ma
   key.delta = s->delta;
   key.stream = s->stream;
   key.profile = s->profile;
+  key.cmode = s->cmode;
+  key.delta_ptw = s->delta_ptw;
+  key.mask = s->ptw_partial ? s->d_mask : nullptr;
+  key.dc = s->ptw_dc;
   if (!(s->gexec && s->gkey == key)) {
     if (s->gexec) cudaGraphExecDestroy(s->gexec);
     if (s->graph) cudaGraphDestroy(s->graph);
@@ -517,6 +562,9 @@ void free_all(ffcz_solver *s) {
   for (void *p : bufs)
     if (p) cudaFree(p);
   if (s->d_up_blk) cudaFree(s->d_up_blk);
+  if (s->d_bound) cudaFree(s->d_bound);
+  if (s->d_orig) cudaFree(s->d_orig);
+  if (s->d_mask) cudaFree(s->d_mask);
   if (s->h_ctl) cudaFreeHost(s->h_ctl);
   if (s->cap) cudaStreamDestroy(s->cap);
   for (cudaEvent_t e : s->ev)
@@ -577,7 +625,7 @@ int reconstruct(ffcz_solver *s, const void *d_decomp, const uint16_t *fq, size_t
   c2<T> *spec = (c2<T> *)s->d_spec;
   FFCZ_CUDA(cudaMemsetAsync(s->d_spec, 0, (size_t)s->rows * s->Hzp * 2 * s->es, st));
   if (nf) FFCZ_TRY(unpack_edits<T>(s, fq, nf, fpack, 2 * s->H, fmin, fmax, s->d_fpack, s->fpack_bytes, nullptr, spec));
-  const T delta = (T)s->delta;
+  const ClampArgs<T> delta = clamp_args<T>(s);
   if (s->fused == 2) {
     ((StridedFn<T>)s->kx[MODE_INV])<<<s->lx.grid, s->lx.threads, s->lx.smem, st>>>(spec, s->sx, s->px, delta,
                                                                                    tp<T>(s->d_fedits), H);
@@ -601,6 +649,31 @@ int reconstruct(ffcz_solver *s, const void *d_decomp, const uint16_t *fq, size_t
   FFCZ_CUDA(cudaGetLastError());
   FFCZ_CUDA(cudaStreamSynchronize(st));
   s->extracted = false;
+  return FFCZ_OK;
+}
+
+// R2C of x with the solver's forward passes into d_orig (padded layout), the
+// spectrum the pointwise modes compare against (impl:612-623).
+template <typename T>
+int forward_spectrum(ffcz_solver *s) {
+  cudaStream_t st = s->stream;
+  c2<T> *spec = (c2<T> *)s->d_spec;
+  const c2<T> *post = (const c2<T> *)s->d_tw + s->post_off;
+  const ClampArgs<T> none;
+  const long long H = (long long)s->H;
+  ((ZfwdFn<T>)s->kzf[PRO_PLAIN])<<<s->lz_f.grid, s->lz_f.threads, s->lz_f.smem, st>>>(
+      (const T *)s->d_x, nullptr, tp<T>(s->d_sedits), (T)s->eps, spec, s->za, s->pz, post);
+  if (s->has_y)
+    ((StridedFn<T>)s->ky[MODE_FWD])<<<s->ly.grid, s->ly.threads, s->ly.smem, st>>>(spec, s->sy, s->py, none,
+                                                                                   tp<T>(s->d_fedits), H);
+  if (s->has_x)
+    ((StridedFn<T>)s->kx[MODE_FWD])<<<s->lx.grid, s->lx.threads, s->lx.smem, st>>>(spec, s->sx, s->px, none,
+                                                                                   tp<T>(s->d_fedits), H);
+  const size_t bytes = (size_t)s->rows * s->Hzp * 2 * s->es;
+  if (!s->d_orig) FFCZ_CUDA(cudaMalloc(&s->d_orig, bytes));
+  FFCZ_CUDA(cudaMemcpyAsync(s->d_orig, s->d_spec, bytes, cudaMemcpyDeviceToDevice, st));
+  FFCZ_CUDA(cudaGetLastError());
+  FFCZ_CUDA(cudaStreamSynchronize(st));
   return FFCZ_OK;
 }
 
@@ -710,17 +783,68 @@ int ffcz_solver_set_pack_mode(ffcz_solver *s, int mode) {
   return FFCZ_OK;
 }
 
-static int init_common(ffcz_solver *s, const void *src, cudaMemcpyKind kind, double eps, double delta) {
+static double round_t(const ffcz_solver *s, double v) { return s->dtype == FFCZ_F32 ? (double)(float)v : v; }
+
+// Copies x and stores eps rounded to the solver type (the reference's T
+// parameters, impl:604, 640-646, 675, 706).
+static int init_x(ffcz_solver *s, const void *src, cudaMemcpyKind kind, double eps) {
   FFCZ_TRY(check_solver(s));
   if (!src) return fail(FFCZ_ERR_INVALID, "original data is NULL");
-  // eps / delta are stored rounded to the solver type (the reference's T
-  // parameters, impl:640-646).
-  s->eps = s->dtype == FFCZ_F32 ? (double)(float)eps : eps;
-  s->delta = s->dtype == FFCZ_F32 ? (double)(float)delta : delta;
+  s->eps = round_t(s, eps);
   FFCZ_CUDA(cudaMemcpyAsync(s->d_x, src, s->N * s->es, kind, s->stream));
   FFCZ_CUDA(cudaStreamSynchronize(s->stream));
   s->initialized = true;
   return FFCZ_OK;
+}
+
+static int init_common(ffcz_solver *s, const void *src, cudaMemcpyKind kind, double eps, double delta) {
+  FFCZ_TRY(init_x(s, src, kind, eps));
+  s->delta = round_t(s, delta);
+  s->abs_ready = true;
+  return FFCZ_OK;
+}
+
+static int init_ptw(ffcz_solver *s, const void *src, cudaMemcpyKind kind, double eps, double delta_ptw) {
+  FFCZ_TRY(init_x(s, src, kind, eps));
+  s->delta_ptw = round_t(s, delta_ptw);
+  FFCZ_TRY(DISPATCH(s, forward_spectrum, s));
+  s->ptw_ready = true;
+  return FFCZ_OK;
+}
+
+static int check_indices(ffcz_solver *s, const size_t *idx, size_t num) {
+  if (num && !idx) return fail(FFCZ_ERR_INVALID, "frequency indices are NULL");
+  for (size_t c = 0; c < num; ++c)
+    if (idx[c] >= s->H) return fail(FFCZ_ERR_INVALID, "frequency index " + std::to_string(idx[c]) + " >= H");
+  return FFCZ_OK;
+}
+
+// Runs the loop with constraint mode `mode` (FFCZ_MODE_*) and, with
+// extract, the compaction.
+static int solve_mode(ffcz_solver *s, int mode, int pro, const void *a, const void *b, int max_iter, double tol,
+                      bool extract_after) {
+  FFCZ_TRY(check_solver(s));
+  const bool ready = mode == FFCZ_MODE_ALL_ABS ? s->abs_ready
+                   : mode == FFCZ_MODE_DIRECT ? s->direct_ready
+                   : mode == FFCZ_MODE_ALL_PTW ? s->ptw_ready
+                   : mode == FFCZ_MODE_PARTIAL_PTW ? (s->ptw_ready && s->d_mask != nullptr)
+                   : false;
+  if (mode < FFCZ_MODE_ALL_ABS || mode > FFCZ_MODE_PARTIAL_PTW) return fail(FFCZ_ERR_INVALID, "unknown mode");
+  if (!ready) return fail(FFCZ_ERR_NOT_INITIALIZED, "Solver not initialized");
+  s->cmode = mode == FFCZ_MODE_ALL_ABS ? CLAMP_ABS : mode == FFCZ_MODE_DIRECT ? CLAMP_DIRECT : CLAMP_PTW;
+  s->ptw_partial = mode == FFCZ_MODE_PARTIAL_PTW;
+  s->ptw_dc = s->ptw_partial ? s->partial_dc : 1;
+  FFCZ_TRY(DISPATCH(s, project, s, pro, a, b, max_iter, tol));
+  return extract_after ? DISPATCH(s, extract, s) : FFCZ_OK;
+}
+
+static int solve_host(ffcz_solver *s, int mode, const void *h_err, int max_iter, double tol) {
+  FFCZ_TRY(check_solver(s));
+  if (!h_err) return fail(FFCZ_ERR_INVALID, "initial error is NULL");
+  if (!s->initialized) return fail(FFCZ_ERR_NOT_INITIALIZED, "Solver not initialized");
+  // e0 is staged in the e buffer (impl:830-831); the first pass reads it.
+  FFCZ_CUDA(cudaMemcpyAsync(s->d_e, h_err, s->N * s->es, cudaMemcpyHostToDevice, s->stream));
+  return solve_mode(s, mode, PRO_PLAIN, s->d_e, nullptr, max_iter, tol, true);
 }
 
 int ffcz_init_all_abs(ffcz_solver *s, const void *h_orig, double eps, double delta) {
@@ -730,15 +854,62 @@ int ffcz_init_all_abs_device(ffcz_solver *s, const void *d_orig, double eps, dou
   return init_common(s, d_orig, cudaMemcpyDeviceToDevice, eps, delta);
 }
 
+int ffcz_init_direct(ffcz_solver *s, const void *h_orig, const size_t *h_freq_indices, const void *h_delta_k,
+                     double eps, size_t num_constraints) {
+  FFCZ_TRY(check_solver(s));
+  FFCZ_TRY(check_indices(s, h_freq_indices, num_constraints));
+  if (num_constraints && !h_delta_k) return fail(FFCZ_ERR_INVALID, "delta_k is NULL");
+  FFCZ_TRY(init_x(s, h_orig, cudaMemcpyHostToDevice, eps));
+  if (!s->d_bound) FFCZ_CUDA(cudaMalloc(&s->d_bound, s->H * s->es));
+  if (s->dtype == FFCZ_F32) {
+    std::vector<float> b(s->H, std::numeric_limits<float>::infinity());
+    for (size_t c = 0; c < num_constraints; ++c)
+      b[h_freq_indices[c]] = std::min(b[h_freq_indices[c]], ((const float *)h_delta_k)[c]);
+    FFCZ_CUDA(cudaMemcpy(s->d_bound, b.data(), s->H * 4, cudaMemcpyHostToDevice));
+  } else {
+    std::vector<double> b(s->H, std::numeric_limits<double>::infinity());
+    for (size_t c = 0; c < num_constraints; ++c)
+      b[h_freq_indices[c]] = std::min(b[h_freq_indices[c]], ((const double *)h_delta_k)[c]);
+    FFCZ_CUDA(cudaMemcpy(s->d_bound, b.data(), s->H * 8, cudaMemcpyHostToDevice));
+  }
+  s->direct_ready = true;
+  s->last_indexed = FFCZ_MODE_DIRECT;
+  return FFCZ_OK;
+}
+
+int ffcz_init_all_ptw(ffcz_solver *s, const void *h_orig, double eps, double delta_ptw) {
+  return init_ptw(s, h_orig, cudaMemcpyHostToDevice, eps, delta_ptw);
+}
+int ffcz_init_all_ptw_device(ffcz_solver *s, const void *d_orig, double eps, double delta_ptw) {
+  return init_ptw(s, d_orig, cudaMemcpyDeviceToDevice, eps, delta_ptw);
+}
+
+int ffcz_init_partial_ptw(ffcz_solver *s, const void *h_orig, const size_t *h_freq_indices, double delta_ptw,
+                          double eps, size_t num_constraints) {
+  FFCZ_TRY(check_solver(s));
+  FFCZ_TRY(check_indices(s, h_freq_indices, num_constraints));
+  FFCZ_TRY(init_ptw(s, h_orig, cudaMemcpyHostToDevice, eps, delta_ptw));
+  // constraint 0 is the DC rule whatever index it names (projection_algorithm.cu:
+  // 276-289); the pointwise rule covers the others.
+  std::vector<unsigned char> m(s->H, 0);
+  for (size_t c = 1; c < num_constraints; ++c) m[h_freq_indices[c]] = 1;
+  if (!s->d_mask) FFCZ_CUDA(cudaMalloc(&s->d_mask, s->H));
+  FFCZ_CUDA(cudaMemcpy(s->d_mask, m.data(), s->H, cudaMemcpyHostToDevice));
+  s->partial_dc = num_constraints > 0 ? 1 : 0;
+  s->last_indexed = FFCZ_MODE_PARTIAL_PTW;
+  return FFCZ_OK;
+}
+
 int ffcz_project_all_abs_device(ffcz_solver *s, const void *d_err, int max_iter, double tol) {
   FFCZ_TRY(check_solver(s));
   FFCZ_TRY(check_dev_ptr(d_err, "initial error"));
-  return DISPATCH(s, project, s, PRO_PLAIN, d_err, nullptr, max_iter, tol);
+  return solve_mode(s, FFCZ_MODE_ALL_ABS, PRO_PLAIN, d_err, nullptr, max_iter, tol, false);
 }
 
 int ffcz_solve_all_abs_device(ffcz_solver *s, const void *d_err, int max_iter, double tol) {
-  FFCZ_TRY(ffcz_project_all_abs_device(s, d_err, max_iter, tol));
-  return DISPATCH(s, extract, s);
+  FFCZ_TRY(check_solver(s));
+  FFCZ_TRY(check_dev_ptr(d_err, "initial error"));
+  return solve_mode(s, FFCZ_MODE_ALL_ABS, PRO_PLAIN, d_err, nullptr, max_iter, tol, true);
 }
 
 int ffcz_solve_all_abs_pair_device(ffcz_solver *s, const void *d_orig, const void *d_decomp, int max_iter,
@@ -746,18 +917,26 @@ int ffcz_solve_all_abs_pair_device(ffcz_solver *s, const void *d_orig, const voi
   FFCZ_TRY(check_solver(s));
   FFCZ_TRY(check_dev_ptr(d_orig, "original data"));
   FFCZ_TRY(check_dev_ptr(d_decomp, "decompressed data"));
-  FFCZ_TRY(DISPATCH(s, project, s, PRO_DIFF, d_decomp, d_orig, max_iter, tol));
-  return DISPATCH(s, extract, s);
+  return solve_mode(s, FFCZ_MODE_ALL_ABS, PRO_DIFF, d_decomp, d_orig, max_iter, tol, true);
 }
 
 int ffcz_solve_all_abs(ffcz_solver *s, const void *h_err, int max_iter, double tol) {
+  return solve_host(s, FFCZ_MODE_ALL_ABS, h_err, max_iter, tol);
+}
+
+int ffcz_solve(ffcz_solver *s, const void *h_err, int max_iter, double tol) {
   FFCZ_TRY(check_solver(s));
-  if (!h_err) return fail(FFCZ_ERR_INVALID, "initial error is NULL");
-  if (!s->initialized) return fail(FFCZ_ERR_NOT_INITIALIZED, "Solver not initialized");
-  // e0 is staged in the e buffer (impl:830-831); the first pass reads it.
-  FFCZ_CUDA(cudaMemcpyAsync(s->d_e, h_err, s->N * s->es, cudaMemcpyHostToDevice, s->stream));
-  FFCZ_TRY(DISPATCH(s, project, s, PRO_PLAIN, s->d_e, nullptr, max_iter, tol));
-  return DISPATCH(s, extract, s);
+  return solve_host(s, s->last_indexed, h_err, max_iter, tol);
+}
+
+int ffcz_solve_all_ptw(ffcz_solver *s, const void *h_err, int max_iter, double tol) {
+  return solve_host(s, FFCZ_MODE_ALL_PTW, h_err, max_iter, tol);
+}
+
+int ffcz_solve_mode_device(ffcz_solver *s, int mode, const void *d_err, int max_iter, double tol) {
+  FFCZ_TRY(check_solver(s));
+  FFCZ_TRY(check_dev_ptr(d_err, "initial error"));
+  return solve_mode(s, mode, PRO_PLAIN, d_err, nullptr, max_iter, tol, true);
 }
 
 int ffcz_extract(ffcz_solver *s) {
@@ -901,10 +1080,23 @@ int ffcz_get_device_array(ffcz_solver *s, int which, void **dptr, size_t *bytes)
     case 6: p = s->d_spack; b = (N + 7) / 8; break;
     case 7: p = s->d_fcompact; b = cf * es; break;
     case 8: p = s->d_scompact; b = cs * es; break;
+    case 9: p = s->d_orig; b = s->d_orig ? (size_t)s->rows * s->Hzp * 2 * es : 0; break;
     default: return fail(FFCZ_ERR_INVALID, "unknown array");
   }
   *dptr = p;
   if (bytes) *bytes = b;
+  return FFCZ_OK;
+}
+
+int ffcz_get_orig_spectrum(ffcz_solver *s, void *h_dst, size_t cap_complex) {
+  FFCZ_TRY(check_solver(s));
+  if (!s->d_orig) return fail(FFCZ_ERR_NOT_INITIALIZED, "no spectrum of x: initialize a pointwise mode first");
+  if (!h_dst) return fail(FFCZ_ERR_INVALID, "destination is NULL");
+  if (cap_complex < s->H) return fail(FFCZ_ERR_CAPACITY, "destination too small");
+  const size_t ce = 2 * s->es;
+  FFCZ_CUDA(cudaMemcpy2DAsync(h_dst, (size_t)s->Hz * ce, s->d_orig, (size_t)s->Hzp * ce, (size_t)s->Hz * ce,
+                              (size_t)s->rows, cudaMemcpyDeviceToHost, s->stream));
+  FFCZ_CUDA(cudaStreamSynchronize(s->stream));
   return FFCZ_OK;
 }
 
@@ -1180,8 +1372,9 @@ int ffcz_batch_solve_pair_device(ffcz_batch *b, const void *const *d_orig, const
   if (!d_orig || !d_decomp) return fail(FFCZ_ERR_INVALID, "field pointer arrays are NULL");
   const size_t nf = b->f.size();
   for (size_t i = 0; i < nf; ++i) {
-    if (!b->f[i]->initialized)
+    if (!b->f[i]->abs_ready)
       return fail(FFCZ_ERR_NOT_INITIALIZED, "Solver not initialized (field " + std::to_string(i) + ")");
+    b->f[i]->cmode = CLAMP_ABS;
     FFCZ_TRY(check_dev_ptr(d_orig[i], "original data"));
     FFCZ_TRY(check_dev_ptr(d_decomp[i], "decompressed data"));
   }

@@ -14,7 +14,7 @@ using ZfwdFn = void (*)(const T *, const T *, T *, T, c2<T> *, ZArgs, AxisPlan, 
 template <typename T>
 using ZinvFn = void (*)(const c2<T> *, T *, T, T, LoopCtl *, ZArgs, AxisPlan, const c2<T> *);
 template <typename T>
-using StridedFn = void (*)(c2<T> *, SArgs, AxisPlan, T, T *, long long);
+using StridedFn = void (*)(c2<T> *, SArgs, AxisPlan, ClampArgs<T>, T *, long long);
 
 struct StaticGeom {
   int TW = 0;        // tile width (columns or rows)

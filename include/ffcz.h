@@ -112,6 +112,43 @@ int ffcz_solve_all_abs_device(ffcz_solver *s, const void *d_err,
 int ffcz_solve_all_abs_pair_device(ffcz_solver *s, const void *d_orig,
                                    const void *d_decomp, int max_iter,
                                    double tol);
+/* ---- the other constraint modes (impl:598-637, 670-738, 772-814,
+ * 860-902; kernels projection_algorithm.cu:93-145, 191-333) ---------------- */
+#define FFCZ_MODE_ALL_ABS     0  /* every coefficient within +-delta       */
+#define FFCZ_MODE_DIRECT      1  /* listed coefficients within +-delta_k   */
+#define FFCZ_MODE_ALL_PTW     2  /* pointwise power-spectrum box, all k    */
+#define FFCZ_MODE_PARTIAL_PTW 3  /* the same on listed coefficients        */
+/* initialize(h_orig, h_freq_indices, h_delta_k, eps, num) -- impl:598-637.
+ * h_delta_k: num values of the solver's dtype.  Indices must be < H; an
+ * index listed twice keeps its smaller bound (the reference races there). */
+int ffcz_init_direct(ffcz_solver *s, const void *h_orig,
+                     const size_t *h_freq_indices, const void *h_delta_k,
+                     double eps, size_t num_constraints);
+/* initialize_all_ptw(h_orig, eps, delta_ptw) -- impl:670-697: also the
+ * spectrum of x the pointwise box compares against. */
+int ffcz_init_all_ptw(ffcz_solver *s, const void *h_orig, double eps,
+                      double delta_ptw);
+int ffcz_init_all_ptw_device(ffcz_solver *s, const void *d_orig, double eps,
+                             double delta_ptw);
+/* initialize_partial_ptw(h_orig, h_freq_indices, delta_ptw, eps, num) --
+ * impl:699-738.  As in projection_algorithm.cu:276-289, constraint 0 is the
+ * DC rule whatever index it lists; constraints 1.. get the pointwise box. */
+int ffcz_init_partial_ptw(ffcz_solver *s, const void *h_orig,
+                          const size_t *h_freq_indices, double delta_ptw,
+                          double eps, size_t num_constraints);
+/* solve(h_err, max_iter, tol) -- impl:772-814: the direct mode, or the
+ * partial pointwise mode when initialize_partial_ptw ran last of the two
+ * (the reference's solve() reads the direct mode's bounds in that case,
+ * which initialize_partial_ptw never sets). */
+int ffcz_solve(ffcz_solver *s, const void *h_err, int max_iter, double tol);
+/* solve_all_ptw(h_err, max_iter, tol) -- impl:860-902. */
+int ffcz_solve_all_ptw(ffcz_solver *s, const void *h_err, int max_iter,
+                       double tol);
+/* Any mode with e0 resident on the device (FFCZ_ERR_NOT_INITIALIZED when
+ * the mode's initialiser did not run). */
+int ffcz_solve_mode_device(ffcz_solver *s, int mode, const void *d_err,
+                           int max_iter, double tol);
+
 /* Projection loop only, without the compaction (impl:835-852). */
 int ffcz_project_all_abs_device(ffcz_solver *s, const void *d_err,
                                 int max_iter, double tol);
@@ -158,9 +195,15 @@ int ffcz_get_spatial_flags(ffcz_solver *s, uint8_t *dst, size_t cap,
                            size_t *len);
 /* Device pointers of the solver-owned arrays (for zero-copy callers):
  * which = 0 e, 1 freq_edits, 2 spatial_edits, 3 freq quant, 4 spatial
- * quant, 5 freq pack, 6 spatial pack, 7 freq compact, 8 spatial compact. */
+ * quant, 5 freq pack, 6 spatial pack, 7 freq compact, 8 spatial compact,
+ * 9 spectrum of x of the pointwise modes (Nx*Ny rows of pitch Hzp complex
+ * values, Hzp = Nz/2+1 rounded up to 128 bytes; 0 bytes before an
+ * initialize_*_ptw). */
 int ffcz_get_device_array(ffcz_solver *s, int which, void **dptr,
                           size_t *bytes);
+/* The spectrum of x of the pointwise modes (d_orig_freq, impl:612-623):
+ * H interleaved complex values of the solver's dtype. */
+int ffcz_get_orig_spectrum(ffcz_solver *s, void *h_dst, size_t cap_complex);
 /* Sizes: n = Nx*Ny*Nz, h = Nx*Ny*(Nz/2+1). */
 int ffcz_get_sizes(ffcz_solver *s, size_t *n, size_t *h);
 /* Kernel launches issued since the last solve started (projection loop,

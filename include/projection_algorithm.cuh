@@ -221,28 +221,39 @@ class ProjectionSolver {
   ProjectionSolver(const ProjectionSolver &) = delete;
   ProjectionSolver &operator=(const ProjectionSolver &) = delete;
 
-  // Per-index bounds (impl:598-637) and the power-spectrum modes (impl:670-
-  // 738) are not implemented by the GB300 library: they throw.
-  void initialize(const T *, const size_t *, const T *, T, size_t) {
-    throw std::runtime_error("ProjectionSolver::initialize (per-index bounds) is not supported");
+  // initialize -- impl:598-637 (per-index bounds delta_k)
+  void initialize(const T *h_orig_data, const size_t *h_freq_indices, const T *h_delta_k, T spatial_epsilon,
+                  size_t num_freq_constraints) {
+    ffcz_detail::check(ffcz_init_direct(h_, h_orig_data, h_freq_indices, h_delta_k, (double)spatial_epsilon,
+                                        num_freq_constraints));
   }
   void initialize_all_abs(const T *h_orig_data, T spatial_epsilon, T delta) {
     ffcz_detail::check(ffcz_init_all_abs(h_, h_orig_data, (double)spatial_epsilon, (double)delta));
   }
-  void initialize_all_ptw(const T *, T, T) {
-    throw std::runtime_error("ProjectionSolver::initialize_all_ptw is not supported");
+  // initialize_all_ptw -- impl:670-697 (pointwise power-spectrum box)
+  void initialize_all_ptw(const T *h_orig_data, T spatial_epsilon, T delta_ptw) {
+    ffcz_detail::check(ffcz_init_all_ptw(h_, h_orig_data, (double)spatial_epsilon, (double)delta_ptw));
   }
-  void initialize_partial_ptw(const T *, const size_t *, const T, T, size_t) {
-    throw std::runtime_error("ProjectionSolver::initialize_partial_ptw is not supported");
+  // initialize_partial_ptw -- impl:699-738
+  void initialize_partial_ptw(const T *h_orig_data, const size_t *h_freq_indices, const T delta_ptw,
+                              T spatial_epsilon, size_t num_freq_constraints) {
+    ffcz_detail::check(ffcz_init_partial_ptw(h_, h_orig_data, h_freq_indices, (double)delta_ptw,
+                                             (double)spatial_epsilon, num_freq_constraints));
   }
-  void solve(T *, int, T) { throw std::runtime_error("ProjectionSolver::solve (per-index bounds) is not supported"); }
+  // solve -- impl:772-814
+  void solve(T *h_spatial_error, int max_iterations, T convergence_tolerance) {
+    ffcz_detail::check(ffcz_solve(h_, h_spatial_error, max_iterations, (double)convergence_tolerance));
+    print_iterations_();
+  }
   void solve_all_abs(T *h_spatial_error, int max_iterations, T convergence_tolerance) {
     ffcz_detail::check(ffcz_solve_all_abs(h_, h_spatial_error, max_iterations, (double)convergence_tolerance));
-    int it = 0;
-    ffcz_get_iterations(h_, &it);
-    printf("Total number of iterations: %d\n", it);
+    print_iterations_();
   }
-  void solve_all_ptw(T *, int, T) { throw std::runtime_error("ProjectionSolver::solve_all_ptw is not supported"); }
+  // solve_all_ptw -- impl:860-902
+  void solve_all_ptw(T *h_spatial_error, int max_iterations, T convergence_tolerance) {
+    ffcz_detail::check(ffcz_solve_all_ptw(h_, h_spatial_error, max_iterations, (double)convergence_tolerance));
+    print_iterations_();
+  }
 
   void get_results(T *h_spatial_error) { ffcz_detail::check(ffcz_get_results(h_, h_spatial_error)); }
 
@@ -284,6 +295,11 @@ class ProjectionSolver {
   size_t Nx_, Ny_, Nz_;
 
   size_t freq_size_() const { return Nx_ * Ny_ * (Nz_ / 2 + 1); }
+  void print_iterations_() {
+    int it = 0;
+    ffcz_get_iterations(h_, &it);
+    printf("Total number of iterations: %d\n", it);
+  }
   double minmax_(int i) {
     double v[4] = {0, 0, 0, 0};
     ffcz_detail::check(ffcz_get_minmax(h_, &v[0], &v[1], &v[2], &v[3]));

@@ -100,14 +100,17 @@ def _ptr(a: np.ndarray) -> int:
 
 
 # --------------------------------------------------------------- projection
-def solve_all_abs(e0: np.ndarray, shape, eps: float, delta: float, max_iter: int = 100, tol: float = 1e-7,
-                  dtype=np.float32) -> dict:
-    """Alternating projections of projection_algorithm_impl.cuh:816-858."""
+def _loop(e0, shape, eps, max_iter, tol, dtype, clamp):
+    """The alternating-projection loop shared by every solve of
+    projection_algorithm_impl.cuh:772-902: R2C, clamp(re, im, freq_edits)
+    (in place on the half spectrum's real and imaginary parts, flat index
+    order), C2R * T(1)/T(N), violation, stop when it is below tol, spatial
+    clamp."""
     T = np.dtype(dtype).type
     shape = tuple(int(s) for s in shape)
     N = int(np.prod(shape))
     H = shape[0] * shape[1] * (shape[2] // 2 + 1)
-    eps, delta, tol = T(eps), T(delta), T(tol)
+    eps, tol = T(eps), T(tol)
     factor = T(1) / T(N)
     e = np.array(e0, dtype=T).reshape(shape)
     fed = np.zeros(2 * H, T)
@@ -121,14 +124,7 @@ def solve_all_abs(e0: np.ndarray, shape, eps: float, delta: float, max_iter: int
         fshape = F.shape
         re = np.ascontiguousarray(F.real).reshape(-1)
         im = np.ascontiguousarray(F.imag).reshape(-1)
-        for part, off in ((re, 0), (im, H)):
-            hi = part > delta
-            lo = part < -delta
-            view = fed[off:off + H]
-            view[hi] += delta - part[hi]
-            part[hi] = delta
-            view[lo] += -delta - part[lo]
-            part[lo] = -delta
+        clamp(re, im, fed)
         G = (re.astype(np.float64) + 1j * im.astype(np.float64)).reshape(fshape)
         e = (_irfftn(G, s=shape) * N).astype(T) * factor
         a = np.abs(e)
@@ -146,6 +142,107 @@ def solve_all_abs(e0: np.ndarray, shape, eps: float, delta: float, max_iter: int
         flat[lo] = -eps
     return {"e": e, "freq_edits": fed, "spatial_edits": sed, "iterations": it, "metric": float(viol),
             "converged": converged}
+
+
+def _box(part, bound, view):
+    """Re or Im clamp of projection_algorithm.cu:160-187 with a per-entry
+    bound (scalar or array): above -> bound, below -bound -> -bound, the
+    difference accumulated into view."""
+    hi = part > bound
+    lo = (part < -bound) & ~hi
+    b = np.broadcast_to(bound, part.shape)
+    view[hi] += b[hi] - part[hi]
+    part[hi] = b[hi]
+    view[lo] += -b[lo] - part[lo]
+    part[lo] = -b[lo]
+
+
+def solve_all_abs(e0: np.ndarray, shape, eps: float, delta: float, max_iter: int = 100, tol: float = 1e-7,
+                  dtype=np.float32) -> dict:
+    """Alternating projections of projection_algorithm_impl.cuh:816-858."""
+    T = np.dtype(dtype).type
+    d = T(delta)
+
+    def clamp(re, im, fed):
+        H = re.size
+        _box(re, d, fed[:H])
+        _box(im, d, fed[H:])
+
+    return _loop(e0, shape, eps, max_iter, tol, dtype, clamp)
+
+
+def direct_bounds(shape, indices, delta_k, dtype=np.float32) -> np.ndarray:
+    """Per-coefficient bounds of the direct mode (initialize, impl:598-637):
+    +inf where unconstrained; an index listed twice keeps the smaller bound."""
+    T = np.dtype(dtype).type
+    H = shape[0] * shape[1] * (shape[2] // 2 + 1)
+    b = np.full(H, np.inf, T)
+    np.minimum.at(b, np.asarray(indices, np.int64), np.asarray(delta_k, T))
+    return b
+
+
+def solve_direct(e0, shape, eps, bounds, max_iter=100, tol=1e-7, dtype=np.float32) -> dict:
+    """solve() with project_frequency_constraints_direct
+    (projection_algorithm.cu:93-145): Re and Im of coefficient k clamped to
+    +-bounds[k]."""
+    b = np.asarray(bounds, np.dtype(dtype))
+
+    def clamp(re, im, fed):
+        H = re.size
+        _box(re, b, fed[:H])
+        _box(im, b, fed[H:])
+
+    return _loop(e0, shape, eps, max_iter, tol, dtype, clamp)
+
+
+def ptw_constants(delta_ptw, dtype=np.float32) -> dict:
+    """The T constants of projection_algorithm.cu:191-333: sqrt(1 +- d), the
+    DC factors 1/sqrt(1 +- d) - 1 and the clamp half-width
+    min(1 - sqrt(1-d), sqrt(1+d) - 1) / sqrtf(2) (sqrt(2) rounded to float, as
+    sqrt_val(2.0f) gives)."""
+    T = np.dtype(dtype).type
+    d = T(delta_ptw)
+    sp, sm = np.sqrt(T(1) + d), np.sqrt(T(1) - d)
+    return {"sp": sp, "sm": sm, "lo": T(1) / sp - T(1), "hi": T(1) / sm - T(1),
+            "cd": T(min(T(1) - sm, sp - T(1)) / T(np.sqrt(np.float32(2.0))))}
+
+
+def solve_ptw(e0, shape, eps, delta_ptw, orig, mask=None, dc=True, max_iter=100, tol=1e-7,
+              dtype=np.float32) -> dict:
+    """solve_all_ptw (mask None) and the partial form (mask: coefficients
+    listed after the first constraint) of projection_algorithm.cu:191-333.
+    orig: the half spectrum of x (complex, flat index order).  Coefficient 0
+    (when dc): Re error outside [orig0.re*(1/sqrt(1+d)-1), orig0.re*(1/sqrt(1-d)-1)]
+    is set to 0.  Others: if |orig+err|^2/|orig|^2 lies outside [sqrt(1-d),
+    sqrt(1+d)], Re and Im of the error are clamped to +-cd."""
+    T = np.dtype(dtype).type
+    c = ptw_constants(delta_ptw, dtype)
+    o = np.asarray(orig).reshape(-1)
+    ore, oim = o.real.astype(T), o.imag.astype(T)
+    om = ore * ore + oim * oim
+    sel = np.ones(o.size, bool) if mask is None else np.asarray(mask, bool).copy()
+    sel[0] = False
+
+    def clamp(re, im, fed):
+        H = re.size
+        if dc:
+            lo, hi = ore[0] * c["lo"], ore[0] * c["hi"]
+            if re[0] > hi or re[0] < lo:
+                fed[0] += -re[0]
+                re[0] = T(0)
+        cx, cy = ore + re, oim + im
+        with np.errstate(divide="ignore", invalid="ignore"):
+            ratio = (cx * cx + cy * cy) / om
+        inside = (ratio <= c["sp"]) & (ratio >= c["sm"])
+        act = sel & ~inside
+        r_act, i_act = re[act], im[act]
+        fr, fi = fed[:H][act], fed[H:][act]
+        _box(r_act, c["cd"], fr)
+        _box(i_act, c["cd"], fi)
+        re[act], im[act] = r_act, i_act
+        fed[:H][act], fed[H:][act] = fr, fi
+
+    return _loop(e0, shape, eps, max_iter, tol, dtype, clamp)
 
 
 def check_bounds(x: np.ndarray, xhat: np.ndarray, eps: float, delta: float) -> dict:
