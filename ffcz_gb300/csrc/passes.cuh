@@ -386,7 +386,10 @@ __global__ void __launch_bounds__(sizeof(T) == 4 ? 512 : 256) k_strided(c2<T> *_
       const int c = it & (TW - 1);
       if (c < ncol) {
         const long long k = ((bb * s.L + l) * (long long)s.Q + q) * s.Hz + kz0 + c;
-        buf[l * P + c] = freq_project<T>(buf[l * P + c], ca, fedits, k, base + (long long)l * s.Wtot + c, H);
+        if (ca.mode == CLAMP_ABS)
+          buf[l * P + c] = freq_clamp<T>(buf[l * P + c], ca.delta, fedits, k, H);
+        else
+          buf[l * P + c] = freq_project<T>(buf[l * P + c], ca, fedits, k, base + (long long)l * s.Wtot + c, H);
       }
     }
     __syncthreads();

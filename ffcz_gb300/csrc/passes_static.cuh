@@ -61,7 +61,12 @@ __host__ __device__ constexpr int mx_r(int L, int s) { return (int)((mx_list(L) 
 // then one radix 4 or 2 stage for the remainder.
 __host__ __device__ constexpr int rp_nst(int L, int cap = 16) {
   return mx_list(L) ? mx_nst(L)
-       : cap == 8 ? (ilog2(L) / 3 + (ilog2(L) % 3 ? 1 : 0)) : (L == 16 ? 1 : (L <= 256 ? 2 : 3));
+       : cap == 8 ? (ilog2(L) / 3 + (ilog2(L) % 3 ? 1 : 0))
+#ifdef FFCZ_L256_R8
+       : (L == 16 ? 1 : (L < 256 ? 2 : 3));
+#else
+       : (L == 16 ? 1 : (L <= 256 ? 2 : 3));
+#endif
 }
 __host__ __device__ constexpr int rp_radix(int L, int s, int cap = 16) {
   return mx_list(L) ? mx_r(L, s)
@@ -70,14 +75,22 @@ __host__ __device__ constexpr int rp_radix(int L, int s, int cap = 16) {
        : L == 32 ? (s == 0 ? 8 : 4)
        : L == 64 ? 8
        : L == 128 ? (s == 0 ? 16 : 8)
+#ifdef FFCZ_L256_R8
+       : L == 256 ? (s < 2 ? 8 : 4)
+#else
        : L == 256 ? 16
+#endif
        : L == 512 ? 8
        : L == 1024 ? (s == 0 ? 16 : 8)
        : L == 2048 ? (s < 2 ? 16 : 8)
        : 16;
 }
 __host__ __device__ constexpr int rp_elems(int L, int cap = 16) {
+#ifdef FFCZ_L256_R8
+  return mx_list(L) ? mx_E(L) : cap == 8 ? 8 : ((L == 32 || L == 64 || L == 256 || L == 512) ? 8 : 16);
+#else
   return mx_list(L) ? mx_E(L) : cap == 8 ? 8 : ((L == 32 || L == 64 || L == 512) ? 8 : 16);
+#endif
 }
 // radix of stage s in direction DIR (inverse = reversed list)
 __host__ __device__ constexpr int rp_rad(int L, int dir, int s, int cap = 16) {
@@ -317,11 +330,17 @@ __device__ __forceinline__ int first_pos(int t, int i) {
 }
 
 // Resident blocks the FP32 strided tiles are compiled for: three for the
-// 256-thread radix-16 tiles (35 KB tiles, 24 warps resident); others: one
-// (two blocks of the 30-value lists would cap them at 128 registers, and
-// their spills cost more than the occupancy gains: 63 vs 48 us at 1800).
+// 256-thread radix-16 tiles (35 KB tiles, 24 warps resident), two for tiles
+// of 384+ threads with at most 12 values per thread (the 512-thread L = 512
+// tile at 71 registers would otherwise fit once per SM: 647 vs 460 us for
+// the fused pass at 512^3); others: one (two blocks of the 30-value lists
+// would cap them at 128 registers, and their spills cost more than the
+// occupancy gains: 63 vs 48 us at 1800).
+#ifndef FFCZ_MINB16
+#define FFCZ_MINB16 3
+#endif
 __host__ __device__ constexpr int strided_minb(int es, int nt, int E) {
-  return (es == 4 && nt == 256 && E == 16) ? 3 : 1;
+  return (es == 4 && nt == 256 && E == 16) ? FFCZ_MINB16 : (es == 4 && nt >= 384 && E <= 12) ? 2 : 1;
 }
 
 // ---------------------------------------------------------------------------
@@ -355,7 +374,16 @@ __global__ void __launch_bounds__((L / rp_elems(L)) << LGTW,
     v[i] = live ? src[(long long)first_pos<L, D0>(t, i) * s.Wtot] : mkc<T>(T(0), T(0));
   RRun<T, D0, L, LY, 0>::run(v, buf, t, c, p);
   if (MODE == MODE_FCI) {
-    if (live) {
+    if (live && ca.mode == CLAMP_ABS) {
+#pragma unroll
+      for (int i = 0; i < E; ++i) {
+        const int l = last_pos<L, -1>(t, i);
+        const long long k = ((bb * L + l) * (long long)s.Q + q) * s.Hz + kz0 + c;
+        v[i] = freq_clamp<T>(v[i], ca.delta, fedits, k, H);
+      }
+    } else if (live) {
+      // the other modes apart from the all-abs loop, which stays as tight as a
+      // plain clamp
 #pragma unroll
       for (int i = 0; i < E; ++i) {
         const int l = last_pos<L, -1>(t, i);
