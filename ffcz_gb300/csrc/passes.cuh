@@ -24,7 +24,10 @@
 namespace ffcz {
 
 enum { PRO_PLAIN = 0, PRO_DIFF = 1, PRO_CLAMP = 2 };
-enum { MODE_FWD = 0, MODE_INV = 1, MODE_FCI = 2 };
+// MODE_FCI: fused forward / all-abs clamp / inverse; MODE_FCIX: the same
+// with the other constraint modes (a kernel of its own, so that the all-abs
+// kernel keeps the code and registers of a plain clamp).
+enum { MODE_FWD = 0, MODE_INV = 1, MODE_FCI = 2, MODE_FCIX = 3 };
 
 struct ZArgs {
   long long rows;  // Nx*Ny
@@ -380,13 +383,13 @@ __global__ void __launch_bounds__(sizeof(T) == 4 ? 512 : 256) k_strided(c2<T> *_
   } else {
     fft_tile<T, -1, EPT>(buf, p, P, lg, tid, nthr);
   }
-  if (MODE == MODE_FCI) {
+  if (MODE == MODE_FCI || MODE == MODE_FCIX) {
     for (int it = tid; it < total; it += nthr) {
       const int l = it >> lg;
       const int c = it & (TW - 1);
       if (c < ncol) {
         const long long k = ((bb * s.L + l) * (long long)s.Q + q) * s.Hz + kz0 + c;
-        if (ca.mode == CLAMP_ABS)
+        if (MODE == MODE_FCI)
           buf[l * P + c] = freq_clamp<T>(buf[l * P + c], ca.delta, fedits, k, H);
         else
           buf[l * P + c] = freq_project<T>(buf[l * P + c], ca, fedits, k, base + (long long)l * s.Wtot + c, H);

@@ -373,23 +373,18 @@ __global__ void __launch_bounds__((L / rp_elems(L)) << LGTW,
   for (int i = 0; i < E; ++i)
     v[i] = live ? src[(long long)first_pos<L, D0>(t, i) * s.Wtot] : mkc<T>(T(0), T(0));
   RRun<T, D0, L, LY, 0>::run(v, buf, t, c, p);
-  if (MODE == MODE_FCI) {
-    if (live && ca.mode == CLAMP_ABS) {
+  if (MODE == MODE_FCI || MODE == MODE_FCIX) {
+    if (live) {
 #pragma unroll
       for (int i = 0; i < E; ++i) {
         const int l = last_pos<L, -1>(t, i);
         const long long k = ((bb * L + l) * (long long)s.Q + q) * s.Hz + kz0 + c;
-        v[i] = freq_clamp<T>(v[i], ca.delta, fedits, k, H);
-      }
-    } else if (live) {
-      // the other modes apart from the all-abs loop, which stays as tight as a
-      // plain clamp
-#pragma unroll
-      for (int i = 0; i < E; ++i) {
-        const int l = last_pos<L, -1>(t, i);
-        const long long k = ((bb * L + l) * (long long)s.Q + q) * s.Hz + kz0 + c;
-        const long long pad = (bb * L + l) * s.Wtot + (long long)q * s.Hzp + kz0 + c;
-        v[i] = freq_project<T>(v[i], ca, fedits, k, pad, H);
+        if (MODE == MODE_FCI) {
+          v[i] = freq_clamp<T>(v[i], ca.delta, fedits, k, H);
+        } else {
+          const long long pad = (bb * L + l) * s.Wtot + (long long)q * s.Hzp + kz0 + c;
+          v[i] = freq_project<T>(v[i], ca, fedits, k, pad, H);
+        }
       }
     }
     // The inverse's first stage reads the positions the forward's last

@@ -82,7 +82,7 @@ struct ffcz_solver {
   Launch lz_f, lz_i, ly, lx;
   int has_x = 0, has_y = 0, fused = 0;  // fused: 0 none, 1 y, 2 x
   // kernels of each pass (generic or compile-time-sized), typed at launch
-  void *kzf[3] = {}, *kzi = nullptr, *ky[3] = {}, *kx[3] = {};
+  void *kzf[3] = {}, *kzi = nullptr, *ky[4] = {}, *kx[4] = {};
   int static_z = 0, static_y = 0, static_x = 0;
   // parameters
   double eps = 0, delta = 0;
@@ -149,6 +149,7 @@ int set_smem_attrs() {
   FFCZ_CUDA(cudaFuncSetAttribute(k_strided<T, MODE_FWD, E>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
   FFCZ_CUDA(cudaFuncSetAttribute(k_strided<T, MODE_INV, E>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
   FFCZ_CUDA(cudaFuncSetAttribute(k_strided<T, MODE_FCI, E>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+  FFCZ_CUDA(cudaFuncSetAttribute(k_strided<T, MODE_FCIX, E>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
   return FFCZ_OK;
 }
 
@@ -163,9 +164,9 @@ int select_kernels(ffcz_solver *s) {
   s->kzf[PRO_DIFF] = (void *)k_zfwd<T, PRO_DIFF, E>;
   s->kzf[PRO_CLAMP] = (void *)k_zfwd<T, PRO_CLAMP, E>;
   s->kzi = (void *)k_zinv<T, E>;
-  void *gen[3] = {(void *)k_strided<T, MODE_FWD, E>, (void *)k_strided<T, MODE_INV, E>,
-                  (void *)k_strided<T, MODE_FCI, E>};
-  for (int m = 0; m < 3; ++m) s->ky[m] = s->kx[m] = gen[m];
+  void *gen[4] = {(void *)k_strided<T, MODE_FWD, E>, (void *)k_strided<T, MODE_INV, E>,
+                  (void *)k_strided<T, MODE_FCI, E>, (void *)k_strided<T, MODE_FCIX, E>};
+  for (int m = 0; m < 4; ++m) s->ky[m] = s->kx[m] = gen[m];
   const char *off = getenv("FFCZ_GENERIC_KERNELS");
   if (off && off[0] == '1') return FFCZ_OK;
   StaticGeom g;
@@ -189,11 +190,11 @@ int select_kernels(ffcz_solver *s) {
   }
   auto strided = [&](int L, int Q, long long B, SArgs &sa, Launch &ln, void **k, int &flag, AxisPlan &pl,
                      const AxisPlan &ps) {
-    StridedFn<T> f[3];
+    StridedFn<T> f[4];
     bool ok = ps.nst > 0;
-    for (int m = 0; m < 3 && ok; ++m) ok = static_strided<T>(L, m, f[m], g);
+    for (int m = 0; m < 4 && ok; ++m) ok = static_strided<T>(L, m, f[m], g);
     if (!ok) return;
-    for (int m = 0; m < 3; ++m) k[m] = (void *)f[m];
+    for (int m = 0; m < 4; ++m) k[m] = (void *)f[m];
     pl = ps;
     sa.TW = g.TW;
     sa.log2TW = __builtin_ctz(g.TW);
@@ -331,6 +332,7 @@ void launch_iteration(ffcz_solver *s, cudaStream_t st, int pro, const void *a, c
   mark();
   const T eps = (T)s->eps;
   const ClampArgs<T> delta = clamp_args<T>(s);
+  const int fci = s->cmode == CLAMP_ABS ? MODE_FCI : MODE_FCIX;
   const c2<T> *post = (const c2<T> *)s->d_tw + s->post_off;
   c2<T> *spec = (c2<T> *)s->d_spec;
   const T *pa = (const T *)a, *pb = (const T *)b;
@@ -352,7 +354,7 @@ void launch_iteration(ffcz_solver *s, cudaStream_t st, int pro, const void *a, c
                                                                                      tp<T>(s->d_fedits), H);
       mark();
     }
-    ((StridedFn<T>)s->kx[MODE_FCI])<<<s->lx.grid, s->lx.threads, s->lx.smem, st>>>(spec, s->sx, s->px, delta,
+    ((StridedFn<T>)s->kx[fci])<<<s->lx.grid, s->lx.threads, s->lx.smem, st>>>(spec, s->sx, s->px, delta,
                                                                                    tp<T>(s->d_fedits), H);
     mark();
     if (s->has_y) {
@@ -361,7 +363,7 @@ void launch_iteration(ffcz_solver *s, cudaStream_t st, int pro, const void *a, c
       mark();
     }
   } else if (s->fused == 1) {
-    ((StridedFn<T>)s->ky[MODE_FCI])<<<s->ly.grid, s->ly.threads, s->ly.smem, st>>>(spec, s->sy, s->py, delta,
+    ((StridedFn<T>)s->ky[fci])<<<s->ly.grid, s->ly.threads, s->ly.smem, st>>>(spec, s->sy, s->py, delta,
                                                                                    tp<T>(s->d_fedits), H);
     mark();
   } else {

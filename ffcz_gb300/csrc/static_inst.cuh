@@ -71,7 +71,8 @@ bool strided_for(int mode, StridedFn<T> &fn, StaticGeom &g) {
   using C = Cfg<T, L>;
   if (mode == MODE_FWD) fn = ks_strided<T, MODE_FWD, L, C::LGTW>;
   else if (mode == MODE_INV) fn = ks_strided<T, MODE_INV, L, C::LGTW>;
-  else fn = ks_strided<T, MODE_FCI, L, C::LGTW>;
+  else if (mode == MODE_FCI) fn = ks_strided<T, MODE_FCI, L, C::LGTW>;
+  else fn = ks_strided<T, MODE_FCIX, L, C::LGTW>;
   g.TW = C::TW;
   g.threads = C::NT;
   g.smem = (size_t)sl_size(L, C::TW, sizeof(T)) * sizeof(c2<T>);
