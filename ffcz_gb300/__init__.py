@@ -133,6 +133,7 @@ SIGNATURES = {
     "ffcz_container_read": [C.c_char_p, _p, _PP],
     "ffcz_init_direct": [_p, _p, _p, _p, _d, _sz],
     "ffcz_get_orig_spectrum": [_p, _p, _sz],
+    "ffcz_verify_bounds": [_p, C.POINTER(C.c_double), C.POINTER(C.c_double)],
     "ffcz_init_all_ptw": [_p, _p, _d, _d],
     "ffcz_init_all_ptw_device": [_p, _p, _d, _d],
     "ffcz_init_partial_ptw": [_p, _p, _p, _d, _d, _sz],
@@ -278,6 +279,13 @@ class ProjectionSolver:
         idx = self._indices(freq_indices)
         _check(lib().ffcz_init_partial_ptw(self._h, _np_ptr(x), _np_ptr(idx) if idx.size else None,
                                            float(delta_ptw), float(spatial_epsilon), idx.size))
+
+    def verify_bounds(self) -> tuple[float, float]:
+        """(max |e|, max over the half spectrum of max(|Re|, |Im|) of e's R2C),
+        both in FP64 on the device."""
+        a, b = C.c_double(), C.c_double()
+        _check(lib().ffcz_verify_bounds(self._h, C.byref(a), C.byref(b)))
+        return a.value, b.value
 
     def get_orig_spectrum(self) -> np.ndarray:
         """The spectrum of x the pointwise modes compare against (H complex)."""

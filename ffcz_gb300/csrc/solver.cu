@@ -84,6 +84,7 @@ struct ffcz_solver {
   // kernels of each pass (generic or compile-time-sized), typed at launch
   void *kzf[3] = {}, *kzi = nullptr, *ky[4] = {}, *kx[4] = {};
   int static_z = 0, static_y = 0, static_x = 0;
+  bool z_generic = true, y_generic = true, x_generic = true;  // runtime-planned tile fits
   // parameters
   double eps = 0, delta = 0;
   bool initialized = false;  // some initialiser ran (x is on the device)
@@ -99,6 +100,8 @@ struct ffcz_solver {
   unsigned char *d_mask = nullptr;   // partial pointwise: H flags
   bool ptw_partial = false;
   int partial_dc = 0;
+  ffcz_solver *verifier = nullptr;   // FP64 twin of ffcz_verify_bounds
+  unsigned long long *d_vmax = nullptr;
   bool extracted = false;
   // graph cache
   cudaGraph_t graph = nullptr;
@@ -254,7 +257,11 @@ int plan_solver(ffcz_solver *s) {
     const int rows_smem = s->even ? s->M + 1 : (int)s->nz;
     const int L = s->even ? s->M : (int)s->nz;
     int TW = 1;
-    FFCZ_TRY(pick_tile(rows_smem, L, es2, twmax, s->lz_f, TW, E));
+    // a length the runtime-planned tile cannot hold may still have a
+    // compile-time kernel (FP64 above 1024); select_kernels checks
+    const int rc = pick_tile(rows_smem, L, es2, twmax, s->lz_f, TW, E);
+    if (rc != FFCZ_OK && !zs) return rc;
+    s->z_generic = rc == FFCZ_OK;
     s->lz_i = s->lz_f;
     s->za.rows = s->rows;
     s->za.Nz = (int)s->nz;
@@ -267,9 +274,12 @@ int plan_solver(ffcz_solver *s) {
     s->za.P = TW + 1;
     s->lz_f.grid = s->lz_i.grid = (unsigned)ceil_div((size_t)s->rows, (size_t)TW);
   }
-  auto plan_strided = [&](int L, int Q, long long B, SArgs &sa, Launch &ln) -> int {
+  auto plan_strided = [&](int L, int Q, long long B, SArgs &sa, Launch &ln, bool has_static,
+                          bool &generic) -> int {
     int TW = 1;
-    FFCZ_TRY(pick_tile(L, L, es2, twmax, ln, TW, E));
+    const int rc = pick_tile(L, L, es2, twmax, ln, TW, E);
+    if (rc != FFCZ_OK && !has_static) return rc;
+    generic = rc == FFCZ_OK;
     sa.L = L;
     sa.Q = Q;
     sa.Hz = s->Hz;
@@ -284,13 +294,16 @@ int plan_solver(ffcz_solver *s) {
     ln.grid = (unsigned)tiles;
     return FFCZ_OK;
   };
-  if (s->has_y) FFCZ_TRY(plan_strided((int)s->ny, 1, (long long)s->nx, s->sy, s->ly));
-  if (s->has_x) FFCZ_TRY(plan_strided((int)s->nx, (int)s->ny, 1, s->sx, s->lx));
+  if (s->has_y) FFCZ_TRY(plan_strided((int)s->ny, 1, (long long)s->nx, s->sy, s->ly, ys, s->y_generic));
+  if (s->has_x) FFCZ_TRY(plan_strided((int)s->nx, (int)s->ny, 1, s->sx, s->lx, xs, s->x_generic));
   s->fused = s->has_x ? 2 : (s->has_y ? 1 : 0);
   s->kernels_per_iter = 2 /*z fwd, z inv*/ + 1 /*check*/ + 1 /*fused axis or clamp*/ +
                         ((s->has_y && s->fused == 2) ? 2 : 0);
   FFCZ_TRY(set_smem_attrs<T>());
   FFCZ_TRY(select_kernels<T>(s));
+  if ((!s->z_generic && !s->static_z) || (s->has_y && !s->y_generic && !s->static_y) ||
+      (s->has_x && !s->x_generic && !s->static_x))
+    return fail(FFCZ_ERR_UNSUPPORTED, "an axis length has neither a runtime-planned nor a compile-time kernel");
   return FFCZ_OK;
 }
 
@@ -564,6 +577,11 @@ void free_all(ffcz_solver *s) {
   for (void *p : bufs)
     if (p) cudaFree(p);
   if (s->d_up_blk) cudaFree(s->d_up_blk);
+  if (s->d_vmax) cudaFree(s->d_vmax);
+  if (s->verifier) {
+    free_all(s->verifier);
+    delete s->verifier;
+  }
   if (s->d_bound) cudaFree(s->d_bound);
   if (s->d_orig) cudaFree(s->d_orig);
   if (s->d_mask) cudaFree(s->d_mask);
@@ -657,7 +675,7 @@ int reconstruct(ffcz_solver *s, const void *d_decomp, const uint16_t *fq, size_t
 // R2C of x with the solver's forward passes into d_orig (padded layout), the
 // spectrum the pointwise modes compare against (impl:612-623).
 template <typename T>
-int forward_spectrum(ffcz_solver *s) {
+int forward_spectrum(ffcz_solver *s, bool keep_as_orig = true) {
   cudaStream_t st = s->stream;
   c2<T> *spec = (c2<T> *)s->d_spec;
   const c2<T> *post = (const c2<T> *)s->d_tw + s->post_off;
@@ -671,12 +689,48 @@ int forward_spectrum(ffcz_solver *s) {
   if (s->has_x)
     ((StridedFn<T>)s->kx[MODE_FWD])<<<s->lx.grid, s->lx.threads, s->lx.smem, st>>>(spec, s->sx, s->px, none,
                                                                                    tp<T>(s->d_fedits), H);
-  const size_t bytes = (size_t)s->rows * s->Hzp * 2 * s->es;
-  if (!s->d_orig) FFCZ_CUDA(cudaMalloc(&s->d_orig, bytes));
-  FFCZ_CUDA(cudaMemcpyAsync(s->d_orig, s->d_spec, bytes, cudaMemcpyDeviceToDevice, st));
+  if (keep_as_orig) {
+    const size_t bytes = (size_t)s->rows * s->Hzp * 2 * s->es;
+    if (!s->d_orig) FFCZ_CUDA(cudaMalloc(&s->d_orig, bytes));
+    FFCZ_CUDA(cudaMemcpyAsync(s->d_orig, s->d_spec, bytes, cudaMemcpyDeviceToDevice, st));
+  }
   FFCZ_CUDA(cudaGetLastError());
   FFCZ_CUDA(cudaStreamSynchronize(st));
   return FFCZ_OK;
+}
+
+// |v| of non-negative doubles as ordered 64-bit integers (atomicMax).
+__device__ __forceinline__ void atomic_max_abs(unsigned long long *m, double v) {
+  atomicMax(m, (unsigned long long)__double_as_longlong(fabs(v)));
+}
+
+// e widened exactly to FP64 into the verifier's x, and max |e|.
+template <typename T>
+__global__ void k_widen_absmax(const T *__restrict__ e, double *__restrict__ out, long long n,
+                               unsigned long long *__restrict__ mx) {
+  double m = 0.0;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const double v = (double)e[i];
+    out[i] = v;
+    m = fmax(m, fabs(v));
+  }
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_down_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomic_max_abs(mx, m);
+}
+
+// max over the half spectrum (padding columns skipped) of max(|Re|, |Im|).
+__global__ void k_spec_absmax(const double2 *__restrict__ spec, long long rows, int Hz, int Hzp,
+                              unsigned long long *__restrict__ mx) {
+  double m = 0.0;
+  const long long total = rows * Hz;
+  for (long long it = (long long)blockIdx.x * blockDim.x + threadIdx.x; it < total;
+       it += (long long)gridDim.x * blockDim.x) {
+    const long long r = it / Hz;
+    const double2 v = spec[r * Hzp + (it - r * Hz)];
+    m = fmax(m, fmax(fabs(v.x), fabs(v.y)));
+  }
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_down_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomic_max_abs(mx, m);
 }
 
 }  // namespace
@@ -1087,6 +1141,36 @@ int ffcz_get_device_array(ffcz_solver *s, int which, void **dptr, size_t *bytes)
   }
   *dptr = p;
   if (bytes) *bytes = b;
+  return FFCZ_OK;
+}
+
+int ffcz_verify_bounds(ffcz_solver *s, double *spatial_max, double *freq_max) {
+  FFCZ_TRY(check_solver(s));
+  if (!spatial_max || !freq_max) return fail(FFCZ_ERR_INVALID, "NULL argument");
+  if (!s->verifier) {
+    ffcz_solver *v = nullptr;
+    FFCZ_TRY(ffcz_solver_create(s->nx, s->ny, s->nz, FFCZ_F64, &v));
+    s->verifier = v;
+  }
+  if (!s->d_vmax) FFCZ_CUDA(cudaMalloc(&s->d_vmax, 2 * sizeof(unsigned long long)));
+  ffcz_solver *v = s->verifier;
+  v->stream = s->stream;
+  cudaStream_t st = s->stream;
+  FFCZ_CUDA(cudaMemsetAsync(s->d_vmax, 0, 2 * sizeof(unsigned long long), st));
+  const unsigned g = (unsigned)std::min<size_t>(ceil_div(s->N, 256), 152 * 16);
+  if (s->dtype == FFCZ_F32)
+    k_widen_absmax<float><<<g, 256, 0, st>>>((const float *)s->d_e, (double *)v->d_x, (long long)s->N, s->d_vmax);
+  else
+    k_widen_absmax<double><<<g, 256, 0, st>>>((const double *)s->d_e, (double *)v->d_x, (long long)s->N,
+                                               s->d_vmax);
+  FFCZ_TRY(forward_spectrum<double>(v, false));
+  const unsigned g2 = (unsigned)std::min<size_t>(ceil_div(s->H, 256), 152 * 16);
+  k_spec_absmax<<<g2, 256, 0, st>>>((const double2 *)v->d_spec, (long long)v->rows, v->Hz, v->Hzp, s->d_vmax + 1);
+  unsigned long long h[2] = {0, 0};
+  FFCZ_CUDA(cudaMemcpyAsync(h, s->d_vmax, sizeof(h), cudaMemcpyDeviceToHost, st));
+  FFCZ_CUDA(cudaStreamSynchronize(st));
+  std::memcpy(spatial_max, &h[0], 8);
+  std::memcpy(freq_max, &h[1], 8);
   return FFCZ_OK;
 }
 

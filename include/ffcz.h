@@ -201,6 +201,13 @@ int ffcz_get_spatial_flags(ffcz_solver *s, uint8_t *dst, size_t cap,
  * initialize_*_ptw). */
 int ffcz_get_device_array(ffcz_solver *s, int which, void **dptr,
                           size_t *bytes);
+/* FP64 check of the last solve's corrected error e on the device (no
+ * counterpart in the reference): e widened exactly to FP64, its R2C in FP64
+ * by an FP64 twin of the solver (created on first use), and
+ *   spatial_max = max_i |e_i|,  freq_max = max_k max(|Re E_k|, |Im E_k|)
+ * over the half spectrum.  The all-abs bounds hold when spatial_max <= eps
+ * (+ the loop's tol) and freq_max <= delta. */
+int ffcz_verify_bounds(ffcz_solver *s, double *spatial_max, double *freq_max);
 /* The spectrum of x of the pointwise modes (d_orig_freq, impl:612-623):
  * H interleaved complex values of the solver's dtype. */
 int ffcz_get_orig_spectrum(ffcz_solver *s, void *h_dst, size_t cap_complex);

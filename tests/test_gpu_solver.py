@@ -265,3 +265,24 @@ def test_static_kernels_match_generic(cuda, shape, dtype, monkeypatch):
     assert np.abs(out[0][1] - out[1][1]).max() <= tol * np.abs(e0).max() * out[0][0]
     fs = float(np.abs(out[1][2]).max()) or 1.0
     assert np.abs(out[0][2] - out[1][2]).max() <= tol * max(fs, float(delta))
+
+
+@pytest.mark.parametrize("shape,dtype", [((16, 24, 10), np.float32), ((64, 64, 64), np.float32),
+                                         ((1, 90, 100), np.float32), ((3, 250, 500), np.float32),
+                                         ((1, 1, 4096), np.float32), ((12, 10, 16), np.float64),
+                                         ((5, 7, 9), np.float32)])
+def test_verify_bounds_on_device_matches_fp64_host(cuda, shape, dtype):
+    """ffcz_verify_bounds: max |e| exactly, and the FP64 half-spectrum maximum
+    of e within FP64 transform roundoff of numpy's."""
+    fld = synth.make_field(shape, 11 / 3, 17, 1e-3, 1e-3, dtype, noise=0.3)
+    delta = synth.stress_delta(fld, 1.0)
+    with F.ProjectionSolver(*shape, dtype=dtype) as s:
+        s.initialize_all_abs(fld.x, fld.eps, delta)
+        s.solve_all_abs((fld.xp - fld.x).astype(dtype), 100, 1e-7)
+        sm, fm = s.verify_bounds()
+        e = s.get_results().astype(np.float64)
+    assert sm == float(np.abs(e).max())
+    Fe = np.fft.rfftn(e.reshape(shape))
+    ref = float(max(np.abs(Fe.real).max(), np.abs(Fe.imag).max()))
+    assert abs(fm - ref) <= 1e-12 * max(ref, float(np.abs(e).sum()))
+    assert sm <= fld.eps + 1e-7 and fm <= delta * (1 + 1e-6)
