@@ -362,9 +362,12 @@ def run_ours(args):
 
     e_fin = s.get_results()
     bchk = O.check_bounds(np.zeros(1), e_fin.astype(np.float64), fld.eps, fld.delta)
+    dsm, dfm = s.verify_bounds()
     bounds = {"spatial_max_over_E": bchk["spatial_max"] / fld.eps, "freq_max_over_Delta": bchk["freq_max"] / fld.delta,
               "met": bool(bchk["spatial_excess"] <= 1e-7 and bchk["freq_excess"] <= 0.0),
-              "rule": "reference schedule: spatial within E + tol (1e-7), frequency within Delta"}
+              "rule": "reference schedule: spatial within E + tol (1e-7), frequency within Delta",
+              "check": "FP64 numpy on the host; the device check (ffcz_verify_bounds) beside it",
+              "device": {"spatial_max_over_E": dsm / fld.eps, "freq_max_over_Delta": dfm / fld.delta}}
 
     # e2e through the reference-facing API with host buffers
     for _ in range(max(1, args.warmup // 2)):
@@ -520,13 +523,14 @@ def run_batch(args):
     # FP64 check of both bounds per field (outside the timed regions)
     from oracle import ffcz_oracle as O
 
+    # (ffcz_verify_bounds: FP64 twin transform on the device, one field at a time)
     worst_s = worst_f = 0.0
     met = True
     for f, s in zip(fields, solvers):
-        chk = O.check_bounds(np.zeros(1), s.get_results().astype(np.float64), f.eps, f.delta)
-        worst_s = max(worst_s, chk["spatial_max"] / f.eps)
-        worst_f = max(worst_f, chk["freq_max"] / f.delta)
-        met = met and chk["spatial_excess"] <= 1e-7 and chk["freq_excess"] <= 0.0
+        sm, fm = s.verify_bounds()
+        worst_s = max(worst_s, sm / f.eps)
+        worst_f = max(worst_f, fm / f.delta)
+        met = met and sm - f.eps <= 1e-7 and fm <= f.delta
     # pass table of one field per shape family (single-field solves, profiled)
     peak, peak_kind = peak_hbm()
     fams, seen = {}, set()
@@ -578,7 +582,8 @@ def run_batch(args):
         "gpu_launches": launches,
         "active_edits": {"freq": sum(c[0] for c in counts), "spatial": sum(c[1] for c in counts)},
         "bounds_fp64": {"spatial_max_over_E": worst_s, "freq_max_over_Delta": worst_f, "met": bool(met),
-                        "rule": "every field: spatial within E + tol (1e-7), frequency within Delta"},
+                        "rule": "every field: spatial within E + tol (1e-7), frequency within Delta",
+                        "check": "FP64 on the device (ffcz_verify_bounds)"},
         "compressed_bytes": sum(len(c) for c in comp[len(comp) - last:]),
         "zstd_threads": nzt,
         "clocks": clk,
