@@ -35,23 +35,54 @@ void build_codebook(const uint32_t *hist, size_t nbins, Codebook &cb) {
     cb.max_len = 1;
     return;
   }
-  // Nodes: leaves 0..n-1, internal n..2n-2.
+  // Nodes: leaves 0..n-1, internal n..2n-2.  The reference pops the two
+  // smallest (freq, node index) keys of a min-heap.  The same sequence comes
+  // from two queues: the leaves sorted by (freq, index), and the internal
+  // nodes in creation order, whose keys are already sorted (merged weights
+  // never decrease and indices grow); the smaller head is the heap's top.
   std::vector<int> left(2 * n - 1, -1), right(2 * n - 1, -1);
-  using Key = std::pair<uint32_t, int>;
-  std::priority_queue<Key, std::vector<Key>, std::greater<Key>> pq;
-  for (int i = 0; i < n; ++i) pq.push({cb.freq[i], i});
+  std::vector<uint64_t> wt(2 * n - 1, 0);
+  // (freq, index) packed so that it sorts as the pair; LSD radix sort in
+  // 16-bit digits over the bits in use
+  std::vector<uint64_t> key(n), tmp(n);
+  uint64_t all = 0;
+  for (int i = 0; i < n; ++i) {
+    wt[i] = cb.freq[i];
+    key[i] = ((uint64_t)cb.freq[i] << 32) | (uint32_t)i;
+    all |= key[i];
+  }
+  std::vector<uint32_t> count(1u << 16);
+  for (int shift = 0; shift < 64 && (all >> shift); shift += 16) {
+    if (((all >> shift) & 0xffffu) == 0) continue;  // every digit zero: nothing moves
+    std::fill(count.begin(), count.end(), 0u);
+    for (int i = 0; i < n; ++i) ++count[(key[i] >> shift) & 0xffffu];
+    uint32_t run = 0;
+    for (uint32_t &c : count) {
+      const uint32_t t = c;
+      c = run;
+      run += t;
+    }
+    for (int i = 0; i < n; ++i) tmp[count[(key[i] >> shift) & 0xffffu]++] = key[i];
+    key.swap(tmp);
+  }
+  std::vector<int> leaves(n);
+  for (int i = 0; i < n; ++i) leaves[i] = (int)(key[i] & 0xffffffffu);
+  int qa = 0, qb = n;  // heads: sorted leaves, internal nodes
   int next = n;
-  while (pq.size() > 1) {
-    const Key a = pq.top();
-    pq.pop();
-    const Key b = pq.top();
-    pq.pop();
-    left[next] = a.second;
-    right[next] = b.second;
-    pq.push({a.first + b.first, next});
+  auto take = [&]() {
+    if (qa < n && (qb >= next || wt[leaves[qa]] < wt[qb] || (wt[leaves[qa]] == wt[qb] && leaves[qa] < qb)))
+      return leaves[qa++];
+    return qb++;
+  };
+  while (next < 2 * n - 1) {
+    const int a = take();
+    const int b = take();
+    left[next] = a;
+    right[next] = b;
+    wt[next] = wt[a] + wt[b];
     ++next;
   }
-  const int root = pq.top().second;
+  const int root = 2 * n - 2;
   // Iterative depth-first walk from the root.
   struct Item { int node; uint32_t code; int len; };
   std::vector<Item> stack;
