@@ -10,6 +10,8 @@
 #include <memory>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "extract.cuh"
 #include "fft_plan.h"
 #include "huffman.cuh"
@@ -85,6 +87,7 @@ struct ffcz_solver {
   void *kzf[3] = {}, *kzi = nullptr, *ky[4] = {}, *kx[4] = {};
   int static_z = 0, static_y = 0, static_x = 0;
   bool z_generic = true, y_generic = true, x_generic = true;  // runtime-planned tile fits
+  int z_ept = 0, y_ept = 0, x_ept = 0;  // values per thread of the runtime-planned tiles
   // parameters
   double eps = 0, delta = 0;
   bool initialized = false;  // some initialiser ran (x is on the device)
@@ -141,9 +144,8 @@ int pick_tile(int rows_smem, int L, size_t es2, int twmax, Launch &ln, int &TW, 
 
 template <typename T> constexpr int ept_of() { return sizeof(T) == 4 ? 8 : 4; }
 
-template <typename T>
-int set_smem_attrs() {
-  constexpr int E = ept_of<T>();
+template <typename T, int E>
+int set_smem_attrs_e() {
   const int mx = (int)kSmemMax;
   FFCZ_CUDA(cudaFuncSetAttribute(k_zfwd<T, PRO_PLAIN, E>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
   FFCZ_CUDA(cudaFuncSetAttribute(k_zfwd<T, PRO_DIFF, E>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
@@ -156,6 +158,33 @@ int set_smem_attrs() {
   return FFCZ_OK;
 }
 
+// FP64 axes longer than the 4-values-per-thread tile (1024) run the
+// runtime-planned kernels at 8 values per thread (up to 2048 per tile).
+constexpr int kWideEpt = 8;
+
+template <typename T>
+int set_smem_attrs() {
+  FFCZ_TRY((set_smem_attrs_e<T, ept_of<T>()>()));
+  if (sizeof(T) == 8) FFCZ_TRY((set_smem_attrs_e<T, kWideEpt>()));
+  return FFCZ_OK;
+}
+
+template <typename T, int E>
+void generic_z(ffcz_solver *s) {
+  s->kzf[PRO_PLAIN] = (void *)k_zfwd<T, PRO_PLAIN, E>;
+  s->kzf[PRO_DIFF] = (void *)k_zfwd<T, PRO_DIFF, E>;
+  s->kzf[PRO_CLAMP] = (void *)k_zfwd<T, PRO_CLAMP, E>;
+  s->kzi = (void *)k_zinv<T, E>;
+}
+
+template <typename T, int E>
+void generic_strided(void **k) {
+  k[MODE_FWD] = (void *)k_strided<T, MODE_FWD, E>;
+  k[MODE_INV] = (void *)k_strided<T, MODE_INV, E>;
+  k[MODE_FCI] = (void *)k_strided<T, MODE_FCI, E>;
+  k[MODE_FCIX] = (void *)k_strided<T, MODE_FCIX, E>;
+}
+
 // Generic kernels for every pass, replaced by the compile-time-sized ones
 // where the axis length has one (power of two, FP32 up to 1024, FP64 up to
 // 512); the static kernels fix their own tile width, so the pass arguments
@@ -163,13 +192,12 @@ int set_smem_attrs() {
 template <typename T>
 int select_kernels(ffcz_solver *s) {
   constexpr int E = ept_of<T>();
-  s->kzf[PRO_PLAIN] = (void *)k_zfwd<T, PRO_PLAIN, E>;
-  s->kzf[PRO_DIFF] = (void *)k_zfwd<T, PRO_DIFF, E>;
-  s->kzf[PRO_CLAMP] = (void *)k_zfwd<T, PRO_CLAMP, E>;
-  s->kzi = (void *)k_zinv<T, E>;
-  void *gen[4] = {(void *)k_strided<T, MODE_FWD, E>, (void *)k_strided<T, MODE_INV, E>,
-                  (void *)k_strided<T, MODE_FCI, E>, (void *)k_strided<T, MODE_FCIX, E>};
-  for (int m = 0; m < 4; ++m) s->ky[m] = s->kx[m] = gen[m];
+  if (s->z_ept == kWideEpt) generic_z<T, kWideEpt>(s);
+  else generic_z<T, E>(s);
+  if (s->y_ept == kWideEpt) generic_strided<T, kWideEpt>(s->ky);
+  else generic_strided<T, E>(s->ky);
+  if (s->x_ept == kWideEpt) generic_strided<T, kWideEpt>(s->kx);
+  else generic_strided<T, E>(s->kx);
   const char *off = getenv("FFCZ_GENERIC_KERNELS");
   if (off && off[0] == '1') return FFCZ_OK;
   StaticGeom g;
@@ -259,7 +287,12 @@ int plan_solver(ffcz_solver *s) {
     int TW = 1;
     // a length the runtime-planned tile cannot hold may still have a
     // compile-time kernel (FP64 above 1024); select_kernels checks
-    const int rc = pick_tile(rows_smem, L, es2, twmax, s->lz_f, TW, E);
+    int rc = pick_tile(rows_smem, L, es2, twmax, s->lz_f, TW, E);
+    s->z_ept = E;
+    if (rc != FFCZ_OK && sizeof(T) == 8) {
+      rc = pick_tile(rows_smem, L, es2, twmax, s->lz_f, TW, kWideEpt);
+      s->z_ept = kWideEpt;
+    }
     if (rc != FFCZ_OK && !zs) return rc;
     s->z_generic = rc == FFCZ_OK;
     s->lz_i = s->lz_f;
@@ -275,9 +308,14 @@ int plan_solver(ffcz_solver *s) {
     s->lz_f.grid = s->lz_i.grid = (unsigned)ceil_div((size_t)s->rows, (size_t)TW);
   }
   auto plan_strided = [&](int L, int Q, long long B, SArgs &sa, Launch &ln, bool has_static,
-                          bool &generic) -> int {
+                          bool &generic, int &ept) -> int {
     int TW = 1;
-    const int rc = pick_tile(L, L, es2, twmax, ln, TW, E);
+    int rc = pick_tile(L, L, es2, twmax, ln, TW, E);
+    ept = E;
+    if (rc != FFCZ_OK && sizeof(T) == 8) {
+      rc = pick_tile(L, L, es2, twmax, ln, TW, kWideEpt);
+      ept = kWideEpt;
+    }
     if (rc != FFCZ_OK && !has_static) return rc;
     generic = rc == FFCZ_OK;
     sa.L = L;
@@ -294,8 +332,9 @@ int plan_solver(ffcz_solver *s) {
     ln.grid = (unsigned)tiles;
     return FFCZ_OK;
   };
-  if (s->has_y) FFCZ_TRY(plan_strided((int)s->ny, 1, (long long)s->nx, s->sy, s->ly, ys, s->y_generic));
-  if (s->has_x) FFCZ_TRY(plan_strided((int)s->nx, (int)s->ny, 1, s->sx, s->lx, xs, s->x_generic));
+  if (s->has_y)
+    FFCZ_TRY(plan_strided((int)s->ny, 1, (long long)s->nx, s->sy, s->ly, ys, s->y_generic, s->y_ept));
+  if (s->has_x) FFCZ_TRY(plan_strided((int)s->nx, (int)s->ny, 1, s->sx, s->lx, xs, s->x_generic, s->x_ept));
   s->fused = s->has_x ? 2 : (s->has_y ? 1 : 0);
   s->kernels_per_iter = 2 /*z fwd, z inv*/ + 1 /*check*/ + 1 /*fused axis or clamp*/ +
                         ((s->has_y && s->fused == 2) ? 2 : 0);
@@ -308,6 +347,13 @@ int plan_solver(ffcz_solver *s) {
 }
 
 template <typename T> T *tp(void *p) { return (T *)p; }
+
+// NVTX range for the duration of a scope (visible to profilers that attach
+// an NVTX tool; a no-op otherwise).
+struct Range {
+  explicit Range(const char *name) { nvtxRangePushA(name); }
+  ~Range() { nvtxRangePop(); }
+};
 
 // Kernel arguments of the running constraint mode; the pointwise constants
 // are computed in T the way projection_algorithm.cu:206-236 does.
@@ -765,7 +811,14 @@ int ffcz_solver_create(size_t nx, size_t ny, size_t nz, int dtype, ffcz_solver *
   s->fpack_bytes = round_up(H2, 32) / 8;
   s->spack_bytes = round_up(N, 32) / 8;
   s->nblk_max = ceil_div(std::max(H2, N), (size_t)EX_CHUNK);
+  // FFCZ_FAIL_ALLOC=k makes the k-th allocation below report an out-of-
+  // memory error without calling the allocator (host-side fault injection
+  // for the cleanup paths; the GPU is not touched).
+  const char *inj = getenv("FFCZ_FAIL_ALLOC");
+  const int fail_at = inj ? atoi(inj) : 0;
+  int nalloc = 0;
   auto alloc = [&](void **p, size_t bytes) -> int {
+    if (++nalloc == fail_at) return cuda_fail(cudaErrorMemoryAllocation, "cudaMalloc (injected)", __FILE__, __LINE__);
     FFCZ_CUDA(cudaMalloc(p, std::max<size_t>(bytes, 16)));
     return FFCZ_OK;
   };
@@ -880,6 +933,7 @@ static int check_indices(ffcz_solver *s, const size_t *idx, size_t num) {
 static int solve_mode(ffcz_solver *s, int mode, int pro, const void *a, const void *b, int max_iter, double tol,
                       bool extract_after) {
   FFCZ_TRY(check_solver(s));
+  Range r("ffcz:solve");
   const bool ready = mode == FFCZ_MODE_ALL_ABS ? s->abs_ready
                    : mode == FFCZ_MODE_DIRECT ? s->direct_ready
                    : mode == FFCZ_MODE_ALL_PTW ? s->ptw_ready
@@ -1146,6 +1200,7 @@ int ffcz_get_device_array(ffcz_solver *s, int which, void **dptr, size_t *bytes)
 
 int ffcz_verify_bounds(ffcz_solver *s, double *spatial_max, double *freq_max) {
   FFCZ_TRY(check_solver(s));
+  Range r("ffcz:verify_bounds");
   if (!spatial_max || !freq_max) return fail(FFCZ_ERR_INVALID, "NULL argument");
   if (!s->verifier) {
     ffcz_solver *v = nullptr;
@@ -1245,6 +1300,7 @@ int ffcz_reconstruct_device(ffcz_solver *s, const void *d_decomp, const uint16_t
 int ffcz_solver_decode(ffcz_solver *s, const void *d_decomp, ffcz_huff_result *const *in4, double freq_min,
                        double freq_max, double spatial_min, double spatial_max, void *d_out) {
   FFCZ_TRY(check_solver(s));
+  Range r("ffcz:decode");
   if (!in4) return fail(FFCZ_ERR_INVALID, "in4 is NULL");
   const size_t nf = in4[0] ? in4[0]->num_elements : 0, ns = in4[2] ? in4[2]->num_elements : 0;
   const size_t fpb = (2 * s->H + 7) / 8, spb = (s->N + 7) / 8;
@@ -1287,6 +1343,7 @@ int ffcz_solver_container_header(ffcz_solver *s, ffcz_container_header *h) {
 
 int ffcz_solver_encode(ffcz_solver *s, int zstd_level, int zstd_mode, ffcz_huff_result **out4) {
   FFCZ_TRY(check_solver(s));
+  Range r("ffcz:encode");
   if (!out4) return fail(FFCZ_ERR_INVALID, "out4 is NULL");
   for (int i = 0; i < 4; ++i) out4[i] = nullptr;
   if (!s->extracted) return fail(FFCZ_ERR_INVALID, "extract before encode");
@@ -1455,6 +1512,7 @@ int ffcz_batch_reset_edit_accumulators(ffcz_batch *b) {
 int ffcz_batch_solve_pair_device(ffcz_batch *b, const void *const *d_orig, const void *const *d_decomp,
                                  int max_iter, double tol) {
   if (!b) return fail(FFCZ_ERR_INVALID, "batch is NULL");
+  Range r("ffcz:batch_solve");
   if (!d_orig || !d_decomp) return fail(FFCZ_ERR_INVALID, "field pointer arrays are NULL");
   const size_t nf = b->f.size();
   for (size_t i = 0; i < nf; ++i) {

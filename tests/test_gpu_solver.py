@@ -249,9 +249,8 @@ def test_static_kernels_match_generic(cuda, shape, dtype, monkeypatch):
     delta = synth.stress_delta(fld, 1.5)
     e0 = (fld.xp.astype(np.float64) - fld.x.astype(np.float64)).astype(dtype)
     out = []
-    if dtype == np.float64 and max(shape) > 1024 and max(shape) & (max(shape) - 1):
-        # FP64 axes above 1024 exist only as compile-time lengths (2048)
-        pytest.skip("FP64 axis length above the runtime-planned engine's 1024")
+    if dtype == np.float64 and max(shape) > 2048:
+        pytest.skip("FP64 axis length above the runtime-planned engine's 2048")
     for generic in ("0", "1"):
         monkeypatch.setenv("FFCZ_GENERIC_KERNELS", generic)
         with F.ProjectionSolver(*shape, dtype=dtype) as s:
@@ -286,3 +285,42 @@ def test_verify_bounds_on_device_matches_fp64_host(cuda, shape, dtype):
     ref = float(max(np.abs(Fe.real).max(), np.abs(Fe.imag).max()))
     assert abs(fm - ref) <= 1e-12 * max(ref, float(np.abs(e).sum()))
     assert sm <= fld.eps + 1e-7 and fm <= delta * (1 + 1e-6)
+
+
+def test_allocation_failure_is_reported_and_cleaned_up(cuda, monkeypatch):
+    """Host-side fault injection (FFCZ_FAIL_ALLOC=k fails the k-th device
+    allocation of a solver without calling the allocator): each failure is a
+    CUDA-class status naming the injected call, and nothing is left behind."""
+    F.ProjectionSolver(96, 96, 96).close()  # first creation's one-time costs
+    cuda.cuda.synchronize()
+    free0 = cuda.cuda.mem_get_info()[0]
+    for k in range(1, 17):
+        monkeypatch.setenv("FFCZ_FAIL_ALLOC", str(k))
+        with pytest.raises(F.FFCzError) as ei:
+            F.ProjectionSolver(96, 96, 96)
+        assert ei.value.code == -2 and "injected" in str(ei.value), k
+    monkeypatch.delenv("FFCZ_FAIL_ALLOC")
+    with F.ProjectionSolver(96, 96, 96) as s:
+        s.initialize_all_abs(np.zeros(96 ** 3, np.float32), 1e30, 1e30)
+        assert s.solve_all_abs(np.ones(96 ** 3, np.float32), 3, 1e-7) == 1
+    cuda.cuda.synchronize()
+    assert free0 - cuda.cuda.mem_get_info()[0] < 16 << 20
+
+
+@pytest.mark.parametrize("shape", [(1, 900, 1800), (3, 1250, 16), (2, 6, 3000), (1, 1, 4096)])
+def test_fp64_long_axes(cuda, shape):
+    """FP64 axes beyond the 4-values-per-thread tile (1024): runtime-planned
+    tiles at 8 values per thread, or the compile-time kernels, against the
+    FP64 oracle."""
+    fld = synth.make_field(shape, 11 / 3, 19, 1e-3, 1e-3, np.float64, noise=0.3)
+    delta = synth.stress_delta(fld, 1.0)
+    e0 = fld.xp - fld.x
+    with F.ProjectionSolver(*shape, dtype=np.float64) as s:
+        s.initialize_all_abs(fld.x, fld.eps, delta)
+        it = s.solve_all_abs(e0, 100, 1e-7)
+        ref = O.solve_all_abs(e0, shape, fld.eps, delta, 100, 1e-7, np.float64)
+        assert it == ref["iterations"]
+        es = float(np.abs(e0).max())
+        assert np.abs(s.get_results().reshape(-1) - ref["e"].reshape(-1)).max() <= 1e-12 * es * max(1, it)
+        fs = float(np.abs(np.fft.rfftn(e0.reshape(shape))).max())
+        assert np.abs(s.get_freq_edits_full() - ref["freq_edits"]).max() <= 1e-12 * fs * max(1, it)
