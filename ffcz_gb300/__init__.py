@@ -140,6 +140,7 @@ SIGNATURES = {
     "ffcz_solve": [_p, _p, _i, _d],
     "ffcz_solve_all_ptw": [_p, _p, _i, _d],
     "ffcz_solve_mode_device": [_p, _i, _p, _i, _d],
+    "ffcz_base_quantize_device": [_p, _sz, _i, _d, _p, _p, _p],
     "ffcz_write_map": [C.c_char_p, _p, _p, _p, _sz],
     "ffcz_read_map": [C.c_char_p, _p, _p, _p, _sz, _SP],
     "ffcz_last_error": [],
@@ -647,6 +648,17 @@ def _table_arrays(code_table):
         lens = np.array([code_table[s][1] for s in syms], dtype=np.int32)
         return syms, codes, lens
     return tuple(np.ascontiguousarray(a, dt) for a, dt in zip(code_table, (np.uint32, np.uint32, np.int32)))
+
+
+def base_quantize_device(d_x, eps: float, d_xprime, d_index=None, stream=None) -> None:
+    """x' = 2eps * rint(x / 2eps) on the device (torch CUDA tensors of float32
+    or float64); d_index (int32) optionally receives the quantisation indices."""
+    import torch
+
+    dt = FFCZ_F32 if d_x.dtype == torch.float32 else FFCZ_F64
+    ptr = 0 if stream is None else (stream if isinstance(stream, int) else stream.cuda_stream)
+    _check(lib().ffcz_base_quantize_device(_dev_ptr(d_x), d_x.numel(), dt, float(eps), _dev_ptr(d_xprime),
+                                           None if d_index is None else _dev_ptr(d_index), C.c_void_p(ptr)))
 
 
 def huff_decode_device(d_bits, nbytes: int, code_table, num_elements: int, dtype, d_out, stream=None) -> int:

@@ -389,6 +389,15 @@ int ffcz_solver_decode(ffcz_solver *s, const void *d_decomp,
                        double freq_max, double spatial_min,
                        double spatial_max, void *d_out);
 
+/* ---- base compressor ----------------------------------------------------- */
+/* A uniform scalar quantiser producing x' on the GPU (the step before the
+ * corrector; the reference reads x' from a file, projection_example.cu:
+ * 160-176): q_i = rint(x_i / 2eps) (half to even), x'_i = T(2eps * q_i), in
+ * FP64.  d_index (optional, n int32) receives q.  Returns after `stream`
+ * finished. */
+int ffcz_base_quantize_device(const void *d_x, size_t n, int dtype, double eps,
+                              void *d_xprime, int32_t *d_index, void *stream);
+
 /* ---- the .ffcz container ------------------------------------------------ */
 /* The reference's CLI parses -z/-o but writes nothing (projection_example.cu:
  * 75-86, 255-256).  One file holds what the decoder needs besides x': shape,

@@ -133,3 +133,20 @@ def test_decode_rejects_bad_streams(cuda):
         # no streams at all: x^ = x'
         s.decode_device(dxp, [None] * 4, mm, out)
         assert np.array_equal(out.cpu().numpy(), fld.xp.reshape(-1))
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_base_quantizer_matches_generator(cuda, dtype):
+    """The GPU base compressor gives the synthetic generator's x' (no noise)
+    bit for bit, and its indices."""
+    fld = synth.make_field((16, 24, 40), 11 / 3, 23, 1e-3, 1e-3, dtype)
+    dx = cuda.from_numpy(fld.x.reshape(-1).copy()).cuda()
+    out = cuda.empty_like(dx)
+    idx = cuda.empty(dx.numel(), dtype=cuda.int32, device="cuda")
+    eps = 1e-3 * float(fld.x.astype(np.float64).max() - fld.x.astype(np.float64).min())
+    F.base_quantize_device(dx, eps, out, idx)
+    x64 = fld.x.astype(np.float64).reshape(-1)
+    ref = (2 * eps * np.round(x64 / (2 * eps))).astype(dtype)
+    assert np.array_equal(out.cpu().numpy(), ref)
+    assert np.array_equal(idx.cpu().numpy(), np.round(x64 / (2 * eps)).astype(np.int32))
+    assert np.abs(out.cpu().numpy().astype(np.float64) - x64).max() <= eps * (1 + 1e-6)
