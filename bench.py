@@ -63,6 +63,7 @@ def parse():
     ap.add_argument("--zstd-level", type=int, default=20)
     ap.add_argument("--zstd-mode", default="single", choices=["single", "chunked"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default tile of every pass")
     ap.add_argument("--zstd-threads", type=int, default=0,
                     help="host threads of the ZSTD pool (default: cores - 2, at least 1)")
     ap.add_argument("--loop", default="graph", choices=["graph", "host"],
@@ -281,6 +282,7 @@ def run_ours(args):
     s.set_loop_driver(F.FFCZ_LOOP_HOST if args.loop == "host" else F.FFCZ_LOOP_GRAPH)
     s.set_profiling(True)
     s.initialize_all_abs_device(dx, fld.eps, fld.delta)
+    tune = {} if args.no_autotune else s.autotune(5)
 
     nzt = args.zstd_threads or max(1, (os.cpu_count() or 2) - 2)
     pool = ThreadPoolExecutor(max_workers=nzt)
@@ -408,6 +410,7 @@ def run_ours(args):
                      "algorithmic_bytes_per_launch": by_dom, "avg_launch_ms": ms_dom},
         "passes": {names[i]: {"ms": round(m, 5), "GB/s": round(b / (m / 1e3) / 1e9, 1)} for i, (m, b) in avg.items()},
         "gpu_launches": launches,
+        "autotune_ms": {k: [round(v[0], 4), round(v[1], 4)] for k, v in tune.items()},
         "step_latency_ms": 1e3 * step_latency,
         "serial_ms_per_step": 1e3 * t_serial,
         "serial_breakdown_ms": breakdown,
@@ -458,6 +461,12 @@ def run_batch(args):
         s = F.ProjectionSolver(*f.shape, dtype=f.x.dtype)
         s.initialize_all_abs_device(d, f.eps, f.delta)
         solvers.append(s)
+    tuned = {}
+    if not args.no_autotune:
+        for f, s in zip(fields, solvers):
+            key = "x".join(map(str, f.shape))
+            rep = s.autotune(5)
+            tuned.setdefault(key, {k: [round(v[0], 4), round(v[1], 4)] for k, v in rep.items()})
     batch = F.Batch(solvers)
     batch.set_stream(torch.cuda.current_stream())
     in_bytes = sum(f.x.nbytes for f in fields)
@@ -579,6 +588,7 @@ def run_batch(args):
         "batch_graph": {"ms": 1e3 * t_graph, "canonical_bytes": canon,
                         "GB/s_canonical": canon / t_graph / 1e9},
         "passes_by_family": fams,
+        "autotune_ms": tuned,
         "gpu_launches": launches,
         "active_edits": {"freq": sum(c[0] for c in counts), "spatial": sum(c[1] for c in counts)},
         "bounds_fp64": {"spatial_max_over_E": worst_s, "freq_max_over_Delta": worst_f, "met": bool(met),

@@ -134,6 +134,7 @@ SIGNATURES = {
     "ffcz_init_direct": [_p, _p, _p, _p, _d, _sz],
     "ffcz_get_orig_spectrum": [_p, _p, _sz],
     "ffcz_verify_bounds": [_p, C.POINTER(C.c_double), C.POINTER(C.c_double)],
+    "ffcz_solver_autotune": [_p, _i, _p],
     "ffcz_init_all_ptw": [_p, _p, _d, _d],
     "ffcz_init_all_ptw_device": [_p, _p, _d, _d],
     "ffcz_init_partial_ptw": [_p, _p, _p, _d, _d, _sz],
@@ -280,6 +281,13 @@ class ProjectionSolver:
         idx = self._indices(freq_indices)
         _check(lib().ffcz_init_partial_ptw(self._h, _np_ptr(x), _np_ptr(idx) if idx.size else None,
                                            float(delta_ptw), float(spatial_epsilon), idx.size))
+
+    def autotune(self, reps: int = 5) -> dict:
+        """Keeps the faster of two tile widths per pass (results unchanged);
+        returns {pass: (default ms, alternative ms)} (0 = no alternative)."""
+        ms = np.zeros(6)
+        _check(lib().ffcz_solver_autotune(self._h, int(reps), _np_ptr(ms)))
+        return {"z": (ms[0], ms[1]), "y": (ms[2], ms[3]), "x": (ms[4], ms[5])}
 
     def verify_bounds(self) -> tuple[float, float]:
         """(max |e|, max over the half spectrum of max(|Re|, |Im|) of e's R2C),

@@ -88,6 +88,9 @@ struct ffcz_solver {
   int static_z = 0, static_y = 0, static_x = 0;
   bool z_generic = true, y_generic = true, x_generic = true;  // runtime-planned tile fits
   int z_ept = 0, y_ept = 0, x_ept = 0;  // values per thread of the runtime-planned tiles
+  int zvar = 0, yvar = 0, xvar = 0;     // tile variant of each compile-time pass
+  double tune_ms[6] = {};               // autotuner: (default, alternative) ms of z, y, x
+  int kernel_gen = 0;                   // bumped when the autotuner swaps kernels
   // parameters
   double eps = 0, delta = 0;
   bool initialized = false;  // some initialiser ran (x is on the device)
@@ -185,6 +188,61 @@ void generic_strided(void **k) {
   k[MODE_FCIX] = (void *)k_strided<T, MODE_FCIX, E>;
 }
 
+// Compile-time kernels of the z passes (tile variant var); false when the
+// length has none or the variant is not distinct from the default.
+template <typename T>
+bool apply_static_z(ffcz_solver *s, int var) {
+  if (!s->even || s->pz_s.nst == 0) return false;
+  StaticGeom g;
+  ZfwdFn<T> f[3];
+  ZinvFn<T> fi;
+  bool ok = static_zinv<T>(s->M, fi, g, var);
+  for (int pro = 0; pro < 3 && ok; ++pro) ok = static_zfwd<T>(s->M, pro, f[pro], g, var);
+  if (!ok) return false;
+  for (int pro = 0; pro < 3; ++pro) s->kzf[pro] = (void *)f[pro];
+  s->kzi = (void *)fi;
+  s->pz = s->pz_s;
+  s->za.TW = g.TW;
+  s->za.log2TW = __builtin_ctz(g.TW);
+  s->za.P = g.TW + 1;
+  s->lz_f.threads = s->lz_i.threads = g.threads;
+  s->lz_f.smem = s->lz_i.smem = g.smem;
+  s->lz_f.grid = s->lz_i.grid = (unsigned)ceil_div((size_t)s->rows, (size_t)g.TW);
+  s->static_z = 1;
+  s->zvar = var;
+  return true;
+}
+
+// The same for a strided axis (axis 0: y, 1: x).
+template <typename T>
+bool apply_static_strided(ffcz_solver *s, int axis, int var) {
+  const int L = axis == 0 ? (int)s->ny : (int)s->nx;
+  const int Q = axis == 0 ? 1 : (int)s->ny;
+  const long long B = axis == 0 ? (long long)s->nx : 1;
+  SArgs &sa = axis == 0 ? s->sy : s->sx;
+  Launch &ln = axis == 0 ? s->ly : s->lx;
+  void **k = axis == 0 ? s->ky : s->kx;
+  const AxisPlan &ps = axis == 0 ? s->py_s : s->px_s;
+  if (ps.nst == 0) return false;
+  StaticGeom g;
+  StridedFn<T> f[4];
+  bool ok = true;
+  for (int m = 0; m < 4 && ok; ++m) ok = static_strided<T>(L, m, f[m], g, var);
+  if (!ok) return false;
+  for (int m = 0; m < 4; ++m) k[m] = (void *)f[m];
+  (axis == 0 ? s->py : s->px) = ps;
+  sa.TW = g.TW;
+  sa.log2TW = __builtin_ctz(g.TW);
+  sa.P = g.TW + 1;
+  sa.tpq = (int)ceil_div((size_t)s->Hz, (size_t)g.TW);
+  ln.threads = g.threads;
+  ln.smem = g.smem;
+  ln.grid = (unsigned)(B * Q * (long long)sa.tpq);
+  (axis == 0 ? s->static_y : s->static_x) = 1;
+  (axis == 0 ? s->yvar : s->xvar) = var;
+  return true;
+}
+
 // Generic kernels for every pass, replaced by the compile-time-sized ones
 // where the axis length has one (power of two, FP32 up to 1024, FP64 up to
 // 512); the static kernels fix their own tile width, so the pass arguments
@@ -200,44 +258,9 @@ int select_kernels(ffcz_solver *s) {
   else generic_strided<T, E>(s->kx);
   const char *off = getenv("FFCZ_GENERIC_KERNELS");
   if (off && off[0] == '1') return FFCZ_OK;
-  StaticGeom g;
-  if (s->even) {
-    ZfwdFn<T> f[3];
-    ZinvFn<T> fi;
-    bool ok = static_zinv<T>(s->M, fi, g);
-    for (int pro = 0; pro < 3 && ok; ++pro) ok = static_zfwd<T>(s->M, pro, f[pro], g);
-    if (ok && s->pz_s.nst > 0) {
-      for (int pro = 0; pro < 3; ++pro) s->kzf[pro] = (void *)f[pro];
-      s->kzi = (void *)fi;
-      s->pz = s->pz_s;
-      s->za.TW = g.TW;
-      s->za.log2TW = __builtin_ctz(g.TW);
-      s->za.P = g.TW + 1;
-      s->lz_f.threads = s->lz_i.threads = g.threads;
-      s->lz_f.smem = s->lz_i.smem = g.smem;
-      s->lz_f.grid = s->lz_i.grid = (unsigned)ceil_div((size_t)s->rows, (size_t)g.TW);
-      s->static_z = 1;
-    }
-  }
-  auto strided = [&](int L, int Q, long long B, SArgs &sa, Launch &ln, void **k, int &flag, AxisPlan &pl,
-                     const AxisPlan &ps) {
-    StridedFn<T> f[4];
-    bool ok = ps.nst > 0;
-    for (int m = 0; m < 4 && ok; ++m) ok = static_strided<T>(L, m, f[m], g);
-    if (!ok) return;
-    for (int m = 0; m < 4; ++m) k[m] = (void *)f[m];
-    pl = ps;
-    sa.TW = g.TW;
-    sa.log2TW = __builtin_ctz(g.TW);
-    sa.P = g.TW + 1;
-    sa.tpq = (int)ceil_div((size_t)s->Hz, (size_t)g.TW);
-    ln.threads = g.threads;
-    ln.smem = g.smem;
-    ln.grid = (unsigned)(B * Q * (long long)sa.tpq);
-    flag = 1;
-  };
-  if (s->has_y) strided((int)s->ny, 1, (long long)s->nx, s->sy, s->ly, s->ky, s->static_y, s->py, s->py_s);
-  if (s->has_x) strided((int)s->nx, (int)s->ny, 1, s->sx, s->lx, s->kx, s->static_x, s->px, s->px_s);
+  apply_static_z<T>(s, 0);
+  if (s->has_y) apply_static_strided<T>(s, 0, 0);
+  if (s->has_x) apply_static_strided<T>(s, 1, 0);
   return FFCZ_OK;
 }
 
@@ -779,6 +802,91 @@ __global__ void k_spec_absmax(const double2 *__restrict__ spec, long long rows, 
   if ((threadIdx.x & 31) == 0) atomic_max_abs(mx, m);
 }
 
+// Times the default and the alternative tile of each compile-time pass on
+// the solver's own buffers (z forward + z inverse; y forward + y inverse;
+// the fused pass, with no clamp firing) and keeps the faster.  Every
+// variant computes the same values in the same order, so results do not
+// change.  The edit accumulators are cleared afterwards.
+template <typename T>
+int autotune(ffcz_solver *s, int reps, double *ms6) {
+  cudaStream_t st = s->stream;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  FFCZ_CUDA(cudaEventCreate(&e0));
+  FFCZ_CUDA(cudaEventCreate(&e1));
+  struct Ev {
+    cudaEvent_t a, b;
+    ~Ev() {
+      cudaEventDestroy(a);
+      cudaEventDestroy(b);
+    }
+  } guard{e0, e1};
+  const long long H = (long long)s->H;
+  c2<T> *spec = (c2<T> *)s->d_spec;
+  const c2<T> *post = (const c2<T> *)s->d_tw + s->post_off;
+  ClampArgs<T> ca;
+  ca.delta = std::numeric_limits<T>::infinity();
+  auto timed = [&](auto launch) -> double {
+    launch();
+    if (cudaStreamSynchronize(st) != cudaSuccess) return -1.0;
+    cudaEventRecord(e0, st);
+    for (int r = 0; r < reps; ++r) launch();
+    cudaEventRecord(e1, st);
+    if (cudaEventSynchronize(e1) != cudaSuccess) return -1.0;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    return (double)ms / reps;
+  };
+  double t[6] = {0, 0, 0, 0, 0, 0};
+  auto zrun = [&]() {
+    ((ZfwdFn<T>)s->kzf[PRO_PLAIN])<<<s->lz_f.grid, s->lz_f.threads, s->lz_f.smem, st>>>(
+        (const T *)s->d_x, nullptr, tp<T>(s->d_sedits), (T)s->eps, spec, s->za, s->pz, post);
+    ((ZinvFn<T>)s->kzi)<<<s->lz_i.grid, s->lz_i.threads, s->lz_i.smem, st>>>(spec, tp<T>(s->d_e), (T)s->eps,
+                                                                            T(1), s->d_ctl, s->za, s->pz, post);
+  };
+  if (s->static_z) {
+    for (int var = 0; var < 2; ++var)
+      if (apply_static_z<T>(s, var)) t[var] = timed(zrun);
+    apply_static_z<T>(s, (t[1] > 0 && t[1] < t[0]) ? 1 : 0);
+  }
+  for (int axis = 0; axis < 2; ++axis) {
+    const bool has = axis == 0 ? s->has_y : s->has_x;
+    const bool fused_here = (axis == 1 && s->fused == 2) || (axis == 0 && s->fused == 1);
+    if (!has || !(axis == 0 ? s->static_y : s->static_x)) continue;
+    void **k = axis == 0 ? s->ky : s->kx;
+    const Launch &ln = axis == 0 ? s->ly : s->lx;
+    const SArgs &sa = axis == 0 ? s->sy : s->sx;
+    const AxisPlan &pl = axis == 0 ? s->py : s->px;
+    auto run = [&]() {
+      if (fused_here) {
+        ((StridedFn<T>)k[MODE_FCI])<<<ln.grid, ln.threads, ln.smem, st>>>(spec, sa, pl, ca, tp<T>(s->d_fedits), H);
+      } else {
+        ((StridedFn<T>)k[MODE_FWD])<<<ln.grid, ln.threads, ln.smem, st>>>(spec, sa, pl, ca, tp<T>(s->d_fedits), H);
+        ((StridedFn<T>)k[MODE_INV])<<<ln.grid, ln.threads, ln.smem, st>>>(spec, sa, pl, ca, tp<T>(s->d_fedits), H);
+      }
+    };
+    double *tt = t + 2 + 2 * axis;
+    for (int var = 0; var < 2; ++var)
+      if (apply_static_strided<T>(s, axis, var)) tt[var] = timed(run);
+    apply_static_strided<T>(s, axis, (tt[1] > 0 && tt[1] < tt[0]) ? 1 : 0);
+  }
+  FFCZ_CUDA(cudaGetLastError());
+  for (double v : t)
+    if (v < 0) return fail(FFCZ_ERR_CUDA, "autotune launch failed");
+  FFCZ_CUDA(cudaMemsetAsync(s->d_fedits, 0, 2 * s->H * s->es, st));
+  FFCZ_CUDA(cudaMemsetAsync(s->d_sedits, 0, s->N * s->es, st));
+  FFCZ_CUDA(cudaStreamSynchronize(st));
+  // the cached loop graph holds the previous kernels
+  if (s->gexec) cudaGraphExecDestroy(s->gexec);
+  if (s->graph) cudaGraphDestroy(s->graph);
+  s->gexec = nullptr;
+  s->graph = nullptr;
+  ++s->kernel_gen;
+  for (int i = 0; i < 6; ++i) s->tune_ms[i] = t[i];
+  if (ms6)
+    for (int i = 0; i < 6; ++i) ms6[i] = t[i];
+  return FFCZ_OK;
+}
+
 }  // namespace
 
 #define DISPATCH(s, fn, ...) ((s)->dtype == FFCZ_F32 ? fn<float>(__VA_ARGS__) : fn<double>(__VA_ARGS__))
@@ -1198,6 +1306,13 @@ int ffcz_get_device_array(ffcz_solver *s, int which, void **dptr, size_t *bytes)
   return FFCZ_OK;
 }
 
+int ffcz_solver_autotune(ffcz_solver *s, int reps, double *ms6) {
+  FFCZ_TRY(check_solver(s));
+  if (reps < 1) return fail(FFCZ_ERR_INVALID, "reps must be positive");
+  Range r("ffcz:autotune");
+  return DISPATCH(s, autotune, s, reps, ms6);
+}
+
 int ffcz_verify_bounds(ffcz_solver *s, double *spatial_max, double *freq_max) {
   FFCZ_TRY(check_solver(s));
   Range r("ffcz:verify_bounds");
@@ -1394,7 +1509,7 @@ struct ffcz_batch {
   // graph key
   std::vector<const void *> ka, kb;
   std::vector<double> keps, kdelta;
-  std::vector<int> kpack;
+  std::vector<int> kpack, kgen;
   int kmax_iter = -1;
   double ktol = 0;
   cudaStream_t kstream = nullptr;
@@ -1528,16 +1643,17 @@ int ffcz_batch_solve_pair_device(ffcz_batch *b, const void *const *d_orig, const
     return FFCZ_OK;
   }
   std::vector<double> eps(nf), delta(nf);
-  std::vector<int> pack(nf);
+  std::vector<int> pack(nf), gen(nf);
   for (size_t i = 0; i < nf; ++i) {
     eps[i] = b->f[i]->eps;
     delta[i] = b->f[i]->delta;
     pack[i] = b->f[i]->pack_mode;
+    gen[i] = b->f[i]->kernel_gen;
   }
   const bool same = b->gexec && b->kmax_iter == max_iter && b->ktol == tol && b->kstream == b->stream &&
                     b->ka == std::vector<const void *>(d_orig, d_orig + nf) &&
                     b->kb == std::vector<const void *>(d_decomp, d_decomp + nf) && b->keps == eps &&
-                    b->kdelta == delta && b->kpack == pack;
+                    b->kdelta == delta && b->kpack == pack && b->kgen == gen;
   if (!same) {
     if (b->gexec) cudaGraphExecDestroy(b->gexec);
     if (b->graph) cudaGraphDestroy(b->graph);
@@ -1549,6 +1665,7 @@ int ffcz_batch_solve_pair_device(ffcz_batch *b, const void *const *d_orig, const
     b->keps = eps;
     b->kdelta = delta;
     b->kpack = pack;
+    b->kgen = gen;
     b->kmax_iter = max_iter;
     b->ktol = tol;
     b->kstream = b->stream;

@@ -18,7 +18,9 @@ namespace ffcz {
 #define FFCZ_Z_MIXED_TILE 0
 #endif
 
-template <typename T, int L, int CAP = 16>
+// VAR 0: the default tile; VAR 1: the autotuner's alternative (half or
+// double the thread budget), compiled beside it.
+template <typename T, int L, int CAP = 16, int VAR = 0>
 struct Cfg {
   static constexpr int E = rp_elems(L, CAP);
   static constexpr int TC = L / E;
@@ -27,9 +29,10 @@ struct Cfg {
   // values (~130-170 registers): 256; 8-12 values may use FFCZ_TILE_THREADS.
   // The power-of-two z passes run 256-thread blocks (8 rows of 256 complex
   // values at 512^3: z inverse 283 -> 230 us, z forward 278 -> 264 us).
-  static constexpr int BUDGET = E > 16 ? 256 : E == 16 ? 512
-                              : (CAP == 8 && (FFCZ_Z_MIXED_TILE || !mx_list(L))) ? FFCZ_Z_TILE_THREADS
-                                                                                  : FFCZ_TILE_THREADS;
+  static constexpr int BUDGET0 = E > 16 ? 256 : E == 16 ? 512
+                               : (CAP == 8 && (FFCZ_Z_MIXED_TILE || !mx_list(L))) ? FFCZ_Z_TILE_THREADS
+                                                                                   : FFCZ_TILE_THREADS;
+  static constexpr int BUDGET = VAR == 0 ? BUDGET0 : (BUDGET0 >= 512 ? BUDGET0 / 2 : BUDGET0 * 2);
   static constexpr int TW0 = BUDGET / TC;
   static constexpr int TW1 = TW0 < 1 ? 1 : (TW0 > TWMAX ? TWMAX : TW0);
   static constexpr int LGTW = ilog2(TW1);  // tile widths are powers of two
@@ -44,9 +47,10 @@ int set_smem(F fn, size_t smem) {
   return FFCZ_OK;
 }
 
-template <typename T, int M>
+template <typename T, int M, int VAR>
 bool zfwd_for(int pro, ZfwdFn<T> &fn, StaticGeom &g) {
-  using C = Cfg<T, M, 8>;
+  using C = Cfg<T, M, 8, VAR>;
+  if (VAR && C::TW == Cfg<T, M, 8, 0>::TW) return false;  // same tile as the default
   if (pro == PRO_PLAIN) fn = ks_zfwd<T, PRO_PLAIN, M, C::LGTW>;
   else if (pro == PRO_DIFF) fn = ks_zfwd<T, PRO_DIFF, M, C::LGTW>;
   else fn = ks_zfwd<T, PRO_CLAMP, M, C::LGTW>;
@@ -56,9 +60,10 @@ bool zfwd_for(int pro, ZfwdFn<T> &fn, StaticGeom &g) {
   return set_smem(fn, g.smem) == FFCZ_OK;
 }
 
-template <typename T, int M>
+template <typename T, int M, int VAR>
 bool zinv_for(ZinvFn<T> &fn, StaticGeom &g) {
-  using C = Cfg<T, M, 8>;
+  using C = Cfg<T, M, 8, VAR>;
+  if (VAR && C::TW == Cfg<T, M, 8, 0>::TW) return false;
   fn = ks_zinv<T, M, C::LGTW>;
   g.TW = C::TW;
   g.threads = C::NT;
@@ -66,9 +71,10 @@ bool zinv_for(ZinvFn<T> &fn, StaticGeom &g) {
   return set_smem(fn, g.smem) == FFCZ_OK;
 }
 
-template <typename T, int L>
+template <typename T, int L, int VAR>
 bool strided_for(int mode, StridedFn<T> &fn, StaticGeom &g) {
-  using C = Cfg<T, L>;
+  using C = Cfg<T, L, 16, VAR>;
+  if (VAR && C::TW == Cfg<T, L, 16, 0>::TW) return false;
   if (mode == MODE_FWD) fn = ks_strided<T, MODE_FWD, L, C::LGTW>;
   else if (mode == MODE_INV) fn = ks_strided<T, MODE_INV, L, C::LGTW>;
   else if (mode == MODE_FCI) fn = ks_strided<T, MODE_FCI, L, C::LGTW>;
@@ -86,30 +92,30 @@ bool strided_for(int mode, StridedFn<T> &fn, StaticGeom &g) {
 
 #define DEFINE_LOOKUPS(T, CASES)                                                  \
   template <>                                                                     \
-  bool static_zfwd<T>(int M, int pro, ZfwdFn<T> &fn, StaticGeom &g) {             \
+  bool static_zfwd<T>(int M, int pro, ZfwdFn<T> &fn, StaticGeom &g, int var) {    \
     switch (M) {                                                                  \
       CASES(ZF)                                                                   \
       default: return false;                                                      \
     }                                                                             \
   }                                                                               \
   template <>                                                                     \
-  bool static_zinv<T>(int M, ZinvFn<T> &fn, StaticGeom &g) {                      \
+  bool static_zinv<T>(int M, ZinvFn<T> &fn, StaticGeom &g, int var) {             \
     switch (M) {                                                                  \
       CASES(ZI)                                                                   \
       default: return false;                                                      \
     }                                                                             \
   }                                                                               \
   template <>                                                                     \
-  bool static_strided<T>(int L, int mode, StridedFn<T> &fn, StaticGeom &g) {      \
+  bool static_strided<T>(int L, int mode, StridedFn<T> &fn, StaticGeom &g, int var) { \
     switch (L) {                                                                  \
       CASES(ST)                                                                   \
       default: return false;                                                      \
     }                                                                             \
   }
 
-#define ZF(n) case n: return zfwd_for<TT, n>(pro, fn, g);
-#define ZI(n) case n: return zinv_for<TT, n>(fn, g);
-#define ST(n) case n: return strided_for<TT, n>(mode, fn, g);
+#define ZF(n) case n: return var ? zfwd_for<TT, n, 1>(pro, fn, g) : zfwd_for<TT, n, 0>(pro, fn, g);
+#define ZI(n) case n: return var ? zinv_for<TT, n, 1>(fn, g) : zinv_for<TT, n, 0>(fn, g);
+#define ST(n) case n: return var ? strided_for<TT, n, 1>(mode, fn, g) : strided_for<TT, n, 0>(mode, fn, g);
 
 
 }  // namespace ffcz

@@ -32,8 +32,10 @@ void build_static_plan(int L, int cap, AxisPlan &p, std::vector<std::complex<dou
 
 // Kernel for a length static_length() accepts (false otherwise).
 // z passes: M = Nz/2; pro is PRO_PLAIN/PRO_DIFF/PRO_CLAMP.
-template <typename T> bool static_zfwd(int M, int pro, ZfwdFn<T> &fn, StaticGeom &g);
-template <typename T> bool static_zinv(int M, ZinvFn<T> &fn, StaticGeom &g);
-template <typename T> bool static_strided(int L, int mode, StridedFn<T> &fn, StaticGeom &g);
+// var 0: the default tile; var 1: the autotuner's alternative tile width
+// (false when it equals the default's).
+template <typename T> bool static_zfwd(int M, int pro, ZfwdFn<T> &fn, StaticGeom &g, int var = 0);
+template <typename T> bool static_zinv(int M, ZinvFn<T> &fn, StaticGeom &g, int var = 0);
+template <typename T> bool static_strided(int L, int mode, StridedFn<T> &fn, StaticGeom &g, int var = 0);
 
 }  // namespace ffcz

@@ -201,6 +201,13 @@ int ffcz_get_spatial_flags(ffcz_solver *s, uint8_t *dst, size_t cap,
  * initialize_*_ptw). */
 int ffcz_get_device_array(ffcz_solver *s, int which, void **dptr,
                           size_t *bytes);
+/* Autotuner (no counterpart in the reference): times the default and an
+ * alternative tile width of each pass that has compile-time kernels (z pair,
+ * y pair, fused pass; reps launches each, on the solver's buffers) and keeps
+ * the faster.  Results are unchanged (same arithmetic, same order); the edit
+ * accumulators are cleared.  ms6 (may be NULL) receives the (default,
+ * alternative) ms of z, y and x, 0 where a pass has no alternative. */
+int ffcz_solver_autotune(ffcz_solver *s, int reps, double *ms6);
 /* FP64 check of the last solve's corrected error e on the device (no
  * counterpart in the reference): e widened exactly to FP64, its R2C in FP64
  * by an FP64 twin of the solver (created on first use), and

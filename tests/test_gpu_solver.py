@@ -324,3 +324,23 @@ def test_fp64_long_axes(cuda, shape):
         assert np.abs(s.get_results().reshape(-1) - ref["e"].reshape(-1)).max() <= 1e-12 * es * max(1, it)
         fs = float(np.abs(np.fft.rfftn(e0.reshape(shape))).max())
         assert np.abs(s.get_freq_edits_full() - ref["freq_edits"]).max() <= 1e-12 * fs * max(1, it)
+
+
+@pytest.mark.parametrize("shape", [(40, 512, 256), (8, 16, 2048), (4, 100, 200), (16, 1024, 32), (3, 250, 500)])
+def test_autotune_keeps_results(cuda, shape):
+    """The autotuner swaps tile widths only: results stay bit-identical."""
+    fld = synth.make_field(shape, 11 / 3, 29, 1e-3, 1e-3, np.float32, noise=0.3)
+    delta = synth.stress_delta(fld, 1.5)
+    e0 = (fld.xp - fld.x).astype(np.float32)
+    out = []
+    for tune in (False, True):
+        with F.ProjectionSolver(*shape) as s:
+            s.initialize_all_abs(fld.x, fld.eps, delta)
+            if tune:
+                rep = s.autotune(3)
+                assert all(v[0] >= 0 and v[1] >= 0 for v in rep.values())
+            it = s.solve_all_abs(e0, 100, 1e-7)
+            out.append((it, s.get_results(), s.get_freq_edits_full(), s.get_spatial_edits_full()))
+    assert out[0][0] == out[1][0]
+    for a, b in zip(out[0][1:], out[1][1:]):
+        assert np.array_equal(a, b)
