@@ -388,6 +388,11 @@ def run_ours(args):
     t_e2e = max_over_ranks(time.perf_counter() - t0, world)
     d2h = sum(len(r.bitstream) for r in out_e if r is not None) + 8 * 4
 
+    # the decoder on the last step's streams (GPU Huffman decode + reconstruction)
+    decode = measure_decode(F, torch, s, fld, dxp, args)
+    # the other constraint modes on the same field: fused-pass time and iterations
+    modes = measure_modes(F, s, fld, e0_np, dx)
+
     # dominant pass of the first iteration, from the events inside the graph
     peak, peak_kind = peak_hbm()
     names = pass_names(fld.shape)
@@ -411,6 +416,8 @@ def run_ours(args):
         "passes": {names[i]: {"ms": round(m, 5), "GB/s": round(b / (m / 1e3) / 1e9, 1)} for i, (m, b) in avg.items()},
         "gpu_launches": launches,
         "autotune_ms": {k: [round(v[0], 4), round(v[1], 4)] for k, v in tune.items()},
+        "decode": decode,
+        "modes": modes,
         "step_latency_ms": 1e3 * step_latency,
         "serial_ms_per_step": 1e3 * t_serial,
         "serial_breakdown_ms": breakdown,
@@ -426,6 +433,50 @@ def run_ours(args):
         print(json.dumps(line))
     pool.shutdown()
     s.close()
+
+
+def measure_decode(F, torch, s, fld, dxp, args, reps=5):
+    """GPU decode of the solver's current streams: Huffman decode of the four
+    streams + reconstruction x^ = x' + C2R(F)/N + S, device-event timed (the
+    bitstreams start in host memory, as after ZSTD_decompress)."""
+    streams = s.encode(args.zstd_level, F.FFCZ_ZSTD_NONE)  # the last solve's streams
+    mm = s.minmax()
+    if all(r is None for r in streams):
+        return {"note": "no edit streams to decode"}
+    out = torch.empty_like(dxp)
+    with F.ProjectionSolver(*fld.shape, dtype=fld.x.dtype) as d:
+        d.decode_device(dxp, streams, mm, out)  # warm-up (tables, first allocations)
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        ev0.record()
+        for _ in range(reps):
+            d.decode_device(dxp, streams, mm, out)
+        ev1.record()
+        torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1) / reps
+    nbytes = fld.x.nbytes
+    return {"ms": round(ms, 3), "GB/s_output": round(nbytes / (ms / 1e3) / 1e9, 2),
+            "symbols": int(sum(r.num_elements for r in streams if r is not None)),
+            "bitstream_bytes": int(sum(len(r.bitstream) for r in streams if r is not None))}
+
+
+def measure_modes(F, s, fld, e0_np, dx):
+    """Fused-pass time (first iteration, device events) and iterations of the
+    direct mode (one bound on every coefficient: the all-abs arithmetic) and
+    of the pointwise power-spectrum mode (delta_ptw = 0.05) on the field."""
+    H = fld.shape[0] * fld.shape[1] * (fld.shape[2] // 2 + 1)
+    res = {}
+    with F.ProjectionSolver(*fld.shape, dtype=fld.x.dtype) as m:
+        m.set_profiling(True)
+        m.initialize(fld.x, np.arange(H), np.full(H, fld.delta, fld.x.dtype), fld.eps)
+        it = m.solve(e0_np, 100, 1e-7)
+        res["direct"] = {"iterations": it, "fused_pass_ms": round(max(ms for ms, _ in m.pass_times()), 5)}
+        m.initialize_all_ptw(fld.x, fld.eps, 0.05)
+        it = m.solve_all_ptw(e0_np, 3, -1.0)
+        pt = m.pass_times()
+        res["all_ptw"] = {"iterations": it, "delta_ptw": 0.05,
+                          "passes_ms": [round(ms, 5) for ms, _ in pt]}
+    return res
 
 
 # --------------------------------------------------------------------------- batched form

@@ -11,7 +11,7 @@ namespace ffcz {
 
 // ------------------------------------------------------ Huffman decoding --
 // Segmented self-synchronising decode.  The bitstream is cut into segments
-// of kSegBits bits; each segment is decoded from an entry bit position up
+// of kSegBits bits (one thread each); each segment is decoded from an entry bit position up
 // to the first step boundary at or past the next segment's start.  Entry
 // positions are iterated to the fixed point of "entry[k] = end[k-1]"
 // (entry[0] = 0), which is the sequential decoder's path; a segment whose
@@ -19,42 +19,59 @@ namespace ffcz {
 // sequential decoder's: walk the code trie MSB-first from the step's first
 // bit; at the first leaf emit its symbol; where a bit has no child, the
 // stream ends, or 32 bits pass without a leaf, skip one bit.
-constexpr int kLutBits = 10;
-constexpr int kSegBits = 1024;
+constexpr int kLutBitsMax = 14;   // up to 2^14 table entries (64 KB of shared memory)
+constexpr int kSegBits = 512;
 
 // Device image of a code table: trie nodes (children for bit 0 / bit 1, -1
 // when absent), the symbol index of each node that ends a code (-1
-// otherwise), and a 2^kLutBits table of the walk over the next kLutBits
+// otherwise), and a 2^lut_bits table of the walk over the next lut_bits
 // bits: EMIT (symbol index, length), SKIP, or CONT (node reached after
-// kLutBits bits, no leaf on the way).
+// lut_bits bits, no leaf on the way).  lut_bits = the longest code, within
+// [8, kLutBitsMax], so that codes longer than the table are rare.
 struct DecodeTables {
   int nnodes = 0;
+  int lut_bits = 8;
   int2 *child = nullptr;
   int *leaf = nullptr;
   unsigned *lut = nullptr;
   uint32_t *symbols = nullptr;
 };
 
-// Builds the tables of (symbols, codes, lengths) on the host and uploads
-// them (codes of length 1..32; the first of duplicate codes wins, like the
-// host decoder).
-int decode_tables_build(const uint32_t *symbols, const uint32_t *codes, const int32_t *lengths, size_t nsym,
-                        DecodeTables &t);
-void decode_tables_free(DecodeTables &t);
+// Grow-only device scratch of a decoder (tables, staged bitstream, segment
+// state), so that repeated decodes allocate nothing once warm.
+struct DecodeWorkspace {
+  DecodeTables t;
+  size_t child_cap = 0, leaf_cap = 0, sym_cap = 0;  // elements
+  uint32_t *bits = nullptr;                          // staged bitstream
+  size_t bits_cap = 0;                               // bytes
+  long long *entry = nullptr, *end = nullptr;
+  unsigned long long *cnt = nullptr;
+  unsigned char *dirty = nullptr;
+  size_t seg_cap = 0;
+  int *changed = nullptr, *h_changed = nullptr;
+  unsigned long long *h_total = nullptr;
+  ~DecodeWorkspace();
+};
 
-// Decodes up to num_elements symbols of the nbytes-byte bitstream d_bits
-// (device, 4-byte aligned, readable and zero for 12 bytes past nbytes) into
-// d_out (symbol_bytes 1 or 2).  *decoded receives the count (fewer than
-// num_elements when the stream ends first).  Runs on `st`; synchronises it.
-int huff_decode_gpu(const uint32_t *d_bits, size_t nbytes, const DecodeTables &t, size_t num_elements,
-                    int symbol_bytes, void *d_out, size_t *decoded, cudaStream_t st);
+// Builds the tables of (symbols, codes, lengths) on the host and uploads
+// them into ws, with the host decoder's rules (codes of length 1..32 below
+// 2^length; the first of equal codes wins).
+int decode_tables_build(DecodeWorkspace &ws, const uint32_t *symbols, const uint32_t *codes, const int32_t *lengths,
+                        size_t nsym, cudaStream_t st);
+
+// Decodes up to num_elements symbols of the nbytes-byte bitstream ws.bits
+// into d_out (symbol_bytes 1 or 2).  *decoded receives the count (fewer
+// than num_elements when the stream ends first).  Runs on `st`;
+// synchronises it.
+int huff_decode_gpu(DecodeWorkspace &ws, size_t nbytes, size_t num_elements, int symbol_bytes, void *d_out,
+                    size_t *decoded, cudaStream_t st);
 
 // Table build + staging + decode of a bitstream in host (kind
 // cudaMemcpyHostToDevice) or device memory; returns after the stream
 // finished.
-int huff_decode_bits(const uint8_t *bits, size_t nbytes, cudaMemcpyKind kind, const uint32_t *symbols,
-                     const uint32_t *codes, const int32_t *lengths, size_t nsym, size_t num_elements,
-                     int symbol_bytes, void *d_out, size_t *decoded, void *stream);
+int huff_decode_bits(DecodeWorkspace &ws, const uint8_t *bits, size_t nbytes, cudaMemcpyKind kind,
+                     const uint32_t *symbols, const uint32_t *codes, const int32_t *lengths, size_t nsym,
+                     size_t num_elements, int symbol_bytes, void *d_out, size_t *decoded, void *stream);
 
 // -------------------------------------------------- edits from streams --
 constexpr int UP_THREADS = 128;              // one 32-bit flag word per thread

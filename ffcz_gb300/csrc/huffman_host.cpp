@@ -109,7 +109,9 @@ std::vector<uint32_t> huffman_decode(const uint8_t *bits, size_t nbytes, const u
   std::vector<int> child(2, -1), leaf(1, -1);
   for (size_t s = 0; s < nsym; ++s) {
     const int L = lengths[s];
-    if (L < 1 || L > 32) continue;
+    // the reference keys on (length, code): a stored code of 2^L or more
+    // never matches the L bits read
+    if (L < 1 || L > 32 || (L < 32 && (codes[s] >> L) != 0)) continue;
     int node = 0;
     for (int d = L - 1; d >= 0; --d) {
       const int bit = (codes[s] >> d) & 1u;

@@ -35,7 +35,10 @@ void build_codebook(const uint32_t *hist, size_t nbins, Codebook &cb);
 
 // Prefix decode of HuffmanZSTDCoder.cuh:394-449 over `bits` bytes: stops at
 // num_elements symbols or at the end of the stream; where no code of length
-// 1..32 matches, one bit is skipped.  Returns the decoded symbols.
+// 1..32 matches, one bit is skipped.  A stored code of 2^L or more never
+// matches (the reference keys on length << 32 | code); of entries with the
+// same (length, code) the first wins (the reference leaves this to its hash
+// map's iteration order).  Returns the decoded symbols.
 std::vector<uint32_t> huffman_decode(const uint8_t *bits, size_t nbytes, const uint32_t *symbols,
                                      const uint32_t *codes, const int32_t *lengths, size_t nsym,
                                      size_t num_elements);

@@ -117,6 +117,7 @@ struct ffcz_solver {
   long long launches = 0;
   int kernels_per_iter = 0;
   HuffWorkspace huff;
+  DecodeWorkspace dec;
   // per-pass timing of the first iteration (events recorded inside the graph)
   int profile = 0;
   int npass = 0;
@@ -1431,7 +1432,8 @@ int ffcz_solver_decode(ffcz_solver *s, const void *d_decomp, ffcz_huff_result *c
     if (!j.n) continue;
     const ffcz_huff_result *r = j.r;
     size_t got = 0;
-    FFCZ_TRY(huff_decode_bits(r->bitstream.data(), r->bitstream.size(), cudaMemcpyHostToDevice, r->symbols.data(),
+    FFCZ_TRY(huff_decode_bits(s->dec, r->bitstream.data(), r->bitstream.size(), cudaMemcpyHostToDevice,
+                              r->symbols.data(),
                               r->codes.data(), r->lengths.data(), r->symbols.size(), j.n, j.sb, j.dst, &got,
                               s->stream));
     if (got != j.n) return fail(FFCZ_ERR_INVALID, "a stream decodes to fewer symbols than it declares");

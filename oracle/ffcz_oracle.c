@@ -247,14 +247,30 @@ size_t orc_huff_pack(const uint32_t *data, size_t n, const uint32_t *lut_code, c
 }
 
 /* Reference decoder.  The (length, code) -> symbol table of
- * HuffmanZSTDCoder.cuh:395-402 is held as one code-sorted array per length
- * and searched by bisection.  Returns the number of decoded symbols
- * (<= num_elements). */
-typedef struct { uint32_t code; uint32_t sym; } CodeSym;
+ * HuffmanZSTDCoder.cuh:395-402 is held as one (code, table index)-sorted
+ * array per length and searched by bisection.  A code matches only the
+ * L-bit value it holds (stored codes of 2^L or more never match, as in the
+ * reference's (length << 32 | code) key).  Where two entries share a
+ * (length, code) key -- which the reference resolves by its hash map's
+ * iteration order -- the first table entry is taken.  Returns the number
+ * of decoded symbols (<= num_elements). */
+typedef struct { uint32_t code; uint32_t sym; size_t idx; } CodeSym;
 
 static int cs_cmp(const void *a, const void *b) {
-  const uint32_t x = ((const CodeSym *)a)->code, y = ((const CodeSym *)b)->code;
-  return x < y ? -1 : x > y;
+  const CodeSym *p = (const CodeSym *)a, *q = (const CodeSym *)b;
+  if (p->code != q->code) return p->code < q->code ? -1 : 1;
+  return p->idx < q->idx ? -1 : p->idx > q->idx;
+}
+
+/* first entry with this code (lower bound), or NULL */
+static const CodeSym *cs_find(const CodeSym *t, size_t n, uint32_t code) {
+  size_t lo = 0, hi = n;
+  while (lo < hi) {
+    const size_t mid = lo + (hi - lo) / 2;
+    if (t[mid].code < code) lo = mid + 1;
+    else hi = mid;
+  }
+  return (lo < n && t[lo].code == code) ? &t[lo] : NULL;
 }
 
 size_t orc_huff_decode(const uint8_t *bits, size_t nbytes, const uint32_t *sym, const uint32_t *code,
@@ -269,7 +285,7 @@ size_t orc_huff_decode(const uint8_t *bits, size_t nbytes, const uint32_t *sym, 
   }
   for (size_t s = 0; s < nsym; ++s)
     if (len[s] >= 1 && len[s] <= 32) {
-      CodeSym e = {code[s], sym[s]};
+      CodeSym e = {code[s], sym[s], s};
       tab[len[s]][cnt[len[s]]++] = e;
     }
   for (int L = 1; L <= 32; ++L) qsort(tab[L], cnt[L], sizeof(CodeSym), cs_cmp);
@@ -283,8 +299,7 @@ size_t orc_huff_decode(const uint8_t *bits, size_t nbytes, const uint32_t *sym, 
       const uint64_t p = pos + (uint64_t)(L - 1);
       c = (c << 1) | ((bits[p >> 3] >> (7 - (p & 7))) & 1u);
       if (!cnt[L]) continue;
-      CodeSym key = {c, 0};
-      const CodeSym *hit = (const CodeSym *)bsearch(&key, tab[L], cnt[L], sizeof(CodeSym), cs_cmp);
+      const CodeSym *hit = cs_find(tab[L], cnt[L], c);
       if (hit) {
         out[got++] = hit->sym;
         pos += (uint64_t)L;

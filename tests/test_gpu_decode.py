@@ -53,6 +53,13 @@ def test_garbage_bits_follow_the_sequential_rules(cuda):
         {"symbols": np.arange(5, dtype=np.uint32), "codes": np.array([0, 2, 6, 0x3FFFFFFF, 0xFFFFFFFE], np.uint32),
          "lengths": np.array([1, 2, 3, 30, 32], np.int32)},
         O.huffman_codebook(rng.geometric(0.1, 5000).astype(np.uint16)),
+        # not prefix-free: a code with a shorter code as prefix is never
+        # reached, duplicates resolve to the first, long codes share prefixes
+        {"symbols": np.arange(5, dtype=np.uint32), "codes": np.array([1, 2, 0, 0, 0], np.uint32),
+         "lengths": np.array([1, 2, 1, 1, 20], np.int32)},
+        {"symbols": np.arange(7, dtype=np.uint32),
+         "codes": np.array([0xFFFF, 0xFFFF, 0x3FFFF, 0x0001, 0b01, 0xFFFFFFFF, 0x7FFE], np.uint32),
+         "lengths": np.array([16, 16, 18, 16, 2, 32, 15], np.int32)},
     ]
     for book in tables:
         for n in (10, 100_000, 1_000_000):
