@@ -134,6 +134,7 @@ SIGNATURES = {
     "ffcz_init_direct": [_p, _p, _p, _p, _d, _sz],
     "ffcz_get_orig_spectrum": [_p, _p, _sz],
     "ffcz_verify_bounds": [_p, C.POINTER(C.c_double), C.POINTER(C.c_double)],
+    "ffcz_strict_finish": [_p, _i, _d, _i, _p, _p, _p, _p],
     "ffcz_solver_autotune": [_p, _i, _p],
     "ffcz_init_all_ptw": [_p, _p, _d, _d],
     "ffcz_init_all_ptw_device": [_p, _p, _d, _d],
@@ -295,6 +296,18 @@ class ProjectionSolver:
         a, b = C.c_double(), C.c_double()
         _check(lib().ffcz_verify_bounds(self._h, C.byref(a), C.byref(b)))
         return a.value, b.value
+
+    def strict_finish(self, max_iterations: int = 100, tol: float = 1e-7, max_rounds: int = 4) -> dict:
+        """Makes the last all-abs result meet both bounds in FP64 (clamp to
+        the largest value <= eps, FP64 check, re-runs on a shrunk frequency
+        box while a coefficient exceeds delta).  Returns rounds, met and the
+        FP64 maxima; iterations() is the total afterwards."""
+        r, m = C.c_int(), C.c_int()
+        a, b = C.c_double(), C.c_double()
+        _check(lib().ffcz_strict_finish(self._h, int(max_iterations), float(tol), int(max_rounds), C.byref(r),
+                                        C.byref(m), C.byref(a), C.byref(b)))
+        self._iters()
+        return {"rounds": r.value, "met": bool(m.value), "spatial_max": a.value, "freq_max": b.value}
 
     def get_orig_spectrum(self) -> np.ndarray:
         """The spectrum of x the pointwise modes compare against (H complex)."""

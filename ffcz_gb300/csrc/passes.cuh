@@ -448,12 +448,16 @@ __global__ void k_check(LoopCtl *ctl, T tol, int max_iter, cudaGraphConditionalH
   if (use_graph) cudaGraphSetConditional(h, cont ? 1u : 0u);
 }
 
+// Iteration count of a solve made of several loop runs (strict re-runs).
+static __global__ void k_set_iterations(LoopCtl *ctl, int n) { ctl->iterations = n; }
+
 // Spatial projection after the last iteration when the loop stopped without
-// converging (projection_algorithm_impl.cuh:851 on the final pass).
+// converging (projection_algorithm_impl.cuh:851 on the final pass); with ctl
+// NULL, on every element (the strict-bounds clamp).
 template <typename T>
 __global__ void k_final_clamp(T *__restrict__ e, T *__restrict__ sedits, T eps, long long n,
                               const LoopCtl *ctl) {
-  if (ctl->converged || ctl->iterations == 0) return;
+  if (ctl && (ctl->converged || ctl->iterations == 0)) return;  // ctl NULL: always
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x) {
     const T v = e[i];

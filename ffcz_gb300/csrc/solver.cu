@@ -43,6 +43,19 @@ struct GraphKey {
   }
 };
 
+// A captured loop and the key it was captured for.
+struct LoopGraph {
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  GraphKey key;
+  void reset() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    exec = nullptr;
+    graph = nullptr;
+  }
+};
+
 struct Launch {  // geometry of one pass
   unsigned grid = 0;
   int threads = 0;
@@ -109,10 +122,9 @@ struct ffcz_solver {
   ffcz_solver *verifier = nullptr;   // FP64 twin of ffcz_verify_bounds
   unsigned long long *d_vmax = nullptr;
   bool extracted = false;
-  // graph cache
-  cudaGraph_t graph = nullptr;
-  cudaGraphExec_t gexec = nullptr;
-  GraphKey gkey;
+  // the two most recently used loop graphs (a strict-bounds re-run on a
+  // shrunk box keeps the regular solve's graph)
+  LoopGraph lg[2];
   // bookkeeping
   long long launches = 0;
   int kernels_per_iter = 0;
@@ -523,11 +535,12 @@ int run_loop_graph(ffcz_solver *s, int pro, const void *a, const void *b, int ma
   key.delta_ptw = s->delta_ptw;
   key.mask = s->ptw_partial ? s->d_mask : nullptr;
   key.dc = s->ptw_dc;
-  if (!(s->gexec && s->gkey == key)) {
-    if (s->gexec) cudaGraphExecDestroy(s->gexec);
-    if (s->graph) cudaGraphDestroy(s->graph);
-    s->gexec = nullptr;
-    s->graph = nullptr;
+  if (!(s->lg[0].exec && s->lg[0].key == key)) {
+    std::swap(s->lg[0], s->lg[1]);
+  }
+  if (!(s->lg[0].exec && s->lg[0].key == key)) {
+    LoopGraph &lg = s->lg[0];
+    lg.reset();
     cudaStream_t cs = s->cap;
     FFCZ_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
     const int rc = capture_loop<T>(s, cs, pro, a, b, max_iter, tol, s->profile != 0);
@@ -538,11 +551,11 @@ int run_loop_graph(ffcz_solver *s, int pro, const void *a, const void *b, int ma
       return rc;
     }
     FFCZ_CUDA(e);
-    s->graph = g;
-    FFCZ_CUDA(cudaGraphInstantiate(&s->gexec, s->graph, 0));
-    s->gkey = key;
+    lg.graph = g;
+    FFCZ_CUDA(cudaGraphInstantiate(&lg.exec, lg.graph, 0));
+    lg.key = key;
   }
-  FFCZ_CUDA(cudaGraphLaunch(s->gexec, s->stream));
+  FFCZ_CUDA(cudaGraphLaunch(s->lg[0].exec, s->stream));
   return FFCZ_OK;
 }
 
@@ -639,8 +652,7 @@ int extract(ffcz_solver *s) {
 }
 
 void free_all(ffcz_solver *s) {
-  if (s->gexec) cudaGraphExecDestroy(s->gexec);
-  if (s->graph) cudaGraphDestroy(s->graph);
+  for (LoopGraph &g : s->lg) g.reset();
   void *bufs[] = {s->d_x, s->d_e, s->d_spec, s->d_fedits, s->d_sedits, s->d_fcompact, s->d_scompact,
                   s->d_fquant, s->d_squant, s->d_fpack, s->d_spack, s->d_tw, s->d_ctl, s->d_blk_cnt,
                   s->d_blk_mn, s->d_blk_mx, s->d_mnmx};
@@ -876,11 +888,8 @@ int autotune(ffcz_solver *s, int reps, double *ms6) {
   FFCZ_CUDA(cudaMemsetAsync(s->d_fedits, 0, 2 * s->H * s->es, st));
   FFCZ_CUDA(cudaMemsetAsync(s->d_sedits, 0, s->N * s->es, st));
   FFCZ_CUDA(cudaStreamSynchronize(st));
-  // the cached loop graph holds the previous kernels
-  if (s->gexec) cudaGraphExecDestroy(s->gexec);
-  if (s->graph) cudaGraphDestroy(s->graph);
-  s->gexec = nullptr;
-  s->graph = nullptr;
+  // the cached loop graphs hold the previous kernels
+  for (LoopGraph &g : s->lg) g.reset();
   ++s->kernel_gen;
   for (int i = 0; i < 6; ++i) s->tune_ms[i] = t[i];
   if (ms6)
@@ -889,6 +898,53 @@ int autotune(ffcz_solver *s, int reps, double *ms6) {
 }
 
 }  // namespace
+
+// Strict bounds after an all-abs solve (ffcz_strict_finish in ffcz.h):
+// clamp to the largest T <= eps, FP64 check, re-runs on a shrunk frequency
+// box while a coefficient exceeds delta.
+template <typename T>
+int strict_finish(ffcz_solver *s, int max_iter, double tol, int max_rounds, int *rounds, int *met, double *smax,
+                  double *fmax) {
+  if (!s->initialized || !s->abs_ready) return fail(FFCZ_ERR_NOT_INITIALIZED, "Solver not initialized");
+  if (s->cmode != CLAMP_ABS) return fail(FFCZ_ERR_INVALID, "strict bounds follow an all-abs solve");
+  if (max_rounds < 0 || max_iter < 1) return fail(FFCZ_ERR_INVALID, "max_rounds < 0 or max_iter < 1");
+  Range rg("ffcz:strict_finish");
+  const double E = s->eps, D = s->delta;
+  T Et = (T)E;
+  if ((double)Et > E) Et = std::nextafter(Et, T(0));
+  const bool was_extracted = s->extracted;
+  cudaStream_t st = s->stream;
+  const unsigned g = (unsigned)std::min<size_t>(ceil_div(s->N, 256), 152 * 16);
+  int total = s->h_ctl->iterations, r = 0, rc = FFCZ_OK;
+  double sm = 0.0, fm = 0.0, dt = D;
+  for (;;) {
+    k_final_clamp<T><<<g, 256, 0, st>>>(tp<T>(s->d_e), tp<T>(s->d_sedits), Et, (long long)s->N, nullptr);
+    FFCZ_CUDA(cudaGetLastError());
+    s->extracted = false;
+    if ((rc = ffcz_verify_bounds(s, &sm, &fm)) != FFCZ_OK) break;
+    if ((sm <= E && fm <= D) || r == max_rounds) break;
+    dt -= 2.0 * (fm - D);  // twice the worst overshoot of the last check
+    if (!(dt > 0.0)) break;
+    s->delta = dt;
+    rc = project<T>(s, PRO_PLAIN, s->d_e, nullptr, max_iter, tol);
+    s->delta = D;
+    if (rc != FFCZ_OK) break;
+    total += s->h_ctl->iterations;
+    ++r;
+  }
+  s->delta = D;
+  if (rc != FFCZ_OK) return rc;
+  k_set_iterations<<<1, 1, 0, st>>>(s->d_ctl, total);
+  FFCZ_CUDA(cudaGetLastError());
+  s->h_ctl->iterations = total;
+  if (was_extracted) FFCZ_TRY(extract<T>(s));
+  else FFCZ_CUDA(cudaStreamSynchronize(st));
+  if (rounds) *rounds = r;
+  if (met) *met = (sm <= E && fm <= D) ? 1 : 0;
+  if (smax) *smax = sm;
+  if (fmax) *fmax = fm;
+  return FFCZ_OK;
+}
 
 #define DISPATCH(s, fn, ...) ((s)->dtype == FFCZ_F32 ? fn<float>(__VA_ARGS__) : fn<double>(__VA_ARGS__))
 
@@ -1343,6 +1399,12 @@ int ffcz_verify_bounds(ffcz_solver *s, double *spatial_max, double *freq_max) {
   std::memcpy(spatial_max, &h[0], 8);
   std::memcpy(freq_max, &h[1], 8);
   return FFCZ_OK;
+}
+
+int ffcz_strict_finish(ffcz_solver *s, int max_iter, double tol, int max_rounds, int *rounds, int *met,
+                       double *spatial_max, double *freq_max) {
+  FFCZ_TRY(check_solver(s));
+  return DISPATCH(s, strict_finish, s, max_iter, tol, max_rounds, rounds, met, spatial_max, freq_max);
 }
 
 int ffcz_get_orig_spectrum(ffcz_solver *s, void *h_dst, size_t cap_complex) {

@@ -215,6 +215,22 @@ int ffcz_solver_autotune(ffcz_solver *s, int reps, double *ms6);
  * over the half spectrum.  The all-abs bounds hold when spatial_max <= eps
  * (+ the loop's tol) and freq_max <= delta. */
 int ffcz_verify_bounds(ffcz_solver *s, double *spatial_max, double *freq_max);
+/* Strict bounds (an addition; the reference stops once the spatial
+ * violation is below tol, impl:845-848, so its e may exceed eps by up to tol
+ * and meets delta only up to the FFT's rounding).  After an all-abs solve:
+ *   1. e is clamped to E_T, the largest value of the solver's type <= eps
+ *      (clamps recorded in the spatial edits);
+ *   2. both bounds are checked in FP64 (ffcz_verify_bounds);
+ *   3. while some |Re/Im F(e)_k| > delta, the loop runs again from the
+ *      current e (max_iter, tol) on a frequency box shrunk by twice the worst
+ *      overshoot (frequency edits accumulate as usual), then 1-2 again; at
+ *      most max_rounds times.
+ * Afterwards the iteration count is the total, and the compaction is redone
+ * when the solve had extracted.  *met = 1 when spatial_max <= eps and
+ * freq_max <= delta in FP64, eps and delta as the solver holds them (rounded
+ * to its type at initialisation).  Any out pointer may be NULL. */
+int ffcz_strict_finish(ffcz_solver *s, int max_iter, double tol, int max_rounds, int *rounds, int *met,
+                       double *spatial_max, double *freq_max);
 /* The spectrum of x of the pointwise modes (d_orig_freq, impl:612-623):
  * H interleaved complex values of the solver's dtype. */
 int ffcz_get_orig_spectrum(ffcz_solver *s, void *h_dst, size_t cap_complex);
