@@ -1,7 +1,10 @@
 // Edit compaction (projection_algorithm_impl.cuh:371-456 and
-// projection_algorithm.cu:365-379, 382-405, 427-457, 459-550), in three
-// launches per accumulator instead of the reference's flag kernels, two CUB
-// reductions, a CUB scan, the scatter kernel and two bool-pack kernels:
+// projection_algorithm.cu:365-379, 382-405, 427-457, 459-550) instead of the
+// reference's flag kernels, two CUB reductions, a CUB scan, the scatter
+// kernel and two bool-pack kernels.  The solver uses the single-read form
+// further down (k_ex_part + k_ex_place); the three-launch form below
+// serves the no-allocation entry point, whose caller-provided scratch has no
+// room for the compacted values:
 //   k_ex_stats   : per 4096-element chunk: #(|v| > thr), min, max   (R n*s)
 //   k_ex_scan    : one block: chunk offsets (exclusive scan), global
 //                  min/max, active count                        (tiny)
@@ -245,6 +248,290 @@ __global__ void __launch_bounds__(EX_THREADS) k_ex_compact(
       compact[pos] = v[t];
       quant[pos] = quantize16<T>(v[t], mn, mx);
       ++pos;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Single-read compaction (the solver's path): three launches per
+// accumulator, the edit array read once.  A chunk is the span of one warp (8
+// coalesced 16-byte loads per lane: 1024 FP32 / 512 FP64 values), a group
+// the 8 chunks of one block.
+//   k_ex_part     : warp = chunk: flag words (shuffles), lane offsets of the
+//                   active values (three ballots of the per-lane counts),
+//                   the active values compacted into scratch at the chunk's
+//                   own start, the chunk's count; per block a group record
+//                   (count, min and max as order-preserving integer keys)
+//                                                  (R n*s, W cnt*s + n/8)
+//   k_ex_scan_rec : one block: exclusive offsets of the groups, whole-array
+//                   count, min and max
+//   k_ex_place    : one warp per chunk moves the chunk's values to their
+//                   final positions and quantises them (R cnt*s, W cnt*(s+2))
+// Group records are struct-of-arrays padded to a multiple of XP_PAD groups;
+// the padding keeps its initial neutral values (count 0, min key ~0, max
+// key 0), so the scan reads whole 16-byte vectors.
+constexpr int XP_NQ = 8;                 // 16-byte loads per lane
+constexpr int XP_WPG = EX_THREADS / 32;  // chunks (warps) per group (block)
+template <typename T> __host__ __device__ constexpr int xp_vec() { return 16 / (int)sizeof(T); }
+template <typename T> __host__ __device__ constexpr int xp_chunk() { return 32 * XP_NQ * xp_vec<T>(); }
+template <typename T> __host__ __device__ constexpr int xp_group() { return XP_WPG * xp_chunk<T>(); }
+constexpr int XP_PAD = 4096;
+
+struct ExRec {
+  unsigned *wcnt;                       // per chunk
+  unsigned *cnt;                        // per group
+  unsigned long long *kmn, *kmx, *off;  // per group
+};
+
+template <typename T> __device__ __forceinline__ unsigned long long ord_key(T v);
+template <> __device__ __forceinline__ unsigned long long ord_key<float>(float v) {
+  const unsigned u = __float_as_uint(v);
+  return (unsigned long long)(u ^ ((u >> 31) ? 0xffffffffu : 0x80000000u));
+}
+template <> __device__ __forceinline__ unsigned long long ord_key<double>(double v) {
+  const unsigned long long u = (unsigned long long)__double_as_longlong(v);
+  return u ^ ((u >> 63) ? ~0ull : 0x8000000000000000ull);
+}
+template <typename T> __device__ __forceinline__ T key_val(unsigned long long k);
+template <> __device__ __forceinline__ float key_val<float>(unsigned long long k) {
+  const unsigned u = (unsigned)k;
+  return __uint_as_float(u ^ ((u >> 31) ? 0x80000000u : 0xffffffffu));
+}
+template <> __device__ __forceinline__ double key_val<double>(unsigned long long k) {
+  return __longlong_as_double((long long)(k ^ ((k >> 63) ? 0x8000000000000000ull : ~0ull)));
+}
+
+// One chunk of one warp; FULL: every value of the chunk lies below n.
+// Returns the chunk's active count (the same in every lane).
+template <typename T, bool FULL>
+__device__ __forceinline__ unsigned ex_chunk(const T *__restrict__ a, long long n, long long base, T thr,
+                                             T *__restrict__ dst, unsigned *__restrict__ pack_words,
+                                             int write_pack, T &mn, T &mx, bool &any) {
+  constexpr int VEC = xp_vec<T>(), SPAN = 32 * VEC;
+  constexpr int LPW = 32 / VEC;  // lanes per 32-bit flag word
+  const int lane = threadIdx.x & 31;
+  T v[XP_NQ][VEC];
+  unsigned f[XP_NQ];
+#pragma unroll
+  for (int q = 0; q < XP_NQ; ++q) {
+    const long long i = base + q * SPAN + lane * VEC;
+    if (FULL || i + VEC <= n) {
+      if constexpr (VEC == 4) {
+        const float4 t = *reinterpret_cast<const float4 *>(a + i);
+        v[q][0] = t.x;
+        v[q][1] = t.y;
+        v[q][2] = t.z;
+        v[q][3] = t.w;
+      } else {
+        const double2 t = *reinterpret_cast<const double2 *>(a + i);
+        v[q][0] = t.x;
+        v[q][1] = t.y;
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < VEC; ++j) v[q][j] = (i + j < n) ? a[i + j] : T(0);
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < XP_NQ; ++q) {
+    const long long i = base + q * SPAN + lane * VEC;
+    unsigned bits = 0;
+#pragma unroll
+    for (int j = 0; j < VEC; ++j) {
+      const T x = v[q][j];
+      if (FULL || i + j < n) {
+        bits |= (fabs(x) > thr) ? 1u << j : 0u;
+        mn = fmin(mn, x);
+        mx = fmax(mx, x);
+      }
+    }
+    if (!FULL && i < n) any = true;
+    f[q] = bits;
+    // flag word of the 32 values [base + q*SPAN + 32*(lane/LPW), +32)
+    unsigned w = bits << (VEC * (lane % LPW));
+#pragma unroll
+    for (int o = 1; o < LPW; o <<= 1) w |= __shfl_xor_sync(0xffffffffu, w, o);
+    if (write_pack && lane % LPW == 0 && (FULL || i < n)) pack_words[i >> 5] = w;
+  }
+  if (FULL) any = true;
+  // offsets: values of the chunk in element order (q, lane, j)
+  const unsigned lt = (1u << lane) - 1u;
+  unsigned run = 0;
+#pragma unroll
+  for (int q = 0; q < XP_NQ; ++q) {
+    const unsigned k = __popc(f[q]);  // 0 .. VEC (<= 4)
+    const unsigned b0 = __ballot_sync(0xffffffffu, k & 1u), b1 = __ballot_sync(0xffffffffu, k & 2u),
+                   b2 = __ballot_sync(0xffffffffu, k & 4u);
+    if (b0 | b1 | b2) {
+      if (f[q]) {
+        T *d = dst + run + __popc(b0 & lt) + 2u * __popc(b1 & lt) + 4u * __popc(b2 & lt);
+#pragma unroll
+        for (int j = 0; j < VEC; ++j)
+          if (f[q] & (1u << j)) *d++ = v[q][j];
+      }
+      run += __popc(b0) + 2u * __popc(b1) + 4u * __popc(b2);
+    }
+  }
+  return run;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(EX_THREADS, 3) k_ex_part(const T *__restrict__ a, long long n, long long nchunk, T thr,
+                                                        T *__restrict__ scratch, ExRec rec,
+                                                        unsigned *__restrict__ pack_words, int write_pack) {
+  constexpr int CH = xp_chunk<T>();
+  __shared__ unsigned scnt[XP_WPG];
+  __shared__ unsigned long long smn[XP_WPG], smx[XP_WPG];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const long long c = (long long)blockIdx.x * XP_WPG + warp;
+  T mn = dev_inf<T>(), mx = -dev_inf<T>();
+  bool any = false;
+  unsigned run = 0;
+  if (c < nchunk) {
+    const long long base = c * CH;
+    if (base + CH <= n)
+      run = ex_chunk<T, true>(a, n, base, thr, scratch + base, pack_words, write_pack, mn, mx, any);
+    else
+      run = ex_chunk<T, false>(a, n, base, thr, scratch + base, pack_words, write_pack, mn, mx, any);
+  }
+  unsigned long long kmn = any ? ord_key<T>(mn) : ~0ull, kmx = any ? ord_key<T>(mx) : 0ull;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long p = __shfl_xor_sync(0xffffffffu, kmn, o);
+    const unsigned long long q = __shfl_xor_sync(0xffffffffu, kmx, o);
+    kmn = p < kmn ? p : kmn;
+    kmx = q > kmx ? q : kmx;
+  }
+  if (lane == 0) {
+    if (c < nchunk) rec.wcnt[c] = run;
+    scnt[warp] = run;
+    smn[warp] = kmn;
+    smx[warp] = kmx;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned t = 0;
+    for (int w = 0; w < XP_WPG; ++w) {
+      t += scnt[w];
+      kmn = smn[w] < kmn ? smn[w] : kmn;
+      kmx = smx[w] > kmx ? smx[w] : kmx;
+    }
+    rec.cnt[blockIdx.x] = t;
+    rec.kmn[blockIdx.x] = kmn;
+    rec.kmx[blockIdx.x] = kmx;
+  }
+}
+
+// One block of XS_THREADS: thread t scans the group records [t*K, (t+1)*K)
+// (K a multiple of 4, 16-byte vector loads) into exclusive offsets; the
+// whole-array count, min and max go to mnmx and ctl slot `which`.
+constexpr int XS_THREADS = 1024;
+template <typename T>
+__global__ void __launch_bounds__(XS_THREADS) k_ex_scan_rec(long long ngroup, ExRec rec, T *__restrict__ mnmx,
+                                                            LoopCtl *__restrict__ ctl, int which) {
+  constexpr int NW = XS_THREADS / 32;
+  __shared__ unsigned long long wa[NW], wb[NW], wc[NW];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const long long K = (ngroup + XP_PAD - 1) / XP_PAD * (XP_PAD / XS_THREADS);
+  const long long r0 = threadIdx.x * K;
+  unsigned long long sum = 0, kmn = ~0ull, kmx = 0ull;
+#pragma unroll 4
+  for (long long r = r0; r < r0 + K; r += 4) {
+    const uint4 c4 = *reinterpret_cast<const uint4 *>(rec.cnt + r);
+    const ulonglong2 m0 = *reinterpret_cast<const ulonglong2 *>(rec.kmn + r);
+    const ulonglong2 m1 = *reinterpret_cast<const ulonglong2 *>(rec.kmn + r + 2);
+    const ulonglong2 x0 = *reinterpret_cast<const ulonglong2 *>(rec.kmx + r);
+    const ulonglong2 x1 = *reinterpret_cast<const ulonglong2 *>(rec.kmx + r + 2);
+    sum += (unsigned long long)c4.x + c4.y + c4.z + c4.w;
+    kmn = min(kmn, min(min(m0.x, m0.y), min(m1.x, m1.y)));
+    kmx = max(kmx, max(max(x0.x, x0.y), max(x1.x, x1.y)));
+  }
+  unsigned long long xs = sum;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned long long y = __shfl_up_sync(0xffffffffu, xs, o);
+    if (lane >= o) xs += y;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long p = __shfl_xor_sync(0xffffffffu, kmn, o);
+    const unsigned long long q = __shfl_xor_sync(0xffffffffu, kmx, o);
+    kmn = p < kmn ? p : kmn;
+    kmx = q > kmx ? q : kmx;
+  }
+  if (lane == 31) wc[warp] = xs;
+  if (lane == 0) {
+    wa[warp] = kmn;
+    wb[warp] = kmx;
+  }
+  __syncthreads();
+  unsigned long long off = xs - sum, tot = 0;
+  for (int w = 0; w < NW; ++w) {
+    off += w < warp ? wc[w] : 0ull;
+    tot += wc[w];
+  }
+#pragma unroll 4
+  for (long long r = r0; r < r0 + K; r += 4) {
+    const uint4 c4 = *reinterpret_cast<const uint4 *>(rec.cnt + r);
+    ulonglong2 o0, o1;
+    o0.x = off;
+    o0.y = o0.x + c4.x;
+    o1.x = o0.y + c4.y;
+    o1.y = o1.x + c4.z;
+    off = o1.y + c4.w;
+    *reinterpret_cast<ulonglong2 *>(rec.off + r) = o0;
+    *reinterpret_cast<ulonglong2 *>(rec.off + r + 2) = o1;
+  }
+  if (threadIdx.x == 0) {
+    kmn = wa[0];
+    kmx = wb[0];
+    for (int w = 1; w < NW; ++w) {
+      kmn = wa[w] < kmn ? wa[w] : kmn;
+      kmx = wb[w] > kmx ? wb[w] : kmx;
+    }
+    const T gmn = key_val<T>(kmn), gmx = key_val<T>(kmx);
+    mnmx[0] = gmn;
+    mnmx[1] = gmx;
+    ctl->count[which] = tot;
+    ctl->mn[which] = (double)gmn;
+    ctl->mx[which] = (double)gmx;
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(EX_THREADS) k_ex_place(const T *__restrict__ scratch, long long nchunk, ExRec rec,
+                                                         T *__restrict__ compact, uint16_t *__restrict__ quant,
+                                                         const T *__restrict__ mnmx) {
+  constexpr int CH = xp_chunk<T>();
+  const int lane = threadIdx.x & 31;
+  const long long wpb = EX_THREADS / 32;
+  const T mn = mnmx[0], mx = mnmx[1];
+  for (long long c = blockIdx.x * wpb + (threadIdx.x >> 5); c < nchunk; c += gridDim.x * wpb) {
+    const long long g = c / XP_WPG;
+    const int me = (int)(c - g * XP_WPG);
+    // lane l < XP_WPG holds the count of chunk g*XP_WPG + l (chunks past the
+    // end count 0)
+    const unsigned wc = (lane < XP_WPG && g * XP_WPG + lane < nchunk) ? rec.wcnt[g * XP_WPG + lane] : 0u;
+    unsigned before = lane < me ? wc : 0u;
+#pragma unroll
+    for (int o = 1; o < XP_WPG; o <<= 1) before += __shfl_xor_sync(0xffffffffu, before, o);
+    before = __shfl_sync(0xffffffffu, before, 0);  // the sum sits in lanes 0 .. XP_WPG-1
+    const long long cnt = (long long)__shfl_sync(0xffffffffu, wc, me);
+    if (!cnt) continue;
+    const unsigned long long off = rec.off[g] + before;
+    const T *src = scratch + c * CH;
+    // four loads in flight per lane
+    for (long long r = lane; r < cnt; r += 128) {
+      T v[4];
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+        if (r + 32 * k < cnt) v[k] = src[r + 32 * k];
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+        if (r + 32 * k < cnt) {
+          compact[off + r + 32 * k] = v[k];
+          quant[off + r + 32 * k] = quantize16<T>(v[k], mn, mx);
+        }
     }
   }
 }

@@ -84,8 +84,8 @@ struct ffcz_solver {
   size_t fpack_bytes = 0, spack_bytes = 0;  // allocated (multiple of 4)
   void *d_tw = nullptr;
   LoopCtl *d_ctl = nullptr, *h_ctl = nullptr;
-  unsigned *d_blk_cnt = nullptr;
-  void *d_blk_mn = nullptr, *d_blk_mx = nullptr, *d_mnmx = nullptr;
+  unsigned long long *d_ex_rec = nullptr;  // compaction: chunk records of both accumulators
+  void *d_mnmx = nullptr;
   size_t nblk_max = 0;
   unsigned long long *d_up_blk = nullptr;  // decoder: set flags per chunk (lazy)
   // plans
@@ -601,19 +601,43 @@ int project(ffcz_solver *s, int pro, const void *a, const void *b, int max_iter,
   return FFCZ_OK;
 }
 
+// Record arrays of the single-read compaction, accumulator `which`: chunk
+// counts, then the group counts, min keys, max keys and offsets, padded to a
+// multiple of XP_PAD groups; the frequency accumulator's first, then the
+// spatial one's.
+static size_t xp_pad(size_t ngroup) { return round_up(std::max<size_t>(ngroup, 1), (size_t)XP_PAD); }
+static size_t xp_words(size_t ngroup) {  // 64-bit words: (XP_WPG + 1) x u32 + 3 x u64 per padded group
+  return xp_pad(ngroup) * XP_WPG / 2 + xp_pad(ngroup) / 2 + 3 * xp_pad(ngroup);
+}
+static ExRec xp_rec(unsigned long long *base, size_t gf, size_t gs, int which) {
+  unsigned long long *p = base + (which ? xp_words(gf) : 0);
+  const size_t P = xp_pad(which ? gs : gf);
+  ExRec r;
+  r.wcnt = reinterpret_cast<unsigned *>(p);
+  r.cnt = reinterpret_cast<unsigned *>(p + P * XP_WPG / 2);
+  r.kmn = p + P * XP_WPG / 2 + P / 2;
+  r.kmx = r.kmn + P;
+  r.off = r.kmx + P;
+  return r;
+}
+template <typename T>
+size_t xp_groups(size_t n) { return ceil_div(n, (size_t)xp_group<T>()); }
+
 template <typename T>
 int extract_one(ffcz_solver *s, cudaStream_t st, const T *a, size_t n, int which, T *compact, uint16_t *quant,
                 uint8_t *pack, size_t pack_alloc) {
   const T thr = T(1e-7);
-  const size_t nblk = ceil_div(n, (size_t)EX_CHUNK);
+  const size_t nchunk = ceil_div(n, (size_t)xp_chunk<T>()), ngroup = xp_groups<T>(n);
   T *mnmx = (T *)s->d_mnmx + 2 * which;
-  k_ex_stats<T><<<(unsigned)nblk, EX_THREADS, 0, st>>>(a, (long long)n, thr, s->d_blk_cnt, (T *)s->d_blk_mn,
-                                                       (T *)s->d_blk_mx);
-  k_ex_scan<T><<<1, 1024, 0, st>>>(s->d_blk_cnt, (long long)nblk, (const T *)s->d_blk_mn,
-                                   (const T *)s->d_blk_mx, mnmx, s->d_ctl, which);
+  const ExRec rec = xp_rec(s->d_ex_rec, xp_groups<T>(2 * s->H), xp_groups<T>(s->N), which);
+  // the spectrum buffer (>= n values of T) is idle once the loop has ended
+  T *scratch = (T *)s->d_spec;
   const int correct = s->pack_mode == FFCZ_PACK_CORRECT;
-  k_ex_compact<T><<<(unsigned)nblk, EX_THREADS, 0, st>>>(a, (long long)n, thr, s->d_blk_cnt, mnmx, compact, quant,
-                                                         (unsigned *)pack, correct);
+  k_ex_part<T><<<(unsigned)ngroup, EX_THREADS, 0, st>>>(a, (long long)n, (long long)nchunk, thr, scratch, rec,
+                                                        (unsigned *)pack, correct);
+  k_ex_scan_rec<T><<<1, XS_THREADS, 0, st>>>((long long)ngroup, rec, mnmx, s->d_ctl, which);
+  const unsigned gp = (unsigned)std::min<size_t>(ceil_div(nchunk, (size_t)(EX_THREADS / 32)), 152 * 8);
+  k_ex_place<T><<<gp, EX_THREADS, 0, st>>>(scratch, (long long)nchunk, rec, compact, quant, mnmx);
   s->launches += 3;
   if (!correct) {
     const unsigned g = (unsigned)std::min<size_t>(ceil_div(pack_alloc, 256), 152 * 16);
@@ -622,6 +646,20 @@ int extract_one(ffcz_solver *s, cudaStream_t st, const T *a, size_t n, int which
   }
   FFCZ_CUDA(cudaGetLastError());
   return FFCZ_OK;
+}
+
+// Neutral records (count 0, min key ~0, max key 0, offset 0); the padding
+// keeps these values for good.
+static cudaError_t xp_init(ffcz_solver *s) {
+  const bool f32 = s->dtype == FFCZ_F32;
+  const size_t gf = f32 ? xp_groups<float>(2 * s->H) : xp_groups<double>(2 * s->H);
+  const size_t gs = f32 ? xp_groups<float>(s->N) : xp_groups<double>(s->N);
+  cudaError_t e = cudaMemset(s->d_ex_rec, 0, (xp_words(gf) + xp_words(gs)) * 8);
+  for (int w = 0; w < 2 && e == cudaSuccess; ++w) {
+    const ExRec r = xp_rec(s->d_ex_rec, gf, gs, w);
+    e = cudaMemset(r.kmn, 0xff, xp_pad(w ? gs : gf) * 8);
+  }
+  return e;
 }
 
 template <typename T>
@@ -654,8 +692,8 @@ int extract(ffcz_solver *s) {
 void free_all(ffcz_solver *s) {
   for (LoopGraph &g : s->lg) g.reset();
   void *bufs[] = {s->d_x, s->d_e, s->d_spec, s->d_fedits, s->d_sedits, s->d_fcompact, s->d_scompact,
-                  s->d_fquant, s->d_squant, s->d_fpack, s->d_spack, s->d_tw, s->d_ctl, s->d_blk_cnt,
-                  s->d_blk_mn, s->d_blk_mx, s->d_mnmx};
+                  s->d_fquant, s->d_squant, s->d_fpack, s->d_spack, s->d_tw, s->d_ctl, s->d_ex_rec,
+                  s->d_mnmx};
   for (void *p : bufs)
     if (p) cudaFree(p);
   if (s->d_up_blk) cudaFree(s->d_up_blk);
@@ -1000,9 +1038,10 @@ int ffcz_solver_create(size_t nx, size_t ny, size_t nz, int dtype, ffcz_solver *
   if (rc == FFCZ_OK) rc = alloc((void **)&s->d_fpack, s->fpack_bytes);
   if (rc == FFCZ_OK) rc = alloc((void **)&s->d_spack, s->spack_bytes);
   if (rc == FFCZ_OK) rc = alloc((void **)&s->d_ctl, sizeof(LoopCtl));
-  if (rc == FFCZ_OK) rc = alloc((void **)&s->d_blk_cnt, s->nblk_max * sizeof(unsigned));
-  if (rc == FFCZ_OK) rc = alloc(&s->d_blk_mn, s->nblk_max * es);
-  if (rc == FFCZ_OK) rc = alloc(&s->d_blk_mx, s->nblk_max * es);
+  const bool xf32 = s->dtype == FFCZ_F32;
+  const size_t nrec = xp_words(xf32 ? xp_groups<float>(H2) : xp_groups<double>(H2)) +
+                      xp_words(xf32 ? xp_groups<float>(N) : xp_groups<double>(N));
+  if (rc == FFCZ_OK) rc = alloc((void **)&s->d_ex_rec, nrec * sizeof(unsigned long long));
   if (rc == FFCZ_OK) rc = alloc(&s->d_mnmx, 4 * es);
   if (rc == FFCZ_OK) {
     cudaError_t e = cudaMallocHost(&s->h_ctl, sizeof(LoopCtl));
@@ -1019,6 +1058,7 @@ int ffcz_solver_create(size_t nx, size_t ny, size_t nz, int dtype, ffcz_solver *
     if (e == cudaSuccess) e = cudaMemset(s->d_spack, 0, s->spack_bytes);
     if (e == cudaSuccess) e = cudaMemset(s->d_fedits, 0, H2 * es);
     if (e == cudaSuccess) e = cudaMemset(s->d_sedits, 0, N * es);
+    if (e == cudaSuccess) e = xp_init(s.get());
     if (e != cudaSuccess) rc = cuda_fail(e, "cudaMemset", __FILE__, __LINE__);
   }
   if (rc != FFCZ_OK) {
