@@ -57,8 +57,12 @@ __host__ __device__ constexpr int mx_r(int L, int s) { return (int)((mx_list(L) 
 
 // Power-of-two stage lists.  Strided passes (CAP 16): 16:[16] 32:[8,4]
 // 64:[8,8] 128:[16,8] 256:[16,16] 512:[8,8,8] 1024:[16,8,8] 2048:[16,16,8]
-// 4096:[16,16,16].  z passes (CAP 8, 16+ threads per row): radix-8 stages
-// then one radix 4 or 2 stage for the remainder.
+// 4096:[16,16,16].  CAP 17, the plain forward / inverse strided passes: the
+// same except 512:[16,16,2] (16 values per thread, 16-column tiles: y passes
+// at 512^3 0.286 -> 0.242 ms, while the fused pass, two transforms per
+// tile, is faster on [8,8,8]: 0.451 vs 0.483 ms).  z passes (CAP 8, 16+
+// threads per row): radix-8 stages then one radix 4 or 2 stage for the
+// remainder.
 __host__ __device__ constexpr int rp_nst(int L, int cap = 16) {
   return mx_list(L) ? mx_nst(L)
        : cap == 8 ? (ilog2(L) / 3 + (ilog2(L) % 3 ? 1 : 0))
@@ -80,7 +84,7 @@ __host__ __device__ constexpr int rp_radix(int L, int s, int cap = 16) {
 #else
        : L == 256 ? 16
 #endif
-       : L == 512 ? 8
+       : L == 512 ? (cap == 17 ? (s < 2 ? 16 : 2) : 8)
        : L == 1024 ? (s == 0 ? 16 : 8)
        : L == 2048 ? (s < 2 ? 16 : 8)
        : 16;
@@ -89,7 +93,7 @@ __host__ __device__ constexpr int rp_elems(int L, int cap = 16) {
 #ifdef FFCZ_L256_R8
   return mx_list(L) ? mx_E(L) : cap == 8 ? 8 : ((L == 32 || L == 64 || L == 256 || L == 512) ? 8 : 16);
 #else
-  return mx_list(L) ? mx_E(L) : cap == 8 ? 8 : ((L == 32 || L == 64 || L == 512) ? 8 : 16);
+  return mx_list(L) ? mx_E(L) : cap == 8 ? 8 : ((L == 32 || L == 64 || (L == 512 && cap != 17)) ? 8 : 16);
 #endif
 }
 // radix of stage s in direction DIR (inverse = reversed list)
@@ -104,7 +108,9 @@ __host__ __device__ constexpr int rp_ns(int L, int dir, int s, int cap = 16) {
 // that a butterfly's R-1 twiddles are 16-byte aligned and read in pairs:
 // there a warp's lanes share few twiddle rows.  Odd radices and the z
 // passes (whose lanes each need a different row) keep R-1 per k.
-__host__ __device__ constexpr bool tw_paired(int cap, int R) { return cap == 16 && R % 2 == 0; }
+__host__ __device__ constexpr bool tw_paired(int cap, int R) { return cap != 8 && R % 2 == 0; }
+// Stage-list family of the plain (forward / inverse) strided passes.
+__host__ __device__ constexpr int plain_cap(int L) { return L == 512 ? 17 : 16; }
 
 // Prime-factor butterfly of length N1*N2 (coprime): input n = (N2 n1 + N1 n2)
 // mod N, N2 transforms of length N1, N1 of length N2, output at
@@ -346,13 +352,12 @@ __host__ __device__ constexpr int strided_minb(int es, int nt, int E) {
 // ---------------------------------------------------------------------------
 // Strided C2C pass.  Block = TC threads per column x TW columns (c fastest
 // across lanes, so each row access is TW contiguous complex values).
-template <typename T, int MODE, int L, int LGTW>
-__global__ void __launch_bounds__((L / rp_elems(L)) << LGTW,
-                                  strided_minb(sizeof(T), (L / rp_elems(L)) << LGTW, rp_elems(L))) ks_strided(c2<T> *__restrict__ spec, SArgs s,
-                                                                        AxisPlan p, ClampArgs<T> ca,
-                                                                        T *__restrict__ fedits, long long H) {
+template <typename T, int MODE, int L, int LGTW, int CAP = 16>
+__global__ void __launch_bounds__((L / rp_elems(L, CAP)) << LGTW,
+                                  strided_minb(sizeof(T), (L / rp_elems(L, CAP)) << LGTW, rp_elems(L, CAP)))
+    ks_strided(c2<T> *__restrict__ spec, SArgs s, AxisPlan p, ClampArgs<T> ca, T *__restrict__ fedits, long long H) {
   using V = c2<T>;
-  constexpr int E = rp_elems(L), TW = 1 << LGTW;
+  constexpr int E = rp_elems(L, CAP), TW = 1 << LGTW;
   using LY = ColLayout<sl_p(L, TW, sizeof(T)), sl_b(L, TW, sizeof(T))>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   V *buf = reinterpret_cast<V *>(smem_raw);
@@ -371,13 +376,13 @@ __global__ void __launch_bounds__((L / rp_elems(L)) << LGTW,
   V v[E];
 #pragma unroll
   for (int i = 0; i < E; ++i)
-    v[i] = live ? src[(long long)first_pos<L, D0>(t, i) * s.Wtot] : mkc<T>(T(0), T(0));
-  RRun<T, D0, L, LY, 0>::run(v, buf, t, c, p);
+    v[i] = live ? src[(long long)first_pos<L, D0, CAP>(t, i) * s.Wtot] : mkc<T>(T(0), T(0));
+  RRun<T, D0, L, LY, 0, CAP>::run(v, buf, t, c, p);
   if (MODE == MODE_FCI || MODE == MODE_FCIX) {
     if (live) {
 #pragma unroll
       for (int i = 0; i < E; ++i) {
-        const int l = last_pos<L, -1>(t, i);
+        const int l = last_pos<L, -1, CAP>(t, i);
         const long long k = ((bb * L + l) * (long long)s.Q + q) * s.Hz + kz0 + c;
         if (MODE == MODE_FCI) {
           v[i] = freq_clamp<T>(v[i], ca.delta, fedits, k, H);
@@ -391,13 +396,13 @@ __global__ void __launch_bounds__((L / rp_elems(L)) << LGTW,
     // stage wrote, so the same registers continue.  A barrier separates the
     // forward's last shared reads from the inverse's first shared writes.
     __syncthreads();
-    RRun<T, +1, L, LY, 0>::run(v, buf, t, c, p);
+    RRun<T, +1, L, LY, 0, CAP>::run(v, buf, t, c, p);
   }
   constexpr int DL = (MODE == MODE_FWD) ? -1 : +1;
   V *dst = spec + bb * (long long)L * s.Wtot + (long long)q * s.Hzp + kz0 + c;
   if (live) {
 #pragma unroll
-    for (int i = 0; i < E; ++i) dst[(long long)last_pos<L, DL>(t, i) * s.Wtot] = v[i];
+    for (int i = 0; i < E; ++i) dst[(long long)last_pos<L, DL, CAP>(t, i) * s.Wtot] = v[i];
   }
 }
 

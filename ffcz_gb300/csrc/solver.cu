@@ -90,7 +90,13 @@ struct ffcz_solver {
   unsigned long long *d_up_blk = nullptr;  // decoder: set flags per chunk (lazy)
   // plans
   AxisPlan pz{}, py{}, px{};
-  AxisPlan pz_s{}, py_s{}, px_s{};  // plans of the compile-time-sized kernels
+  AxisPlan pz_s{}, py_s{}, px_s{};  // plans of the compile-time-sized kernels (plain passes)
+  AxisPlan pyf_s{}, pxf_s{};         // the same for the fused passes' stage lists
+  // the fused pass of an axis (forward + clamp + inverse) may use another
+  // stage list, hence another tile and plan, than its plain passes
+  SArgs syf{}, sxf{};
+  Launch lyf{}, lxf{};
+  AxisPlan pyf{}, pxf{};
   size_t post_off = 0;  // offset (complex entries) of the R2C split twiddles
   ZArgs za{};
   SArgs sy{}, sx{};
@@ -232,25 +238,30 @@ bool apply_static_strided(ffcz_solver *s, int axis, int var) {
   const int L = axis == 0 ? (int)s->ny : (int)s->nx;
   const int Q = axis == 0 ? 1 : (int)s->ny;
   const long long B = axis == 0 ? (long long)s->nx : 1;
-  SArgs &sa = axis == 0 ? s->sy : s->sx;
-  Launch &ln = axis == 0 ? s->ly : s->lx;
   void **k = axis == 0 ? s->ky : s->kx;
   const AxisPlan &ps = axis == 0 ? s->py_s : s->px_s;
+  const AxisPlan &psf = axis == 0 ? s->pyf_s : s->pxf_s;
   if (ps.nst == 0) return false;
-  StaticGeom g;
+  StaticGeom g[4];
   StridedFn<T> f[4];
   bool ok = true;
-  for (int m = 0; m < 4 && ok; ++m) ok = static_strided<T>(L, m, f[m], g, var);
+  for (int m = 0; m < 4 && ok; ++m) ok = static_strided<T>(L, m, f[m], g[m], var);
   if (!ok) return false;
   for (int m = 0; m < 4; ++m) k[m] = (void *)f[m];
-  (axis == 0 ? s->py : s->px) = ps;
-  sa.TW = g.TW;
-  sa.log2TW = __builtin_ctz(g.TW);
-  sa.P = g.TW + 1;
-  sa.tpq = (int)ceil_div((size_t)s->Hz, (size_t)g.TW);
-  ln.threads = g.threads;
-  ln.smem = g.smem;
-  ln.grid = (unsigned)(B * Q * (long long)sa.tpq);
+  // plain passes: geometry of MODE_FWD (= MODE_INV); fused: of MODE_FCI
+  for (int fam = 0; fam < 2; ++fam) {
+    const StaticGeom &gg = g[fam ? MODE_FCI : MODE_FWD];
+    SArgs &sa = fam ? (axis == 0 ? s->syf : s->sxf) : (axis == 0 ? s->sy : s->sx);
+    Launch &ln = fam ? (axis == 0 ? s->lyf : s->lxf) : (axis == 0 ? s->ly : s->lx);
+    (fam ? (axis == 0 ? s->pyf : s->pxf) : (axis == 0 ? s->py : s->px)) = fam ? psf : ps;
+    sa.TW = gg.TW;
+    sa.log2TW = __builtin_ctz(gg.TW);
+    sa.P = gg.TW + 1;
+    sa.tpq = (int)ceil_div((size_t)s->Hz, (size_t)gg.TW);
+    ln.threads = gg.threads;
+    ln.smem = gg.smem;
+    ln.grid = (unsigned)(B * Q * (long long)sa.tpq);
+  }
   (axis == 0 ? s->static_y : s->static_x) = 1;
   (axis == 0 ? s->yvar : s->xvar) = var;
   return true;
@@ -269,6 +280,13 @@ int select_kernels(ffcz_solver *s) {
   else generic_strided<T, E>(s->ky);
   if (s->x_ept == kWideEpt) generic_strided<T, kWideEpt>(s->kx);
   else generic_strided<T, E>(s->kx);
+  // runtime-planned kernels: one tile and plan for every pass of an axis
+  s->syf = s->sy;
+  s->lyf = s->ly;
+  s->pyf = s->py;
+  s->sxf = s->sx;
+  s->lxf = s->lx;
+  s->pxf = s->px;
   const char *off = getenv("FFCZ_GENERIC_KERNELS");
   if (off && off[0] == '1') return FFCZ_OK;
   apply_static_z<T>(s, 0);
@@ -301,8 +319,14 @@ int plan_solver(ffcz_solver *s) {
   const bool ys = s->has_y && static_length((int)s->ny, fp64);
   const bool xs = s->has_x && static_length((int)s->nx, fp64);
   if (zs) build_static_plan(s->M, 8, s->pz_s, table);
-  if (ys) build_static_plan((int)s->ny, 16, s->py_s, table);
-  if (xs) build_static_plan((int)s->nx, 16, s->px_s, table);
+  if (ys) {
+    build_static_plan((int)s->ny, static_plain_cap((int)s->ny), s->py_s, table);
+    build_static_plan((int)s->ny, 16, s->pyf_s, table);
+  }
+  if (xs) {
+    build_static_plan((int)s->nx, static_plain_cap((int)s->nx), s->px_s, table);
+    build_static_plan((int)s->nx, 16, s->pxf_s, table);
+  }
   s->post_off = table.size();
   if (s->even)
     for (int k = 0; k <= s->M; ++k) {
@@ -315,7 +339,7 @@ int plan_solver(ffcz_solver *s) {
   FFCZ_CUDA(cudaMalloc(&s->d_tw, tw.size() * es2));
   FFCZ_CUDA(cudaMemcpy(s->d_tw, tw.data(), tw.size() * es2, cudaMemcpyHostToDevice));
   s->pz.tw = s->py.tw = s->px.tw = s->d_tw;
-  s->pz_s.tw = s->py_s.tw = s->px_s.tw = s->d_tw;
+  s->pz_s.tw = s->py_s.tw = s->px_s.tw = s->pyf_s.tw = s->pxf_s.tw = s->d_tw;
   // z passes
   {
     const int rows_smem = s->even ? s->M + 1 : (int)s->nz;
@@ -449,7 +473,7 @@ void launch_iteration(ffcz_solver *s, cudaStream_t st, int pro, const void *a, c
                                                                                      tp<T>(s->d_fedits), H);
       mark();
     }
-    ((StridedFn<T>)s->kx[fci])<<<s->lx.grid, s->lx.threads, s->lx.smem, st>>>(spec, s->sx, s->px, delta,
+    ((StridedFn<T>)s->kx[fci])<<<s->lxf.grid, s->lxf.threads, s->lxf.smem, st>>>(spec, s->sxf, s->pxf, delta,
                                                                                    tp<T>(s->d_fedits), H);
     mark();
     if (s->has_y) {
@@ -458,7 +482,7 @@ void launch_iteration(ffcz_solver *s, cudaStream_t st, int pro, const void *a, c
       mark();
     }
   } else if (s->fused == 1) {
-    ((StridedFn<T>)s->ky[fci])<<<s->ly.grid, s->ly.threads, s->ly.smem, st>>>(spec, s->sy, s->py, delta,
+    ((StridedFn<T>)s->ky[fci])<<<s->lyf.grid, s->lyf.threads, s->lyf.smem, st>>>(spec, s->syf, s->pyf, delta,
                                                                                    tp<T>(s->d_fedits), H);
     mark();
   } else {
@@ -907,9 +931,13 @@ int autotune(ffcz_solver *s, int reps, double *ms6) {
     const Launch &ln = axis == 0 ? s->ly : s->lx;
     const SArgs &sa = axis == 0 ? s->sy : s->sx;
     const AxisPlan &pl = axis == 0 ? s->py : s->px;
+    const Launch &lnf = axis == 0 ? s->lyf : s->lxf;
+    const SArgs &saf = axis == 0 ? s->syf : s->sxf;
+    const AxisPlan &plf = axis == 0 ? s->pyf : s->pxf;
     auto run = [&]() {
       if (fused_here) {
-        ((StridedFn<T>)k[MODE_FCI])<<<ln.grid, ln.threads, ln.smem, st>>>(spec, sa, pl, ca, tp<T>(s->d_fedits), H);
+        ((StridedFn<T>)k[MODE_FCI])<<<lnf.grid, lnf.threads, lnf.smem, st>>>(spec, saf, plf, ca, tp<T>(s->d_fedits),
+                                                                             H);
       } else {
         ((StridedFn<T>)k[MODE_FWD])<<<ln.grid, ln.threads, ln.smem, st>>>(spec, sa, pl, ca, tp<T>(s->d_fedits), H);
         ((StridedFn<T>)k[MODE_INV])<<<ln.grid, ln.threads, ln.smem, st>>>(spec, sa, pl, ca, tp<T>(s->d_fedits), H);

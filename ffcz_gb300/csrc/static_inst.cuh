@@ -71,18 +71,29 @@ bool zinv_for(ZinvFn<T> &fn, StaticGeom &g) {
   return set_smem(fn, g.smem) == FFCZ_OK;
 }
 
-template <typename T, int L, int VAR>
-bool strided_for(int mode, StridedFn<T> &fn, StaticGeom &g) {
-  using C = Cfg<T, L, 16, VAR>;
-  if (VAR && C::TW == Cfg<T, L, 16, 0>::TW) return false;
-  if (mode == MODE_FWD) fn = ks_strided<T, MODE_FWD, L, C::LGTW>;
-  else if (mode == MODE_INV) fn = ks_strided<T, MODE_INV, L, C::LGTW>;
-  else if (mode == MODE_FCI) fn = ks_strided<T, MODE_FCI, L, C::LGTW>;
-  else fn = ks_strided<T, MODE_FCIX, L, C::LGTW>;
+// The plain passes (forward, inverse) take the plain_cap(L) stage list, the
+// fused ones (forward + clamp + inverse) the CAP 16 list.
+template <typename T, int L, int VAR, bool FUSED>
+bool strided_for_family(int mode, StridedFn<T> &fn, StaticGeom &g) {
+  constexpr int CAP = FUSED ? 16 : plain_cap(L);
+  using C = Cfg<T, L, CAP, VAR>;
+  if (VAR && C::TW == Cfg<T, L, CAP, 0>::TW) return false;
+  if constexpr (FUSED) {
+    if (mode == MODE_FCI) fn = ks_strided<T, MODE_FCI, L, C::LGTW, CAP>;
+    else fn = ks_strided<T, MODE_FCIX, L, C::LGTW, CAP>;
+  } else {
+    if (mode == MODE_FWD) fn = ks_strided<T, MODE_FWD, L, C::LGTW, CAP>;
+    else fn = ks_strided<T, MODE_INV, L, C::LGTW, CAP>;
+  }
   g.TW = C::TW;
   g.threads = C::NT;
   g.smem = (size_t)sl_size(L, C::TW, sizeof(T)) * sizeof(c2<T>);
   return set_smem(fn, g.smem) == FFCZ_OK;
+}
+template <typename T, int L, int VAR>
+bool strided_for(int mode, StridedFn<T> &fn, StaticGeom &g) {
+  return (mode == MODE_FWD || mode == MODE_INV) ? strided_for_family<T, L, VAR, false>(mode, fn, g)
+                                                : strided_for_family<T, L, VAR, true>(mode, fn, g);
 }
 
 #define CASES_F32(X)                                                                                      \

@@ -12,6 +12,8 @@ bool static_length(int L, bool fp64) {
   return L >= 16 && (L & (L - 1)) == 0 && L <= (fp64 ? 2048 : 4096);
 }
 
+int static_plain_cap(int L) { return plain_cap(L); }
+
 void build_static_plan(int L, int cap, AxisPlan &p, std::vector<std::complex<double>> &table) {
   p.L = L;
   p.nst = rp_nst(L, cap);

@@ -27,8 +27,12 @@ struct StaticGeom {
 bool static_length(int L, bool fp64);
 // Appends the forward and inverse stage twiddles of length L to `table`
 // and fills p.twoff (forward at [s], inverse at [12 + s]); p.tw left null.
-// cap = 16 for the strided passes' stage lists, 8 for the z passes'.
+// cap = 16 for the strided passes' stage lists (17: the plain passes'
+// family, static_plain_cap), 8 for the z passes'.
 void build_static_plan(int L, int cap, AxisPlan &p, std::vector<std::complex<double>> &table);
+// Stage-list family (the cap argument above) of the plain forward / inverse
+// strided passes of length L; the fused passes use 16.
+int static_plain_cap(int L);
 
 // Kernel for a length static_length() accepts (false otherwise).
 // z passes: M = Nz/2; pro is PRO_PLAIN/PRO_DIFF/PRO_CLAMP.
