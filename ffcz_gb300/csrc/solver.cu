@@ -1636,22 +1636,31 @@ struct ffcz_batch {
   std::vector<cudaStream_t> fs;   // one capture stream per field
   cudaEvent_t fork = nullptr;
   std::vector<cudaEvent_t> join;
-  cudaGraph_t graph = nullptr;
-  cudaGraphExec_t gexec = nullptr;
-  // graph key
-  std::vector<const void *> ka, kb;
-  std::vector<double> keps, kdelta;
-  std::vector<int> kpack, kgen;
-  int kmax_iter = -1;
-  double ktol = 0;
-  cudaStream_t kstream = nullptr;
+  // the two most recently used batch graphs (inputs that alternate between
+  // two buffer sets, e.g. copies of the next step's fields overlapping this
+  // step, keep both)
+  struct Cached {
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    std::vector<const void *> ka, kb;
+    std::vector<double> keps, kdelta;
+    std::vector<int> kpack, kgen;
+    int kmax_iter = -1;
+    double ktol = 0;
+    cudaStream_t kstream = nullptr;
+    void reset() {
+      if (exec) cudaGraphExecDestroy(exec);
+      if (graph) cudaGraphDestroy(graph);
+      exec = nullptr;
+      graph = nullptr;
+    }
+  } bg[2];
 };
 
 namespace {
 
 void free_batch(ffcz_batch *b) {
-  if (b->gexec) cudaGraphExecDestroy(b->gexec);
-  if (b->graph) cudaGraphDestroy(b->graph);
+  for (auto &c : b->bg) c.reset();
   for (cudaStream_t st : b->fs)
     if (st) cudaStreamDestroy(st);
   if (b->cap) cudaStreamDestroy(b->cap);
@@ -1660,7 +1669,8 @@ void free_batch(ffcz_batch *b) {
   if (b->fork) cudaEventDestroy(b->fork);
 }
 
-int capture_batch(ffcz_batch *b, const void *const *a, const void *const *d, int max_iter, double tol) {
+int capture_batch(ffcz_batch *b, ffcz_batch::Cached &out, const void *const *a, const void *const *d, int max_iter,
+                  double tol) {
   FFCZ_CUDA(cudaStreamBeginCapture(b->cap, cudaStreamCaptureModeThreadLocal));
   int rc = FFCZ_OK;
   cudaError_t e = cudaEventRecord(b->fork, b->cap);
@@ -1689,8 +1699,8 @@ int capture_batch(ffcz_batch *b, const void *const *a, const void *const *d, int
     return rc;
   }
   FFCZ_CUDA(e);
-  b->graph = g;
-  FFCZ_CUDA(cudaGraphInstantiate(&b->gexec, b->graph, 0));
+  out.graph = g;
+  FFCZ_CUDA(cudaGraphInstantiate(&out.exec, out.graph, 0));
   return FFCZ_OK;
 }
 
@@ -1782,29 +1792,29 @@ int ffcz_batch_solve_pair_device(ffcz_batch *b, const void *const *d_orig, const
     pack[i] = b->f[i]->pack_mode;
     gen[i] = b->f[i]->kernel_gen;
   }
-  const bool same = b->gexec && b->kmax_iter == max_iter && b->ktol == tol && b->kstream == b->stream &&
-                    b->ka == std::vector<const void *>(d_orig, d_orig + nf) &&
-                    b->kb == std::vector<const void *>(d_decomp, d_decomp + nf) && b->keps == eps &&
-                    b->kdelta == delta && b->kpack == pack && b->kgen == gen;
-  if (!same) {
-    if (b->gexec) cudaGraphExecDestroy(b->gexec);
-    if (b->graph) cudaGraphDestroy(b->graph);
-    b->gexec = nullptr;
-    b->graph = nullptr;
-    FFCZ_TRY(capture_batch(b, d_orig, d_decomp, max_iter, tol));
-    b->ka.assign(d_orig, d_orig + nf);
-    b->kb.assign(d_decomp, d_decomp + nf);
-    b->keps = eps;
-    b->kdelta = delta;
-    b->kpack = pack;
-    b->kgen = gen;
-    b->kmax_iter = max_iter;
-    b->ktol = tol;
-    b->kstream = b->stream;
+  const std::vector<const void *> ka(d_orig, d_orig + nf), kb(d_decomp, d_decomp + nf);
+  auto same = [&](const ffcz_batch::Cached &c) {
+    return c.exec && c.kmax_iter == max_iter && c.ktol == tol && c.kstream == b->stream && c.ka == ka &&
+           c.kb == kb && c.keps == eps && c.kdelta == delta && c.kpack == pack && c.kgen == gen;
+  };
+  if (!same(b->bg[0])) std::swap(b->bg[0], b->bg[1]);
+  if (!same(b->bg[0])) {
+    ffcz_batch::Cached &c = b->bg[0];
+    c.reset();
+    FFCZ_TRY(capture_batch(b, c, d_orig, d_decomp, max_iter, tol));
+    c.ka = ka;
+    c.kb = kb;
+    c.keps = eps;
+    c.kdelta = delta;
+    c.kpack = pack;
+    c.kgen = gen;
+    c.kmax_iter = max_iter;
+    c.ktol = tol;
+    c.kstream = b->stream;
   }
   // the fields' own streams may still run earlier work on their buffers
   for (size_t i = 0; i < nf; ++i) FFCZ_CUDA(cudaStreamSynchronize(b->f[i]->stream));
-  FFCZ_CUDA(cudaGraphLaunch(b->gexec, b->stream));
+  FFCZ_CUDA(cudaGraphLaunch(b->bg[0].exec, b->stream));
   for (size_t i = 0; i < nf; ++i)
     FFCZ_CUDA(cudaMemcpyAsync(b->f[i]->h_ctl, b->f[i]->d_ctl, sizeof(LoopCtl), cudaMemcpyDeviceToHost, b->stream));
   FFCZ_CUDA(cudaStreamSynchronize(b->stream));

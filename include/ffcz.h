@@ -267,8 +267,10 @@ int ffcz_get_pass_times(ffcz_solver *s, double *ms, double *bytes, int cap,
  *             keeps the pointers (destroy the batch before them).
  *   d_orig[f], d_decomp[f] : device arrays of field f (16-byte aligned).
  * The call runs on the batch's stream (ffcz_batch_set_stream; legacy
- * default stream otherwise) and returns after it finished.  The graph is
- * built on the first call and reused while the arguments stay the same. */
+ * default stream otherwise) and returns after it finished.  A graph is
+ * built on the first call with a set of arguments; the two most recent sets
+ * keep theirs, so inputs that alternate between two buffer sets (the next
+ * step's fields copied in while this step runs) capture nothing new. */
 typedef struct ffcz_batch ffcz_batch;
 int ffcz_batch_create(ffcz_solver *const *solvers, int nfields,
                       ffcz_batch **out);

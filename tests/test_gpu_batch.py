@@ -142,3 +142,35 @@ def test_batch_errors(cuda):
     fresh.close()
     for s in ss:
         s.close()
+
+
+def test_batch_alternating_input_sets(cuda):
+    """Inputs alternating between buffer sets (the next step's fields copied
+    in while this step runs): each set's cached graph reads its own buffers,
+    and a third set evicts the older entry without disturbing the results."""
+    fields = make_fields(cuda, FIELDS[:5], seed0=90)
+    ss = solvers_for(fields)
+    sets = [([f[2] for f in fields], [f[3] for f in fields])]
+    for _ in range(2):
+        sets.append(([d.clone() for d in sets[0][0]], [d.clone() for d in sets[0][1]]))
+    with F.Batch(ss) as b:
+        ref_its = b.solve_pair_device(*sets[0], 100, 1e-7)
+        ref = [outputs(s) for s in ss]
+        for k in (1, 0, 1, 2, 0, 2):
+            b.reset_edit_accumulators()
+            assert b.solve_pair_device(*sets[k], 100, 1e-7) == ref_its, k
+            for s, g in zip(ss, ref):
+                assert_same(g, outputs(s), f"set {k}")
+        # a set whose buffers now hold other data gives that data's results
+        other = make_fields(cuda, FIELDS[:5], seed0=95)
+        for d, f in zip(sets[1][0] + sets[1][1], [f[2] for f in other] + [f[3] for f in other]):
+            d.copy_(f)
+        b.reset_edit_accumulators()
+        its = b.solve_pair_device(*sets[1], 100, 1e-7)
+        for i, (fld, delta, dx, dxp) in enumerate(other):
+            with F.ProjectionSolver(*fld.shape, dtype=fld.x.dtype) as s:
+                s.initialize_all_abs(fields[i][0].x, fields[i][0].eps, fields[i][1])
+                assert s.solve_all_abs_pair_device(dx, dxp, 100, 1e-7) == its[i]
+                assert_same(outputs(s), outputs(ss[i]), f"refilled field {i}")
+    for s in ss:
+        s.close()
