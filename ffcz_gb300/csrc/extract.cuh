@@ -263,6 +263,9 @@ __global__ void __launch_bounds__(EX_THREADS) k_ex_compact(
 //                   own start, the chunk's count; per block a group record
 //                   (count, min and max as order-preserving integer keys)
 //                                                  (R n*s, W cnt*s + n/8)
+//                   With a clean flag that reads 0 (an accumulator nothing
+//                   has written since it was cleared) it writes zero flag
+//                   words and zero records without reading the array (W n/8).
 //   k_ex_scan_rec : one block: exclusive offsets of the groups, whole-array
 //                   count, min and max
 //   k_ex_place    : one warp per chunk moves the chunk's values to their
@@ -377,9 +380,10 @@ __device__ __forceinline__ unsigned ex_chunk(const T *__restrict__ a, long long 
 
 template <typename T>
 __global__ void __launch_bounds__(EX_THREADS, 3) k_ex_part(const T *__restrict__ a, long long n, long long nchunk, T thr,
-                                                        T *__restrict__ scratch, ExRec rec,
-                                                        unsigned *__restrict__ pack_words, int write_pack) {
-  constexpr int CH = xp_chunk<T>();
+                                                           const unsigned *__restrict__ dirty,
+                                                           T *__restrict__ scratch, ExRec rec,
+                                                           unsigned *__restrict__ pack_words, int write_pack) {
+  constexpr int CH = xp_chunk<T>(), SPAN = 32 * xp_vec<T>();
   __shared__ unsigned scnt[XP_WPG];
   __shared__ unsigned long long smn[XP_WPG], smx[XP_WPG];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -387,7 +391,19 @@ __global__ void __launch_bounds__(EX_THREADS, 3) k_ex_part(const T *__restrict__
   T mn = dev_inf<T>(), mx = -dev_inf<T>();
   bool any = false;
   unsigned run = 0;
-  if (c < nchunk) {
+  if (dirty && *dirty == 0u) {
+    // the accumulator is all zeros (nothing written since it was cleared):
+    // zero flag words, no active value, min = max = 0, nothing read
+    if (c < nchunk) {
+      any = true;
+      mn = mx = T(0);
+      if (write_pack)
+        for (int q = 0; q < XP_NQ; ++q) {
+          const long long i = c * CH + (long long)q * SPAN + 32 * lane;
+          if (32 * lane < SPAN && i < n) pack_words[i >> 5] = 0u;
+        }
+    }
+  } else if (c < nchunk) {
     const long long base = c * CH;
     if (base + CH <= n)
       run = ex_chunk<T, true>(a, n, base, thr, scratch + base, pack_words, write_pack, mn, mx, any);

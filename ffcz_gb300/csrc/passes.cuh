@@ -57,26 +57,34 @@ __device__ __forceinline__ T spatial_clamp(T v, T eps, T *__restrict__ sedits, l
   return v;
 }
 
-// Frequency box (projection_algorithm.cu:160-187) on one coefficient.
+// Frequency box (projection_algorithm.cu:160-187) on one coefficient.  A
+// clamp also sets *dirty (when given): the accumulator is no longer all
+// zeros, so its compaction has to read it.
 template <typename T>
 __device__ __forceinline__ c2<T> freq_clamp(c2<T> v, T delta, T *__restrict__ fedits, long long k,
-                                            long long H) {
+                                            long long H, unsigned *dirty) {
   T re = v.x;
+  bool hit = false;
   if (re > delta) {
     fedits[k] += delta - re;
     v.x = delta;
+    hit = true;
   } else if (re < -delta) {
     fedits[k] += -delta - re;
     v.x = -delta;
+    hit = true;
   }
   T im = v.y;
   if (im > delta) {
     fedits[k + H] += delta - im;
     v.y = delta;
+    hit = true;
   } else if (im < -delta) {
     fedits[k + H] += -delta - im;
     v.y = -delta;
+    hit = true;
   }
+  if (hit && dirty) *dirty = 1u;
   return v;
 }
 
@@ -99,6 +107,7 @@ struct ClampArgs {
   const c2<T> *orig = nullptr;         // PTW: spectrum of x, padded layout
   const unsigned char *mask = nullptr; // PTW: constrained coefficients
   T sp = T(0), sm = T(0), lo = T(0), hi = T(0), cd = T(0);  // PTW constants
+  unsigned *fdirty = nullptr;          // set when a frequency edit is written
 };
 
 __device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
@@ -109,8 +118,8 @@ __device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(
 template <typename T>
 __device__ __forceinline__ c2<T> freq_project(c2<T> v, const ClampArgs<T> &ca, T *__restrict__ fedits, long long k,
                                               long long p, long long H) {
-  if (ca.mode == CLAMP_ABS) return freq_clamp<T>(v, ca.delta, fedits, k, H);
-  if (ca.mode == CLAMP_DIRECT) return freq_clamp<T>(v, ca.bound[k], fedits, k, H);
+  if (ca.mode == CLAMP_ABS) return freq_clamp<T>(v, ca.delta, fedits, k, H, ca.fdirty);
+  if (ca.mode == CLAMP_DIRECT) return freq_clamp<T>(v, ca.bound[k], fedits, k, H, ca.fdirty);
   if (k == 0) {
     if (ca.dc) {
       const T o = ca.orig[0].x;
@@ -118,6 +127,7 @@ __device__ __forceinline__ c2<T> freq_project(c2<T> v, const ClampArgs<T> &ca, T
       if (v.x > upper || v.x < lower) {
         fedits[0] += -v.x;
         v.x = T(0);
+        if (ca.fdirty) *ca.fdirty = 1u;
       }
     }
     return v;
@@ -129,7 +139,7 @@ __device__ __forceinline__ c2<T> freq_project(c2<T> v, const ClampArgs<T> &ca, T
   const T cm = add_rn(mul_rn(cx, cx), mul_rn(cy, cy));
   const T ratio = cm / om;
   if (ratio <= ca.sp && ratio >= ca.sm) return v;
-  return freq_clamp<T>(v, ca.cd, fedits, k, H);
+  return freq_clamp<T>(v, ca.cd, fedits, k, H, ca.fdirty);
 }
 
 // ---------------------------------------------------------------------------
@@ -390,7 +400,7 @@ __global__ void __launch_bounds__(sizeof(T) == 4 ? 512 : 256) k_strided(c2<T> *_
       if (c < ncol) {
         const long long k = ((bb * s.L + l) * (long long)s.Q + q) * s.Hz + kz0 + c;
         if (MODE == MODE_FCI)
-          buf[l * P + c] = freq_clamp<T>(buf[l * P + c], ca.delta, fedits, k, H);
+          buf[l * P + c] = freq_clamp<T>(buf[l * P + c], ca.delta, fedits, k, H, ca.fdirty);
         else
           buf[l * P + c] = freq_project<T>(buf[l * P + c], ca, fedits, k, base + (long long)l * s.Wtot + c, H);
       }

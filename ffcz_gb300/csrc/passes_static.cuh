@@ -385,7 +385,7 @@ __global__ void __launch_bounds__((L / rp_elems(L, CAP)) << LGTW,
         const int l = last_pos<L, -1, CAP>(t, i);
         const long long k = ((bb * L + l) * (long long)s.Q + q) * s.Hz + kz0 + c;
         if (MODE == MODE_FCI) {
-          v[i] = freq_clamp<T>(v[i], ca.delta, fedits, k, H);
+          v[i] = freq_clamp<T>(v[i], ca.delta, fedits, k, H, ca.fdirty);
         } else {
           const long long pad = (bb * L + l) * s.Wtot + (long long)q * s.Hzp + kz0 + c;
           v[i] = freq_project<T>(v[i], ca, fedits, k, pad, H);

@@ -85,6 +85,9 @@ struct ffcz_solver {
   void *d_tw = nullptr;
   LoopCtl *d_ctl = nullptr, *h_ctl = nullptr;
   unsigned long long *d_ex_rec = nullptr;  // compaction: chunk records of both accumulators
+  // 0 while the frequency-edit accumulator is all zeros (cleared with it, set
+  // by every frequency clamp); its compaction then skips reading it
+  unsigned *d_fdirty = nullptr;
   void *d_mnmx = nullptr;
   size_t nblk_max = 0;
   unsigned long long *d_up_blk = nullptr;  // decoder: set flags per chunk (lazy)
@@ -422,6 +425,7 @@ ClampArgs<T> clamp_args(const ffcz_solver *s) {
   ClampArgs<T> ca;
   ca.mode = s->cmode;
   ca.delta = (T)s->delta;
+  ca.fdirty = s->d_fdirty;
   ca.bound = (const T *)s->d_bound;
   ca.orig = (const c2<T> *)s->d_orig;
   if (s->cmode == CLAMP_PTW) {
@@ -657,7 +661,8 @@ int extract_one(ffcz_solver *s, cudaStream_t st, const T *a, size_t n, int which
   // the spectrum buffer (>= n values of T) is idle once the loop has ended
   T *scratch = (T *)s->d_spec;
   const int correct = s->pack_mode == FFCZ_PACK_CORRECT;
-  k_ex_part<T><<<(unsigned)ngroup, EX_THREADS, 0, st>>>(a, (long long)n, (long long)nchunk, thr, scratch, rec,
+  k_ex_part<T><<<(unsigned)ngroup, EX_THREADS, 0, st>>>(a, (long long)n, (long long)nchunk, thr,
+                                                        which == 0 ? s->d_fdirty : nullptr, scratch, rec,
                                                         (unsigned *)pack, correct);
   k_ex_scan_rec<T><<<1, XS_THREADS, 0, st>>>((long long)ngroup, rec, mnmx, s->d_ctl, which);
   const unsigned gp = (unsigned)std::min<size_t>(ceil_div(nchunk, (size_t)(EX_THREADS / 32)), 152 * 8);
@@ -716,7 +721,7 @@ int extract(ffcz_solver *s) {
 void free_all(ffcz_solver *s) {
   for (LoopGraph &g : s->lg) g.reset();
   void *bufs[] = {s->d_x, s->d_e, s->d_spec, s->d_fedits, s->d_sedits, s->d_fcompact, s->d_scompact,
-                  s->d_fquant, s->d_squant, s->d_fpack, s->d_spack, s->d_tw, s->d_ctl, s->d_ex_rec,
+                  s->d_fquant, s->d_squant, s->d_fpack, s->d_spack, s->d_tw, s->d_ctl, s->d_ex_rec, s->d_fdirty,
                   s->d_mnmx};
   for (void *p : bufs)
     if (p) cudaFree(p);
@@ -952,6 +957,7 @@ int autotune(ffcz_solver *s, int reps, double *ms6) {
   for (double v : t)
     if (v < 0) return fail(FFCZ_ERR_CUDA, "autotune launch failed");
   FFCZ_CUDA(cudaMemsetAsync(s->d_fedits, 0, 2 * s->H * s->es, st));
+  FFCZ_CUDA(cudaMemsetAsync(s->d_fdirty, 0, sizeof(unsigned), st));
   FFCZ_CUDA(cudaMemsetAsync(s->d_sedits, 0, s->N * s->es, st));
   FFCZ_CUDA(cudaStreamSynchronize(st));
   // the cached loop graphs hold the previous kernels
@@ -1070,6 +1076,7 @@ int ffcz_solver_create(size_t nx, size_t ny, size_t nz, int dtype, ffcz_solver *
   const size_t nrec = xp_words(xf32 ? xp_groups<float>(H2) : xp_groups<double>(H2)) +
                       xp_words(xf32 ? xp_groups<float>(N) : xp_groups<double>(N));
   if (rc == FFCZ_OK) rc = alloc((void **)&s->d_ex_rec, nrec * sizeof(unsigned long long));
+  if (rc == FFCZ_OK) rc = alloc((void **)&s->d_fdirty, sizeof(unsigned));
   if (rc == FFCZ_OK) rc = alloc(&s->d_mnmx, 4 * es);
   if (rc == FFCZ_OK) {
     cudaError_t e = cudaMallocHost(&s->h_ctl, sizeof(LoopCtl));
@@ -1085,6 +1092,7 @@ int ffcz_solver_create(size_t nx, size_t ny, size_t nz, int dtype, ffcz_solver *
     if (e == cudaSuccess) e = cudaMemset(s->d_fpack, 0, s->fpack_bytes);
     if (e == cudaSuccess) e = cudaMemset(s->d_spack, 0, s->spack_bytes);
     if (e == cudaSuccess) e = cudaMemset(s->d_fedits, 0, H2 * es);
+    if (e == cudaSuccess) e = cudaMemset(s->d_fdirty, 0, sizeof(unsigned));
     if (e == cudaSuccess) e = cudaMemset(s->d_sedits, 0, N * es);
     if (e == cudaSuccess) e = xp_init(s.get());
     if (e != cudaSuccess) rc = cuda_fail(e, "cudaMemset", __FILE__, __LINE__);
@@ -1290,6 +1298,7 @@ int ffcz_extract(ffcz_solver *s) {
 int ffcz_reset_edit_accumulators(ffcz_solver *s) {
   FFCZ_TRY(check_solver(s));
   FFCZ_CUDA(cudaMemsetAsync(s->d_fedits, 0, 2 * s->H * s->es, s->stream));
+  FFCZ_CUDA(cudaMemsetAsync(s->d_fdirty, 0, sizeof(unsigned), s->stream));
   FFCZ_CUDA(cudaMemsetAsync(s->d_sedits, 0, s->N * s->es, s->stream));
   FFCZ_CUDA(cudaStreamSynchronize(s->stream));
   return FFCZ_OK;
@@ -1760,6 +1769,7 @@ int ffcz_batch_reset_edit_accumulators(ffcz_batch *b) {
   for (ffcz_solver *s : b->f) FFCZ_CUDA(cudaStreamSynchronize(s->stream));
   for (ffcz_solver *s : b->f) {
     FFCZ_CUDA(cudaMemsetAsync(s->d_fedits, 0, 2 * s->H * s->es, b->stream));
+    FFCZ_CUDA(cudaMemsetAsync(s->d_fdirty, 0, sizeof(unsigned), b->stream));
     FFCZ_CUDA(cudaMemsetAsync(s->d_sedits, 0, s->N * s->es, b->stream));
   }
   FFCZ_CUDA(cudaStreamSynchronize(b->stream));

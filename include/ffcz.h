@@ -198,7 +198,9 @@ int ffcz_get_spatial_flags(ffcz_solver *s, uint8_t *dst, size_t cap,
  * quant, 5 freq pack, 6 spatial pack, 7 freq compact, 8 spatial compact,
  * 9 spectrum of x of the pointwise modes (Nx*Ny rows of pitch Hzp complex
  * values, Hzp = Nz/2+1 rounded up to 128 bytes; 0 bytes before an
- * initialize_*_ptw). */
+ * initialize_*_ptw).  Read-only for callers: the solver knows when the
+ * frequency-edit accumulator is still all zeros (nothing clamped since
+ * ffcz_reset_edit_accumulators) and then compacts it without reading it. */
 int ffcz_get_device_array(ffcz_solver *s, int which, void **dptr,
                           size_t *bytes);
 /* Autotuner (no counterpart in the reference): times the default and an

@@ -350,3 +350,38 @@ def test_autotune_keeps_results(cuda, shape):
     assert out[0][0] == out[1][0]
     for a, b in zip(out[0][1:], out[1][1:]):
         assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_untouched_frequency_accumulator_compacts_without_reading(cuda, dtype):
+    """While no frequency clamp has fired since the accumulator was cleared,
+    its compaction writes zero flags and zero min/max without reading it;
+    the results equal the oracle's compaction of the (all-zero) array, and
+    a clamp makes the next compaction read it again."""
+    shape = (24, 20, 16)
+    fld = synth.make_field(shape, 11 / 3, 41, 1e-3, 1e-3, dtype, noise=0.3)
+    e0 = (fld.xp.astype(np.float64) - fld.x.astype(np.float64)).astype(dtype)
+
+    def check(s):
+        fe = s.get_freq_edits_full()
+        ref = O.extract(fe)
+        nf = s.active_counts()[0]
+        assert nf == ref["count"]
+        assert s.minmax()[:2] == (ref["min"], ref["max"])
+        assert np.array_equal(s.get_freq_flags_pack(), ref["pack"])
+        assert np.array_equal(s.get_active_freq_quant_edit_distances(), ref["quant"])
+        return nf
+
+    with F.ProjectionSolver(*shape, dtype=dtype) as s:
+        s.initialize_all_abs(fld.x, fld.eps, 1e30)  # no frequency clamp
+        s.solve_all_abs(e0, 100, 1e-7)
+        assert check(s) == 0 and not s.get_freq_edits_full().any()
+        s.initialize_all_abs(fld.x, fld.eps, synth.stress_delta(fld, 1.5))  # clamps fire
+        s.solve_all_abs(e0, 100, 1e-7)
+        assert check(s) > 0
+        s.initialize_all_abs(fld.x, fld.eps, 1e30)  # edits kept: still read
+        s.solve_all_abs(e0, 100, 1e-7)
+        assert check(s) > 0
+        s.reset_edit_accumulators()  # cleared: skipped again
+        s.solve_all_abs(e0, 100, 1e-7)
+        assert check(s) == 0
