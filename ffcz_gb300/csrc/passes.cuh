@@ -445,7 +445,7 @@ static __global__ void k_init_ctl(LoopCtl *ctl) {
 // a graph, sets the WHILE condition.
 template <typename T>
 __global__ void k_check(LoopCtl *ctl, T tol, int max_iter, cudaGraphConditionalHandle h,
-                        int use_graph) {
+                        int use_graph, unsigned *sdirty) {
   const T v = from_bits<T>(ctl->viol_bits);
   ctl->viol_bits = 0ull;
   ctl->last_viol = (double)v;
@@ -455,6 +455,8 @@ __global__ void k_check(LoopCtl *ctl, T tol, int max_iter, cudaGraphConditionalH
   ctl->converged = conv;
   const int cont = (!conv && it < max_iter) ? 1 : 0;
   ctl->cont = cont;
+  // the next iteration's prologue clamps every |e| > eps: spatial edits
+  if (cont && v > T(0)) *sdirty = 1u;
   if (use_graph) cudaGraphSetConditional(h, cont ? 1u : 0u);
 }
 
@@ -466,8 +468,9 @@ static __global__ void k_set_iterations(LoopCtl *ctl, int n) { ctl->iterations =
 // NULL, on every element (the strict-bounds clamp).
 template <typename T>
 __global__ void k_final_clamp(T *__restrict__ e, T *__restrict__ sedits, T eps, long long n,
-                              const LoopCtl *ctl) {
+                              const LoopCtl *ctl, unsigned *sdirty) {
   if (ctl && (ctl->converged || ctl->iterations == 0)) return;  // ctl NULL: always
+  if (blockIdx.x == 0 && threadIdx.x == 0 && (!ctl || ctl->last_viol > 0.0)) *sdirty = 1u;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x) {
     const T v = e[i];

@@ -86,8 +86,10 @@ struct ffcz_solver {
   LoopCtl *d_ctl = nullptr, *h_ctl = nullptr;
   unsigned long long *d_ex_rec = nullptr;  // compaction: chunk records of both accumulators
   // 0 while the frequency-edit accumulator is all zeros (cleared with it, set
-  // by every frequency clamp); its compaction then skips reading it
-  unsigned *d_fdirty = nullptr;
+  // by every frequency clamp); its compaction then skips reading it.
+  // d_sdirty: the same for the spatial accumulator, set by the loop control
+  // (k_check before a clamping prologue, k_final_clamp) and the decoder.
+  unsigned *d_fdirty = nullptr, *d_sdirty = nullptr;
   void *d_mnmx = nullptr;
   size_t nblk_max = 0;
   unsigned long long *d_up_blk = nullptr;  // decoder: set flags per chunk (lazy)
@@ -500,13 +502,14 @@ void launch_iteration(ffcz_solver *s, cudaStream_t st, int pro, const void *a, c
                                                                           s->d_ctl, s->za, s->pz, post);
   mark();
   if (record) s->npass = ne - 1;
-  k_check<T><<<1, 1, 0, st>>>(s->d_ctl, tol, max_iter, h, use_graph);
+  k_check<T><<<1, 1, 0, st>>>(s->d_ctl, tol, max_iter, h, use_graph, s->d_sdirty);
 }
 
 template <typename T>
 void launch_final(ffcz_solver *s, cudaStream_t st) {
   const unsigned g = (unsigned)std::min<size_t>(ceil_div(s->N, 256), 152 * 16);
-  k_final_clamp<T><<<g, 256, 0, st>>>(tp<T>(s->d_e), tp<T>(s->d_sedits), (T)s->eps, (long long)s->N, s->d_ctl);
+  k_final_clamp<T><<<g, 256, 0, st>>>(tp<T>(s->d_e), tp<T>(s->d_sedits), (T)s->eps, (long long)s->N, s->d_ctl,
+                                      s->d_sdirty);
 }
 
 // Captures onto `cs` (a stream taking part in a capture) one field's whole
@@ -662,7 +665,7 @@ int extract_one(ffcz_solver *s, cudaStream_t st, const T *a, size_t n, int which
   T *scratch = (T *)s->d_spec;
   const int correct = s->pack_mode == FFCZ_PACK_CORRECT;
   k_ex_part<T><<<(unsigned)ngroup, EX_THREADS, 0, st>>>(a, (long long)n, (long long)nchunk, thr,
-                                                        which == 0 ? s->d_fdirty : nullptr, scratch, rec,
+                                                        which == 0 ? s->d_fdirty : s->d_sdirty, scratch, rec,
                                                         (unsigned *)pack, correct);
   k_ex_scan_rec<T><<<1, XS_THREADS, 0, st>>>((long long)ngroup, rec, mnmx, s->d_ctl, which);
   const unsigned gp = (unsigned)std::min<size_t>(ceil_div(nchunk, (size_t)(EX_THREADS / 32)), 152 * 8);
@@ -721,7 +724,7 @@ int extract(ffcz_solver *s) {
 void free_all(ffcz_solver *s) {
   for (LoopGraph &g : s->lg) g.reset();
   void *bufs[] = {s->d_x, s->d_e, s->d_spec, s->d_fedits, s->d_sedits, s->d_fcompact, s->d_scompact,
-                  s->d_fquant, s->d_squant, s->d_fpack, s->d_spack, s->d_tw, s->d_ctl, s->d_ex_rec, s->d_fdirty,
+                  s->d_fquant, s->d_squant, s->d_fpack, s->d_spack, s->d_tw, s->d_ctl, s->d_ex_rec, s->d_fdirty, s->d_sdirty,
                   s->d_mnmx};
   for (void *p : bufs)
     if (p) cudaFree(p);
@@ -812,6 +815,9 @@ int reconstruct(ffcz_solver *s, const void *d_decomp, const uint16_t *fq, size_t
   FFCZ_CUDA(cudaMemsetAsync(s->d_sedits, 0, s->N * s->es, st));
   if (ns) FFCZ_TRY(unpack_edits<T>(s, sq, ns, spack, s->N, smin, smax, s->d_spack, s->spack_bytes, tp<T>(s->d_sedits),
                                    nullptr));
+  // the spatial accumulator now holds the decoded edits
+  static const unsigned one = 1u;
+  FFCZ_CUDA(cudaMemcpyAsync(s->d_sdirty, &one, sizeof(unsigned), cudaMemcpyHostToDevice, st));
   const unsigned g = (unsigned)std::min<size_t>(ceil_div(s->N, 256), 152 * 16);
   k_recon_sum<T><<<g, 256, 0, st>>>((const T *)d_decomp, tp<T>(s->d_e), tp<T>(s->d_sedits), (T *)d_out,
                                     (long long)s->N);
@@ -959,6 +965,7 @@ int autotune(ffcz_solver *s, int reps, double *ms6) {
   FFCZ_CUDA(cudaMemsetAsync(s->d_fedits, 0, 2 * s->H * s->es, st));
   FFCZ_CUDA(cudaMemsetAsync(s->d_fdirty, 0, sizeof(unsigned), st));
   FFCZ_CUDA(cudaMemsetAsync(s->d_sedits, 0, s->N * s->es, st));
+  FFCZ_CUDA(cudaMemsetAsync(s->d_sdirty, 0, sizeof(unsigned), st));
   FFCZ_CUDA(cudaStreamSynchronize(st));
   // the cached loop graphs hold the previous kernels
   for (LoopGraph &g : s->lg) g.reset();
@@ -990,7 +997,8 @@ int strict_finish(ffcz_solver *s, int max_iter, double tol, int max_rounds, int 
   int total = s->h_ctl->iterations, r = 0, rc = FFCZ_OK;
   double sm = 0.0, fm = 0.0, dt = D;
   for (;;) {
-    k_final_clamp<T><<<g, 256, 0, st>>>(tp<T>(s->d_e), tp<T>(s->d_sedits), Et, (long long)s->N, nullptr);
+    k_final_clamp<T><<<g, 256, 0, st>>>(tp<T>(s->d_e), tp<T>(s->d_sedits), Et, (long long)s->N, nullptr,
+                                        s->d_sdirty);
     FFCZ_CUDA(cudaGetLastError());
     s->extracted = false;
     if ((rc = ffcz_verify_bounds(s, &sm, &fm)) != FFCZ_OK) break;
@@ -1077,6 +1085,7 @@ int ffcz_solver_create(size_t nx, size_t ny, size_t nz, int dtype, ffcz_solver *
                       xp_words(xf32 ? xp_groups<float>(N) : xp_groups<double>(N));
   if (rc == FFCZ_OK) rc = alloc((void **)&s->d_ex_rec, nrec * sizeof(unsigned long long));
   if (rc == FFCZ_OK) rc = alloc((void **)&s->d_fdirty, sizeof(unsigned));
+  if (rc == FFCZ_OK) rc = alloc((void **)&s->d_sdirty, sizeof(unsigned));
   if (rc == FFCZ_OK) rc = alloc(&s->d_mnmx, 4 * es);
   if (rc == FFCZ_OK) {
     cudaError_t e = cudaMallocHost(&s->h_ctl, sizeof(LoopCtl));
@@ -1094,6 +1103,7 @@ int ffcz_solver_create(size_t nx, size_t ny, size_t nz, int dtype, ffcz_solver *
     if (e == cudaSuccess) e = cudaMemset(s->d_fedits, 0, H2 * es);
     if (e == cudaSuccess) e = cudaMemset(s->d_fdirty, 0, sizeof(unsigned));
     if (e == cudaSuccess) e = cudaMemset(s->d_sedits, 0, N * es);
+    if (e == cudaSuccess) e = cudaMemset(s->d_sdirty, 0, sizeof(unsigned));
     if (e == cudaSuccess) e = xp_init(s.get());
     if (e != cudaSuccess) rc = cuda_fail(e, "cudaMemset", __FILE__, __LINE__);
   }
@@ -1300,6 +1310,7 @@ int ffcz_reset_edit_accumulators(ffcz_solver *s) {
   FFCZ_CUDA(cudaMemsetAsync(s->d_fedits, 0, 2 * s->H * s->es, s->stream));
   FFCZ_CUDA(cudaMemsetAsync(s->d_fdirty, 0, sizeof(unsigned), s->stream));
   FFCZ_CUDA(cudaMemsetAsync(s->d_sedits, 0, s->N * s->es, s->stream));
+  FFCZ_CUDA(cudaMemsetAsync(s->d_sdirty, 0, sizeof(unsigned), s->stream));
   FFCZ_CUDA(cudaStreamSynchronize(s->stream));
   return FFCZ_OK;
 }
@@ -1771,6 +1782,7 @@ int ffcz_batch_reset_edit_accumulators(ffcz_batch *b) {
     FFCZ_CUDA(cudaMemsetAsync(s->d_fedits, 0, 2 * s->H * s->es, b->stream));
     FFCZ_CUDA(cudaMemsetAsync(s->d_fdirty, 0, sizeof(unsigned), b->stream));
     FFCZ_CUDA(cudaMemsetAsync(s->d_sedits, 0, s->N * s->es, b->stream));
+    FFCZ_CUDA(cudaMemsetAsync(s->d_sdirty, 0, sizeof(unsigned), b->stream));
   }
   FFCZ_CUDA(cudaStreamSynchronize(b->stream));
   return FFCZ_OK;

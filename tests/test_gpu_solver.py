@@ -385,3 +385,41 @@ def test_untouched_frequency_accumulator_compacts_without_reading(cuda, dtype):
         s.reset_edit_accumulators()  # cleared: skipped again
         s.solve_all_abs(e0, 100, 1e-7)
         assert check(s) == 0
+
+
+@pytest.mark.parametrize("loop", ["graph", "host"])
+def test_untouched_spatial_accumulator_compacts_without_reading(cuda, loop):
+    """The spatial accumulator is written only by the clamping prologue of
+    an iteration after a violation and by the final clamp; while neither
+    ran since the accumulator was cleared, its compaction skips reading it.
+    Both cases match the oracle's compaction of the accumulator."""
+    shape = (20, 18, 16)
+    fld = synth.make_field(shape, 11 / 3, 43, 1e-3, 1e-3, np.float32, noise=0.3)
+    e0 = (fld.xp.astype(np.float64) - fld.x.astype(np.float64)).astype(np.float32)
+
+    def check(s):
+        se = s.get_spatial_edits_full()
+        ref = O.extract(se)
+        ns = s.active_counts()[1]
+        assert ns == ref["count"]
+        assert s.minmax()[2:] == (ref["min"], ref["max"])
+        assert np.array_equal(s.get_spatial_flags_pack(), ref["pack"])
+        assert np.array_equal(s.get_active_spatial_quant_edit_distances(), ref["quant"])
+        return ns
+
+    with F.ProjectionSolver(*shape) as s:
+        s.set_loop_driver(F.FFCZ_LOOP_GRAPH if loop == "graph" else F.FFCZ_LOOP_HOST)
+        s.initialize_all_abs(fld.x, 1e30, 1e30)  # converges at once: no clamp
+        assert s.solve_all_abs(e0, 100, 1e-7) == 1
+        assert check(s) == 0 and not s.get_spatial_edits_full().any()
+        s.initialize_all_abs(fld.x, fld.eps, 1e30)  # x' - x exceeds E: clamps
+        assert s.solve_all_abs(e0, 100, 1e-7) > 1
+        assert check(s) > 0
+        s.reset_edit_accumulators()
+        s.initialize_all_abs(fld.x, fld.eps, 1e30)
+        assert s.solve_all_abs(e0, 1, 1e-7) == 1  # stopped by max_iter: final clamp
+        assert check(s) > 0
+        s.reset_edit_accumulators()
+        s.initialize_all_abs(fld.x, 1e30, 1e30)
+        s.solve_all_abs(e0, 100, 1e-7)
+        assert check(s) == 0
