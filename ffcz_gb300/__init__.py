@@ -29,6 +29,7 @@ FFCZ_F32, FFCZ_F64 = 0, 1
 FFCZ_PACK_CORRECT, FFCZ_PACK_REFERENCE = 0, 1
 FFCZ_MODE_ALL_ABS, FFCZ_MODE_DIRECT, FFCZ_MODE_ALL_PTW, FFCZ_MODE_PARTIAL_PTW = 0, 1, 2, 3
 FFCZ_LOOP_GRAPH, FFCZ_LOOP_HOST = 0, 1
+FFCZ_PRECISION_NATIVE, FFCZ_PRECISION_SPLIT = 0, 1
 FFCZ_ZSTD_SINGLE, FFCZ_ZSTD_CHUNKED, FFCZ_ZSTD_NONE = 0, 1, 2
 ERRORS = {-1: "INVALID", -2: "CUDA", -3: "UNSUPPORTED", -4: "NOT_INITIALIZED", -5: "ZSTD",
           -6: "CAPACITY", -7: "CODE_TOO_LONG", -8: "EMPTY", -9: "IO"}
@@ -136,6 +137,7 @@ SIGNATURES = {
     "ffcz_verify_bounds": [_p, C.POINTER(C.c_double), C.POINTER(C.c_double)],
     "ffcz_strict_finish": [_p, _i, _d, _i, _p, _p, _p, _p],
     "ffcz_solver_autotune": [_p, _i, _p],
+    "ffcz_solver_set_precision": [_p, _i],
     "ffcz_init_all_ptw": [_p, _p, _d, _d],
     "ffcz_init_all_ptw_device": [_p, _p, _d, _d],
     "ffcz_init_partial_ptw": [_p, _p, _p, _d, _d, _sz],
@@ -224,6 +226,11 @@ class ProjectionSolver:
 
     def set_loop_driver(self, driver: int) -> None:
         _check(lib().ffcz_solver_set_loop_driver(self._h, driver))
+
+    def set_precision(self, precision: int) -> None:
+        """FFCZ_PRECISION_NATIVE or FFCZ_PRECISION_SPLIT (FP64 solvers:
+        float-float pass kernels on the FP32 pipes where a length has them)."""
+        _check(lib().ffcz_solver_set_precision(self._h, int(precision)))
 
     def set_pack_mode(self, mode: int) -> None:
         _check(lib().ffcz_solver_set_pack_mode(self._h, mode))

@@ -7,6 +7,7 @@
 #include <cstddef>
 #include <cstdint>
 #include <string>
+#include <type_traits>
 
 #include "../../include/ffcz.h"
 
@@ -74,6 +75,103 @@ __host__ __device__ __forceinline__ V cmul_i(V a) {
 }
 template <typename V, typename S>
 __host__ __device__ __forceinline__ V cscale(V a, S s) { a.x *= s; a.y *= s; return a; }
+
+// ------------------------------------------------------- float-float --
+// Split-precision scalar for FP64 data computed on the FP32 pipes: value =
+// hi + lo, |lo| <= ulp(hi)/2, a 48-bit significand (relative rounding about
+// 2^-47 per operation instead of 2^-53).  Error-free transformations of
+// Knuth (two-sum) and Dekker (fast two-sum), products through one rounded
+// product and FMAs for the error term; every step rounded on its own (no
+// contraction, no reassociation).
+struct ff {
+  float hi, lo;
+  ff() = default;
+  __host__ __device__ constexpr ff(float h, float l) : hi(h), lo(l) {}
+  // from a double (a literal folds at compile time)
+  __host__ __device__ constexpr ff(double d) : hi((float)d), lo((float)(d - (double)(float)d)) {}
+  __host__ __device__ constexpr ff(int i) : ff((double)i) {}
+};
+__host__ __device__ __forceinline__ float ff_add(float a, float b) {
+#ifdef __CUDA_ARCH__
+  return __fadd_rn(a, b);
+#else
+  volatile float r = a + b;
+  return r;
+#endif
+}
+__host__ __device__ __forceinline__ float ff_sub(float a, float b) {
+#ifdef __CUDA_ARCH__
+  return __fsub_rn(a, b);
+#else
+  volatile float r = a - b;
+  return r;
+#endif
+}
+__host__ __device__ __forceinline__ float ff_mul(float a, float b) {
+#ifdef __CUDA_ARCH__
+  return __fmul_rn(a, b);
+#else
+  volatile float r = a * b;
+  return r;
+#endif
+}
+__host__ __device__ __forceinline__ float ff_fma(float a, float b, float c) {
+#ifdef __CUDA_ARCH__
+  return __fmaf_rn(a, b, c);
+#else
+  return fmaf(a, b, c);
+#endif
+}
+// s + e = a + b exactly, |e| <= ulp(s)/2 (needs |a| >= |b| or a == 0)
+__host__ __device__ __forceinline__ ff ff_fast_two_sum(float a, float b) {
+  const float s = ff_add(a, b);
+  return ff(s, ff_sub(b, ff_sub(s, a)));
+}
+__host__ __device__ __forceinline__ ff operator+(ff a, ff b) {
+  const float s = ff_add(a.hi, b.hi);
+  const float bb = ff_sub(s, a.hi);
+  float e = ff_add(ff_sub(a.hi, ff_sub(s, bb)), ff_sub(b.hi, bb));  // two-sum error
+  e = ff_add(e, ff_add(a.lo, b.lo));
+  return ff_fast_two_sum(s, e);
+}
+__host__ __device__ __forceinline__ ff operator-(ff a) { return ff(-a.hi, -a.lo); }
+__host__ __device__ __forceinline__ ff operator-(ff a, ff b) { return a + (-b); }
+__host__ __device__ __forceinline__ ff operator*(ff a, ff b) {
+  const float p = ff_mul(a.hi, b.hi);
+  float e = ff_fma(a.hi, b.hi, -p);  // exact error of the rounded product
+  e = ff_fma(a.hi, b.lo, e);
+  e = ff_fma(a.lo, b.hi, e);
+  return ff_fast_two_sum(p, e);
+}
+__host__ __device__ __forceinline__ ff &operator+=(ff &a, ff b) { return a = a + b; }
+__host__ __device__ __forceinline__ ff &operator-=(ff &a, ff b) { return a = a - b; }
+__host__ __device__ __forceinline__ ff &operator*=(ff &a, ff b) { return a = a * b; }
+__host__ __device__ __forceinline__ double ff_to_double(ff a) { return (double)a.hi + (double)a.lo; }
+
+struct ffc {
+  ff x, y;
+};
+template <> struct C2<ff> { using type = ffc; };
+
+// Complex conversions between a storage type and a compute type (identity
+// unless one side is ff).
+template <typename To, typename VF>
+__host__ __device__ __forceinline__ c2<To> cvt(const VF &a) {
+  using From = std::remove_cv_t<decltype(a.x)>;
+  if constexpr (std::is_same<To, From>::value) {
+    return a;
+  } else if constexpr (std::is_same<To, ff>::value) {
+    c2<To> r;
+    r.x = ff((double)a.x);
+    r.y = ff((double)a.y);
+    return r;
+  } else {
+    c2<To> r;
+    r.x = (To)ff_to_double(a.x);
+    r.y = (To)ff_to_double(a.y);
+    return r;
+  }
+}
 
 // ---------------------------------------------------------- loop control --
 // Device-resident state of one solve.  viol_bits holds the bit pattern of

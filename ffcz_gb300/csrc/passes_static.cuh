@@ -200,8 +200,8 @@ template <int DIR, typename V> struct Dft<30, DIR, V> : DftPfa<2, 15, DIR, V> {}
 
 // Butterflies of one stage on the thread's registers: v[m*R + r] is input
 // r of butterfly m (j = t + m*TC) and becomes output r.
-template <typename T, int DIR, int R, int NS, int L, int E, bool VEC>
-__device__ __forceinline__ void rstage(c2<T> (&v)[E], int t, const c2<T> *__restrict__ tw) {
+template <typename T, int DIR, int R, int NS, int L, int E, bool VEC, typename TS = T>
+__device__ __forceinline__ void rstage(c2<T> (&v)[E], int t, const c2<TS> *__restrict__ tw) {
   using V = c2<T>;
   constexpr int TC = L / E;
 #pragma unroll
@@ -209,9 +209,9 @@ __device__ __forceinline__ void rstage(c2<T> (&v)[E], int t, const c2<T> *__rest
     if (NS > 1) {
       const int j = t + m * TC;
       if constexpr (VEC) {
-        const V *w = tw + (j % NS) * R;
+        const c2<TS> *w = tw + (j % NS) * R;
         V ww[R];
-        if (sizeof(T) == 4) {
+        if constexpr (sizeof(TS) == 4) {
 #pragma unroll
           for (int r = 0; r < R; r += 2) {
             const float4 q = *reinterpret_cast<const float4 *>(w + r);
@@ -220,15 +220,15 @@ __device__ __forceinline__ void rstage(c2<T> (&v)[E], int t, const c2<T> *__rest
           }
         } else {
 #pragma unroll
-          for (int r = 1; r < R; ++r) ww[r] = w[r];
+          for (int r = 1; r < R; ++r) ww[r] = cvt<T>(w[r]);
         }
 #pragma unroll
         for (int r = 1; r < R; ++r) v[m * R + r] = (DIR < 0) ? cmul(v[m * R + r], ww[r]) : cmulc(v[m * R + r], ww[r]);
       } else {
-        const V *w = tw + (j % NS) * (R - 1);
+        const c2<TS> *w = tw + (j % NS) * (R - 1);
 #pragma unroll
         for (int r = 1; r < R; ++r) {
-          const V ww = w[r - 1];
+          const V ww = cvt<T>(w[r - 1]);
           v[m * R + r] = (DIR < 0) ? cmul(v[m * R + r], ww) : cmulc(v[m * R + r], ww);
         }
       }
@@ -295,14 +295,15 @@ __device__ __forceinline__ int out_pos(int t, int m, int r) {
 // Runs stages S..end of direction DIR; v holds stage S's inputs.  Between
 // stages the data goes through shared memory (layout LY).  On return v
 // holds the last stage's outputs (positions out_pos of that stage).
-template <typename T, int DIR, int L, typename LY, int S, int CAP = 16>
+// T: register / shared-memory type; TS: type of the twiddle table.
+template <typename T, int DIR, int L, typename LY, int S, int CAP = 16, typename TS = T>
 struct RRun {
   static constexpr int E = rp_elems(L, CAP);
   static __device__ __forceinline__ void run(c2<T> (&v)[E], c2<T> *buf, int t, int c, const AxisPlan &p) {
     if constexpr (S < rp_nst(L, CAP)) {
       constexpr int R = rp_rad(L, DIR, S, CAP), LG = rp_ns(L, DIR, S, CAP);
-      const c2<T> *tw = (const c2<T> *)p.tw + p.twoff[(DIR < 0 ? 0 : kInvBase) + S];
-      rstage<T, DIR, R, LG, L, E, tw_paired(CAP, R)>(v, t, tw);
+      const c2<TS> *tw = (const c2<TS> *)p.tw + p.twoff[(DIR < 0 ? 0 : kInvBase) + S];
+      rstage<T, DIR, R, LG, L, E, tw_paired(CAP, R), TS>(v, t, tw);
       if constexpr (S + 1 < rp_nst(L, CAP)) {
         constexpr int R2 = rp_rad(L, DIR, S + 1, CAP);
 #pragma unroll
@@ -315,7 +316,7 @@ struct RRun {
 #pragma unroll
           for (int r = 0; r < R2; ++r) v[m * R2 + r] = buf[LY::idx(in_pos<L, E, R2>(t, m, r), c)];
         __syncthreads();
-        RRun<T, DIR, L, LY, S + 1, CAP>::run(v, buf, t, c, p);
+        RRun<T, DIR, L, LY, S + 1, CAP, TS>::run(v, buf, t, c, p);
       }
     }
   }
@@ -352,11 +353,15 @@ __host__ __device__ constexpr int strided_minb(int es, int nt, int E) {
 // ---------------------------------------------------------------------------
 // Strided C2C pass.  Block = TC threads per column x TW columns (c fastest
 // across lanes, so each row access is TW contiguous complex values).
-template <typename T, int MODE, int L, int LGTW, int CAP = 16>
+// SPLIT (FP64 data): registers and shared memory in float-float, loads,
+// stores, twiddle table and clamps in FP64.
+template <typename T, int MODE, int L, int LGTW, int CAP = 16, bool SPLIT = false>
 __global__ void __launch_bounds__((L / rp_elems(L, CAP)) << LGTW,
                                   strided_minb(sizeof(T), (L / rp_elems(L, CAP)) << LGTW, rp_elems(L, CAP)))
     ks_strided(c2<T> *__restrict__ spec, SArgs s, AxisPlan p, ClampArgs<T> ca, T *__restrict__ fedits, long long H) {
-  using V = c2<T>;
+  using C = std::conditional_t<SPLIT, ff, T>;
+  using V = c2<C>;
+  using VG = c2<T>;
   constexpr int E = rp_elems(L, CAP), TW = 1 << LGTW;
   using LY = ColLayout<sl_p(L, TW, sizeof(T)), sl_b(L, TW, sizeof(T))>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -371,20 +376,31 @@ __global__ void __launch_bounds__((L / rp_elems(L, CAP)) << LGTW,
   const int kb = rem - q * s.tpq;
   const int kz0 = kb * TW;
   const bool live = c < s.Hz - kz0;
-  const V *src = spec + bb * (long long)L * s.Wtot + (long long)q * s.Hzp + kz0 + c;
+  const VG *src = spec + bb * (long long)L * s.Wtot + (long long)q * s.Hzp + kz0 + c;
   constexpr int D0 = (MODE == MODE_INV) ? +1 : -1;
   V v[E];
 #pragma unroll
   for (int i = 0; i < E; ++i)
-    v[i] = live ? src[(long long)first_pos<L, D0, CAP>(t, i) * s.Wtot] : mkc<T>(T(0), T(0));
-  RRun<T, D0, L, LY, 0, CAP>::run(v, buf, t, c, p);
+    v[i] = live ? cvt<C>(src[(long long)first_pos<L, D0, CAP>(t, i) * s.Wtot]) : mkc<C>(C(0), C(0));
+  RRun<C, D0, L, LY, 0, CAP, T>::run(v, buf, t, c, p);
   if (MODE == MODE_FCI || MODE == MODE_FCIX) {
     if (live) {
 #pragma unroll
       for (int i = 0; i < E; ++i) {
         const int l = last_pos<L, -1, CAP>(t, i);
         const long long k = ((bb * L + l) * (long long)s.Q + q) * s.Hz + kz0 + c;
-        if (MODE == MODE_FCI) {
+        if constexpr (SPLIT) {  // the box in FP64; unclamped values keep their split form
+          const VG g = cvt<T>(v[i]);
+          VG h;
+          if (MODE == MODE_FCI) {
+            h = freq_clamp<T>(g, ca.delta, fedits, k, H, ca.fdirty);
+          } else {
+            const long long pad = (bb * L + l) * s.Wtot + (long long)q * s.Hzp + kz0 + c;
+            h = freq_project<T>(g, ca, fedits, k, pad, H);
+          }
+          if (h.x != g.x) v[i].x = C((double)h.x);
+          if (h.y != g.y) v[i].y = C((double)h.y);
+        } else if (MODE == MODE_FCI) {
           v[i] = freq_clamp<T>(v[i], ca.delta, fedits, k, H, ca.fdirty);
         } else {
           const long long pad = (bb * L + l) * s.Wtot + (long long)q * s.Hzp + kz0 + c;
@@ -396,25 +412,27 @@ __global__ void __launch_bounds__((L / rp_elems(L, CAP)) << LGTW,
     // stage wrote, so the same registers continue.  A barrier separates the
     // forward's last shared reads from the inverse's first shared writes.
     __syncthreads();
-    RRun<T, +1, L, LY, 0, CAP>::run(v, buf, t, c, p);
+    RRun<C, +1, L, LY, 0, CAP, T>::run(v, buf, t, c, p);
   }
   constexpr int DL = (MODE == MODE_FWD) ? -1 : +1;
-  V *dst = spec + bb * (long long)L * s.Wtot + (long long)q * s.Hzp + kz0 + c;
+  VG *dst = spec + bb * (long long)L * s.Wtot + (long long)q * s.Hzp + kz0 + c;
   if (live) {
 #pragma unroll
-    for (int i = 0; i < E; ++i) dst[(long long)last_pos<L, DL, CAP>(t, i) * s.Wtot] = v[i];
+    for (int i = 0; i < E; ++i) dst[(long long)last_pos<L, DL, CAP>(t, i) * s.Wtot] = cvt<T>(v[i]);
   }
 }
 
 // ---------------------------------------------------------------------------
 // R2C along z (Nz = 2M): TC = M/E threads per row x TW rows (t fastest
 // across lanes: each load is a run of consecutive complex values of one row).
-template <typename T, int PRO, int M, int LGTW>
+template <typename T, int PRO, int M, int LGTW, bool SPLIT = false>
 __global__ void __launch_bounds__((M / rp_elems(M, 8)) << LGTW) ks_zfwd(const T *__restrict__ a, const T *__restrict__ b,
                                                           T *__restrict__ sedits, T eps,
                                                           c2<T> *__restrict__ spec, ZArgs z, AxisPlan p,
                                                           const c2<T> *__restrict__ post) {
-  using V = c2<T>;
+  using C = std::conditional_t<SPLIT, ff, T>;  // float-float for split FP64
+  using V = c2<C>;
+  using VG = c2<T>;
   constexpr int E = rp_elems(M, 8), TC = M / E;
   using LY = RowLayout<row_pitch(M, sizeof(T)), zl_b(M, sizeof(T))>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -424,17 +442,17 @@ __global__ void __launch_bounds__((M / rp_elems(M, 8)) << LGTW) ks_zfwd(const T 
   const long long row = (long long)blockIdx.x * (1 << LGTW) + c;
   const bool live = row < z.rows;
   const long long rbase = row * (long long)(2 * M);
-  V v[E];
+  VG g[E];  // prologue in the storage type
 #pragma unroll
   for (int i = 0; i < E; ++i) {
-    v[i] = mkc<T>(T(0), T(0));
+    g[i] = mkc<T>(T(0), T(0));
     if (live) {
       const long long gi = rbase + 2 * first_pos<M, -1, 8>(t, i);
-      v[i] = *reinterpret_cast<const V *>(a + gi);
+      g[i] = *reinterpret_cast<const VG *>(a + gi);
       if (PRO == PRO_DIFF) {
-        const V w = *reinterpret_cast<const V *>(b + gi);
-        v[i].x -= w.x;
-        v[i].y -= w.y;
+        const VG w = *reinterpret_cast<const VG *>(b + gi);
+        g[i].x -= w.x;
+        g[i].y -= w.y;
       }
     }
   }
@@ -442,11 +460,14 @@ __global__ void __launch_bounds__((M / rp_elems(M, 8)) << LGTW) ks_zfwd(const T 
 #pragma unroll
     for (int i = 0; i < E; ++i) {
       const long long gi = rbase + 2 * first_pos<M, -1, 8>(t, i);
-      v[i].x = spatial_clamp(v[i].x, eps, sedits, gi);
-      v[i].y = spatial_clamp(v[i].y, eps, sedits, gi + 1);
+      g[i].x = spatial_clamp(g[i].x, eps, sedits, gi);
+      g[i].y = spatial_clamp(g[i].y, eps, sedits, gi + 1);
     }
   }
-  RRun<T, -1, M, LY, 0, 8>::run(v, buf, t, c, p);
+  V v[E];
+#pragma unroll
+  for (int i = 0; i < E; ++i) v[i] = cvt<C>(g[i]);
+  RRun<C, -1, M, LY, 0, 8, T>::run(v, buf, t, c, p);
   // Z in natural order to shared memory, then the real-to-complex split of
   // row c: X[k] = (Z[k] + conj Z[M-k])/2 - i W^k (Z[k] - conj Z[M-k])/2.
   if (rp_nst(M, 8) > 1) __syncthreads();
@@ -454,20 +475,20 @@ __global__ void __launch_bounds__((M / rp_elems(M, 8)) << LGTW) ks_zfwd(const T 
   for (int i = 0; i < E; ++i) buf[LY::idx(last_pos<M, -1, 8>(t, i), c)] = v[i];
   __syncthreads();
   if (!live) return;
-  V *out = spec + row * (long long)z.Hzp;
+  VG *out = spec + row * (long long)z.Hzp;
   for (int k = t; k <= M; k += TC) {
     const int k1 = (k == M) ? 0 : k;
     const int k2 = (k == 0) ? 0 : M - k;
     const V A = buf[LY::idx(k1, c)];
     const V B = cconj(buf[LY::idx(k2, c)]);
-    const V w = post[k];
+    const V w = cvt<C>(post[k]);
     const V sm = cadd(A, B);
     const V d = csub(A, B);
-    const V tt = cmul(mkc<T>(-w.y, w.x), d);
+    const V tt = cmul(mkc<C>(-w.y, w.x), d);
     V X;
-    X.x = T(0.5) * (sm.x - tt.x);
-    X.y = T(0.5) * (sm.y - tt.y);
-    out[k] = X;
+    X.x = C(0.5) * (sm.x - tt.x);
+    X.y = C(0.5) * (sm.y - tt.y);
+    out[k] = cvt<T>(X);
   }
 }
 
@@ -476,11 +497,13 @@ __global__ void __launch_bounds__((M / rp_elems(M, 8)) << LGTW) ks_zfwd(const T 
 // (the row is read by the block, so the second read mostly hits L1) and
 // forms Z[k] = (X[k] + conj X[M-k]) + i W^-k (X[k] - conj X[M-k]) in
 // registers (imaginary parts of X[0] and X[M] ignored).
-template <typename T, int M, int LGTW>
+template <typename T, int M, int LGTW, bool SPLIT = false>
 __global__ void __launch_bounds__((M / rp_elems(M, 8)) << LGTW) ks_zinv(const c2<T> *__restrict__ spec, T *__restrict__ e,
                                                           T eps, T factor, LoopCtl *ctl, ZArgs z, AxisPlan p,
                                                           const c2<T> *__restrict__ post) {
-  using V = c2<T>;
+  using C = std::conditional_t<SPLIT, ff, T>;  // float-float for split FP64
+  using V = c2<C>;
+  using VG = c2<T>;
   constexpr int E = rp_elems(M, 8), TC = M / E;
   using LY = RowLayout<row_pitch(M, sizeof(T)), zl_b(M, sizeof(T))>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -489,42 +512,43 @@ __global__ void __launch_bounds__((M / rp_elems(M, 8)) << LGTW) ks_zinv(const c2
   const int c = threadIdx.x / TC;
   const long long row = (long long)blockIdx.x * (1 << LGTW) + c;
   const bool live = row < z.rows;
-  const V *in = spec + row * (long long)z.Hzp;
+  const VG *in = spec + row * (long long)z.Hzp;
   V v[E];
   if (live) {
     V xa[E], xb[E];
 #pragma unroll
     for (int i = 0; i < E; ++i) {
       const int k = first_pos<M, +1, 8>(t, i);
-      xa[i] = in[k];
-      xb[i] = in[M - k];
+      xa[i] = cvt<C>(in[k]);
+      xb[i] = cvt<C>(in[M - k]);
     }
 #pragma unroll
     for (int i = 0; i < E; ++i) {
       const int k = first_pos<M, +1, 8>(t, i);
       if (k == 0) {
-        v[i] = mkc<T>(xa[i].x + xb[i].x, xa[i].x - xb[i].x);
+        v[i] = mkc<C>(xa[i].x + xb[i].x, xa[i].x - xb[i].x);
       } else {
-        const V w = post[k];
+        const V w = cvt<C>(post[k]);
         const V s1 = cadd(xa[i], cconj(xb[i]));
         const V d1 = csub(xa[i], cconj(xb[i]));
-        v[i] = cadd(s1, cmul(mkc<T>(w.y, w.x), d1));
+        v[i] = cadd(s1, cmul(mkc<C>(w.y, w.x), d1));
       }
     }
   } else {
 #pragma unroll
-    for (int i = 0; i < E; ++i) v[i] = mkc<T>(T(0), T(0));
+    for (int i = 0; i < E; ++i) v[i] = mkc<C>(C(0), C(0));
   }
-  RRun<T, +1, M, LY, 0, 8>::run(v, buf, t, c, p);
+  RRun<C, +1, M, LY, 0, 8, T>::run(v, buf, t, c, p);
   T vmax = T(0);
   if (live) {
     T *out = e + row * (long long)(2 * M);
 #pragma unroll
     for (int i = 0; i < E; ++i) {
-      V o;
-      o.x = v[i].x * factor;
-      o.y = v[i].y * factor;
-      *reinterpret_cast<V *>(out + 2 * last_pos<M, +1, 8>(t, i)) = o;
+      const VG u = cvt<T>(v[i]);
+      VG o;
+      o.x = u.x * factor;
+      o.y = u.y * factor;
+      *reinterpret_cast<VG *>(out + 2 * last_pos<M, +1, 8>(t, i)) = o;
       const T a0 = fabs(o.x), a1 = fabs(o.y);
       if (a0 > eps) vmax = max(vmax, a0 - eps);
       if (a1 > eps) vmax = max(vmax, a1 - eps);

@@ -113,6 +113,7 @@ struct ffcz_solver {
   bool z_generic = true, y_generic = true, x_generic = true;  // runtime-planned tile fits
   int z_ept = 0, y_ept = 0, x_ept = 0;  // values per thread of the runtime-planned tiles
   int zvar = 0, yvar = 0, xvar = 0;     // tile variant of each compile-time pass
+  int split = 0;                        // FP64: float-float pass kernels where they exist
   double tune_ms[6] = {};               // autotuner: (default, alternative) ms of z, y, x
   int kernel_gen = 0;                   // bumped when the autotuner swaps kernels
   // parameters
@@ -220,8 +221,13 @@ bool apply_static_z(ffcz_solver *s, int var) {
   StaticGeom g;
   ZfwdFn<T> f[3];
   ZinvFn<T> fi;
-  bool ok = static_zinv<T>(s->M, fi, g, var);
-  for (int pro = 0; pro < 3 && ok; ++pro) ok = static_zfwd<T>(s->M, pro, f[pro], g, var);
+  bool ok = false;
+  // float-float kernels first when the solver asks for them and the length
+  // has them, then the native ones
+  for (int split = s->split; split >= 0 && !ok; --split) {
+    ok = static_zinv<T>(s->M, fi, g, var, split);
+    for (int pro = 0; pro < 3 && ok; ++pro) ok = static_zfwd<T>(s->M, pro, f[pro], g, var, split);
+  }
   if (!ok) return false;
   for (int pro = 0; pro < 3; ++pro) s->kzf[pro] = (void *)f[pro];
   s->kzi = (void *)fi;
@@ -249,8 +255,11 @@ bool apply_static_strided(ffcz_solver *s, int axis, int var) {
   if (ps.nst == 0) return false;
   StaticGeom g[4];
   StridedFn<T> f[4];
-  bool ok = true;
-  for (int m = 0; m < 4 && ok; ++m) ok = static_strided<T>(L, m, f[m], g[m], var);
+  bool ok = false;
+  for (int split = s->split; split >= 0 && !ok; --split) {
+    ok = true;
+    for (int m = 0; m < 4 && ok; ++m) ok = static_strided<T>(L, m, f[m], g[m], var, split);
+  }
   if (!ok) return false;
   for (int m = 0; m < 4; ++m) k[m] = (void *)f[m];
   // plain passes: geometry of MODE_FWD (= MODE_INV); fused: of MODE_FCI
@@ -1448,6 +1457,21 @@ int ffcz_get_device_array(ffcz_solver *s, int which, void **dptr, size_t *bytes)
   }
   *dptr = p;
   if (bytes) *bytes = b;
+  return FFCZ_OK;
+}
+
+int ffcz_solver_set_precision(ffcz_solver *s, int precision) {
+  FFCZ_TRY(check_solver(s));
+  if (precision != FFCZ_PRECISION_NATIVE && precision != FFCZ_PRECISION_SPLIT)
+    return fail(FFCZ_ERR_INVALID, "unknown precision");
+  if (s->dtype != FFCZ_F64)
+    return precision == FFCZ_PRECISION_NATIVE ? FFCZ_OK
+                                               : fail(FFCZ_ERR_UNSUPPORTED, "split precision applies to FP64 solvers");
+  FFCZ_CUDA(cudaStreamSynchronize(s->stream));
+  s->split = precision == FFCZ_PRECISION_SPLIT ? 1 : 0;
+  FFCZ_TRY(select_kernels<double>(s));
+  for (LoopGraph &g : s->lg) g.reset();  // the cached loops hold the previous kernels
+  ++s->kernel_gen;
   return FFCZ_OK;
 }
 

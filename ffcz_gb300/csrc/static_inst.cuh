@@ -47,24 +47,24 @@ int set_smem(F fn, size_t smem) {
   return FFCZ_OK;
 }
 
-template <typename T, int M, int VAR>
+template <typename T, int M, int VAR, bool SPLIT = false>
 bool zfwd_for(int pro, ZfwdFn<T> &fn, StaticGeom &g) {
   using C = Cfg<T, M, 8, VAR>;
   if (VAR && C::TW == Cfg<T, M, 8, 0>::TW) return false;  // same tile as the default
-  if (pro == PRO_PLAIN) fn = ks_zfwd<T, PRO_PLAIN, M, C::LGTW>;
-  else if (pro == PRO_DIFF) fn = ks_zfwd<T, PRO_DIFF, M, C::LGTW>;
-  else fn = ks_zfwd<T, PRO_CLAMP, M, C::LGTW>;
+  if (pro == PRO_PLAIN) fn = ks_zfwd<T, PRO_PLAIN, M, C::LGTW, SPLIT>;
+  else if (pro == PRO_DIFF) fn = ks_zfwd<T, PRO_DIFF, M, C::LGTW, SPLIT>;
+  else fn = ks_zfwd<T, PRO_CLAMP, M, C::LGTW, SPLIT>;
   g.TW = C::TW;
   g.threads = C::NT;
   g.smem = (size_t)C::TW * row_pitch(M, sizeof(T)) * sizeof(c2<T>);
   return set_smem(fn, g.smem) == FFCZ_OK;
 }
 
-template <typename T, int M, int VAR>
+template <typename T, int M, int VAR, bool SPLIT = false>
 bool zinv_for(ZinvFn<T> &fn, StaticGeom &g) {
   using C = Cfg<T, M, 8, VAR>;
   if (VAR && C::TW == Cfg<T, M, 8, 0>::TW) return false;
-  fn = ks_zinv<T, M, C::LGTW>;
+  fn = ks_zinv<T, M, C::LGTW, SPLIT>;
   g.TW = C::TW;
   g.threads = C::NT;
   g.smem = (size_t)C::TW * row_pitch(M, sizeof(T)) * sizeof(c2<T>);
@@ -73,28 +73,36 @@ bool zinv_for(ZinvFn<T> &fn, StaticGeom &g) {
 
 // The plain passes (forward, inverse) take the plain_cap(L) stage list, the
 // fused ones (forward + clamp + inverse) the CAP 16 list.
-template <typename T, int L, int VAR, bool FUSED>
+template <typename T, int L, int VAR, bool FUSED, bool SPLIT = false>
 bool strided_for_family(int mode, StridedFn<T> &fn, StaticGeom &g) {
   constexpr int CAP = FUSED ? 16 : plain_cap(L);
   using C = Cfg<T, L, CAP, VAR>;
   if (VAR && C::TW == Cfg<T, L, CAP, 0>::TW) return false;
   if constexpr (FUSED) {
-    if (mode == MODE_FCI) fn = ks_strided<T, MODE_FCI, L, C::LGTW, CAP>;
-    else fn = ks_strided<T, MODE_FCIX, L, C::LGTW, CAP>;
+    if (mode == MODE_FCI) fn = ks_strided<T, MODE_FCI, L, C::LGTW, CAP, SPLIT>;
+    else fn = ks_strided<T, MODE_FCIX, L, C::LGTW, CAP, SPLIT>;
   } else {
-    if (mode == MODE_FWD) fn = ks_strided<T, MODE_FWD, L, C::LGTW, CAP>;
-    else fn = ks_strided<T, MODE_INV, L, C::LGTW, CAP>;
+    if (mode == MODE_FWD) fn = ks_strided<T, MODE_FWD, L, C::LGTW, CAP, SPLIT>;
+    else fn = ks_strided<T, MODE_INV, L, C::LGTW, CAP, SPLIT>;
   }
   g.TW = C::TW;
   g.threads = C::NT;
   g.smem = (size_t)sl_size(L, C::TW, sizeof(T)) * sizeof(c2<T>);
   return set_smem(fn, g.smem) == FFCZ_OK;
 }
-template <typename T, int L, int VAR>
+template <typename T, int L, int VAR, bool SPLIT = false>
 bool strided_for(int mode, StridedFn<T> &fn, StaticGeom &g) {
-  return (mode == MODE_FWD || mode == MODE_INV) ? strided_for_family<T, L, VAR, false>(mode, fn, g)
-                                                : strided_for_family<T, L, VAR, true>(mode, fn, g);
+  return (mode == MODE_FWD || mode == MODE_INV) ? strided_for_family<T, L, VAR, false, SPLIT>(mode, fn, g)
+                                                : strided_for_family<T, L, VAR, true, SPLIT>(mode, fn, g);
 }
+
+// The float-float kernels (FP64 storage) are instantiated in their own
+// translation unit for the power-of-two lengths 128..512 (their fully
+// unrolled float-float butterflies grow the code about tenfold; compiling
+// longer or mixed-radix lists takes minutes each).
+template <typename T> bool split_zfwd(int M, int pro, ZfwdFn<T> &fn, StaticGeom &g, int var);
+template <typename T> bool split_zinv(int M, ZinvFn<T> &fn, StaticGeom &g, int var);
+template <typename T> bool split_strided(int L, int mode, StridedFn<T> &fn, StaticGeom &g, int var);
 
 #define CASES_F32(X)                                                                                      \
   X(16) X(32) X(64) X(128) X(256) X(512) X(1024) X(2048) X(4096) X(96) X(100) X(192) X(200) X(250) X(384)  \
@@ -103,21 +111,24 @@ bool strided_for(int mode, StridedFn<T> &fn, StaticGeom &g) {
 
 #define DEFINE_LOOKUPS(T, CASES)                                                  \
   template <>                                                                     \
-  bool static_zfwd<T>(int M, int pro, ZfwdFn<T> &fn, StaticGeom &g, int var) {    \
+  bool static_zfwd<T>(int M, int pro, ZfwdFn<T> &fn, StaticGeom &g, int var, int split) { \
+    if (split) return split_zfwd<T>(M, pro, fn, g, var);                          \
     switch (M) {                                                                  \
       CASES(ZF)                                                                   \
       default: return false;                                                      \
     }                                                                             \
   }                                                                               \
   template <>                                                                     \
-  bool static_zinv<T>(int M, ZinvFn<T> &fn, StaticGeom &g, int var) {             \
+  bool static_zinv<T>(int M, ZinvFn<T> &fn, StaticGeom &g, int var, int split) {  \
+    if (split) return split_zinv<T>(M, fn, g, var);                               \
     switch (M) {                                                                  \
       CASES(ZI)                                                                   \
       default: return false;                                                      \
     }                                                                             \
   }                                                                               \
   template <>                                                                     \
-  bool static_strided<T>(int L, int mode, StridedFn<T> &fn, StaticGeom &g, int var) { \
+  bool static_strided<T>(int L, int mode, StridedFn<T> &fn, StaticGeom &g, int var, int split) { \
+    if (split) return split_strided<T>(L, mode, fn, g, var);                      \
     switch (L) {                                                                  \
       CASES(ST)                                                                   \
       default: return false;                                                      \
@@ -128,5 +139,11 @@ bool strided_for(int mode, StridedFn<T> &fn, StaticGeom &g) {
 #define ZI(n) case n: return var ? zinv_for<TT, n, 1>(fn, g) : zinv_for<TT, n, 0>(fn, g);
 #define ST(n) case n: return var ? strided_for<TT, n, 1>(mode, fn, g) : strided_for<TT, n, 0>(mode, fn, g);
 
+#define CASES_SPLIT(X) X(128) X(256) X(512)
+#define ZFS(n) case n: return var ? zfwd_for<double, n, 1, true>(pro, fn, g) : zfwd_for<double, n, 0, true>(pro, fn, g);
+#define ZIS(n) case n: return var ? zinv_for<double, n, 1, true>(fn, g) : zinv_for<double, n, 0, true>(fn, g);
+#define STS(n)                                                                 \
+  case n:                                                                      \
+    return var ? strided_for<double, n, 1, true>(mode, fn, g) : strided_for<double, n, 0, true>(mode, fn, g);
 
 }  // namespace ffcz

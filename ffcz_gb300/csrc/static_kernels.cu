@@ -38,6 +38,10 @@ void build_static_plan(int L, int cap, AxisPlan &p, std::vector<std::complex<dou
   }
 }
 
+template <> bool split_zfwd<float>(int, int, ZfwdFn<float> &, StaticGeom &, int) { return false; }
+template <> bool split_zinv<float>(int, ZinvFn<float> &, StaticGeom &, int) { return false; }
+template <> bool split_strided<float>(int, int, StridedFn<float> &, StaticGeom &, int) { return false; }
+
 #define TT float
 DEFINE_LOOKUPS(float, CASES_F32)
 #undef TT

@@ -37,9 +37,11 @@ int static_plain_cap(int L);
 // Kernel for a length static_length() accepts (false otherwise).
 // z passes: M = Nz/2; pro is PRO_PLAIN/PRO_DIFF/PRO_CLAMP.
 // var 0: the default tile; var 1: the autotuner's alternative tile width
-// (false when it equals the default's).
-template <typename T> bool static_zfwd(int M, int pro, ZfwdFn<T> &fn, StaticGeom &g, int var = 0);
-template <typename T> bool static_zinv(int M, ZinvFn<T> &fn, StaticGeom &g, int var = 0);
-template <typename T> bool static_strided(int L, int mode, StridedFn<T> &fn, StaticGeom &g, int var = 0);
+// (false when it equals the default's).  split (FP64 only): the kernels that
+// compute in float-float on the FP32 pipes.
+template <typename T> bool static_zfwd(int M, int pro, ZfwdFn<T> &fn, StaticGeom &g, int var = 0, int split = 0);
+template <typename T> bool static_zinv(int M, ZinvFn<T> &fn, StaticGeom &g, int var = 0, int split = 0);
+template <typename T>
+bool static_strided(int L, int mode, StridedFn<T> &fn, StaticGeom &g, int var = 0, int split = 0);
 
 }  // namespace ffcz

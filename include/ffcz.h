@@ -210,6 +210,18 @@ int ffcz_get_device_array(ffcz_solver *s, int which, void **dptr,
  * accumulators are cleared.  ms6 (may be NULL) receives the (default,
  * alternative) ms of z, y and x, 0 where a pass has no alternative. */
 int ffcz_solver_autotune(ffcz_solver *s, int reps, double *ms6);
+/* Arithmetic of an FP64 solver's pass kernels (an addition; the reference
+ * computes in cuFFT double).  FFCZ_PRECISION_NATIVE (default): FP64.
+ * FFCZ_PRECISION_SPLIT: the compile-time pass kernels of the power-of-two
+ * lengths 128..512 keep FP64 in memory but compute in float-float (pairs of
+ * FP32 values, ~48-bit significand, relative rounding ~1e-14 per operation)
+ * on the FP32 pipes; other lengths stay FP64; the frequency and spatial
+ * boxes and the violation are evaluated in FP64; ffcz_verify_bounds and
+ * ffcz_strict_finish keep checking in FP64.  Reselects the kernels (the
+ * autotuner's choice is reset).  FP32 solvers accept NATIVE only. */
+#define FFCZ_PRECISION_NATIVE 0
+#define FFCZ_PRECISION_SPLIT  1
+int ffcz_solver_set_precision(ffcz_solver *s, int precision);
 /* FP64 check of the last solve's corrected error e on the device (no
  * counterpart in the reference): e widened exactly to FP64, its R2C in FP64
  * by an FP64 twin of the solver (created on first use), and

@@ -423,3 +423,44 @@ def test_untouched_spatial_accumulator_compacts_without_reading(cuda, loop):
         s.initialize_all_abs(fld.x, 1e30, 1e30)
         s.solve_all_abs(e0, 100, 1e-7)
         assert check(s) == 0
+
+
+@pytest.mark.parametrize("shape", [(8, 128, 256), (4, 256, 512), (2, 512, 128)])
+def test_fp64_split_precision_against_fp64_oracle(cuda, shape):
+    """FP64 fields with the float-float pass kernels (FP64 storage, boxes and
+    violation in FP64): the corrected error and the edits stay within 1e-11
+    (relative to the field's scale, per iteration) of the FP64 oracle and of
+    the native FP64 solver; the FP64 device check of the bounds still
+    holds."""
+    fld = synth.make_field(shape, 11 / 3, 23, 1e-3, 1e-3, np.float64, noise=0.3)
+    delta = synth.stress_delta(fld, 1.0)
+    e0 = fld.xp - fld.x
+    ref = O.solve_all_abs(e0, shape, fld.eps, delta, 100, 1e-7, np.float64)
+    out = {}
+    for prec in (F.FFCZ_PRECISION_NATIVE, F.FFCZ_PRECISION_SPLIT):
+        with F.ProjectionSolver(*shape, dtype=np.float64) as s:
+            s.set_precision(prec)
+            s.initialize_all_abs(fld.x, fld.eps, delta)
+            it = s.solve_all_abs(e0, 100, 1e-7)
+            out[prec] = (it, s.get_results().reshape(-1), s.get_freq_edits_full(), s.get_spatial_edits_full(),
+                         s.verify_bounds())
+    it, e, fe, se, (sm, fm) = out[F.FFCZ_PRECISION_SPLIT]
+    assert it == ref["iterations"] == out[F.FFCZ_PRECISION_NATIVE][0]
+    es = float(np.abs(e0).max())
+    fs = float(np.abs(np.fft.rfftn(e0)).max())
+    t = 1e-11 * max(1, it)
+    assert np.abs(e - ref["e"].reshape(-1)).max() <= t * es
+    assert np.abs(fe - ref["freq_edits"]).max() <= t * fs
+    assert np.abs(se - ref["spatial_edits"]).max() <= t * es
+    assert np.abs(e - out[F.FFCZ_PRECISION_NATIVE][1]).max() <= t * es
+    assert sm <= fld.eps + 1e-7 and fm <= delta * (1 + 1e-9)
+
+
+def test_precision_setting_rules(cuda):
+    with F.ProjectionSolver(8, 8, 8) as s:  # FP32: native only
+        s.set_precision(F.FFCZ_PRECISION_NATIVE)
+        with pytest.raises(F.FFCzError) as ei:
+            s.set_precision(F.FFCZ_PRECISION_SPLIT)
+        assert ei.value.code == -3
+        with pytest.raises(F.FFCzError):
+            s.set_precision(7)
