@@ -58,13 +58,13 @@ __device__ __forceinline__ T spatial_clamp(T v, T eps, T *__restrict__ sedits, l
 }
 
 // Frequency box (projection_algorithm.cu:160-187) on one coefficient.  A
-// clamp also sets *dirty (when given): the accumulator is no longer all
-// zeros, so its compaction has to read it.
+// clamp also sets `hit`; the caller publishes it once per warp with
+// mark_dirty (the accumulator is no longer all zeros, so its compaction has
+// to read it).
 template <typename T>
 __device__ __forceinline__ c2<T> freq_clamp(c2<T> v, T delta, T *__restrict__ fedits, long long k,
-                                            long long H, unsigned *dirty) {
+                                            long long H, bool &hit) {
   T re = v.x;
-  bool hit = false;
   if (re > delta) {
     fedits[k] += delta - re;
     v.x = delta;
@@ -84,8 +84,14 @@ __device__ __forceinline__ c2<T> freq_clamp(c2<T> v, T delta, T *__restrict__ fe
     v.y = -delta;
     hit = true;
   }
-  if (hit && dirty) *dirty = 1u;
   return v;
+}
+
+// One store per warp at most (the first lane that clamped, and only while
+// the flag still reads 0): many clamps must not serialise on one address.
+__device__ __forceinline__ void mark_dirty(unsigned *dirty, bool hit) {
+  const unsigned m = __ballot_sync(__activemask(), hit);
+  if (hit && dirty && (int)(threadIdx.x & 31) == __ffs(m) - 1 && *dirty == 0u) *dirty = 1u;
 }
 
 // Frequency projection of every constraint mode, applied where the forward
@@ -117,9 +123,9 @@ __device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(
 
 template <typename T>
 __device__ __forceinline__ c2<T> freq_project(c2<T> v, const ClampArgs<T> &ca, T *__restrict__ fedits, long long k,
-                                              long long p, long long H) {
-  if (ca.mode == CLAMP_ABS) return freq_clamp<T>(v, ca.delta, fedits, k, H, ca.fdirty);
-  if (ca.mode == CLAMP_DIRECT) return freq_clamp<T>(v, ca.bound[k], fedits, k, H, ca.fdirty);
+                                              long long p, long long H, bool &hit) {
+  if (ca.mode == CLAMP_ABS) return freq_clamp<T>(v, ca.delta, fedits, k, H, hit);
+  if (ca.mode == CLAMP_DIRECT) return freq_clamp<T>(v, ca.bound[k], fedits, k, H, hit);
   if (k == 0) {
     if (ca.dc) {
       const T o = ca.orig[0].x;
@@ -127,7 +133,7 @@ __device__ __forceinline__ c2<T> freq_project(c2<T> v, const ClampArgs<T> &ca, T
       if (v.x > upper || v.x < lower) {
         fedits[0] += -v.x;
         v.x = T(0);
-        if (ca.fdirty) *ca.fdirty = 1u;
+        hit = true;
       }
     }
     return v;
@@ -139,7 +145,7 @@ __device__ __forceinline__ c2<T> freq_project(c2<T> v, const ClampArgs<T> &ca, T
   const T cm = add_rn(mul_rn(cx, cx), mul_rn(cy, cy));
   const T ratio = cm / om;
   if (ratio <= ca.sp && ratio >= ca.sm) return v;
-  return freq_clamp<T>(v, ca.cd, fedits, k, H, ca.fdirty);
+  return freq_clamp<T>(v, ca.cd, fedits, k, H, hit);
 }
 
 // ---------------------------------------------------------------------------
@@ -394,17 +400,20 @@ __global__ void __launch_bounds__(sizeof(T) == 4 ? 512 : 256) k_strided(c2<T> *_
     fft_tile<T, -1, EPT>(buf, p, P, lg, tid, nthr);
   }
   if (MODE == MODE_FCI || MODE == MODE_FCIX) {
+    bool hit = false;
     for (int it = tid; it < total; it += nthr) {
       const int l = it >> lg;
       const int c = it & (TW - 1);
       if (c < ncol) {
         const long long k = ((bb * s.L + l) * (long long)s.Q + q) * s.Hz + kz0 + c;
         if (MODE == MODE_FCI)
-          buf[l * P + c] = freq_clamp<T>(buf[l * P + c], ca.delta, fedits, k, H, ca.fdirty);
+          buf[l * P + c] = freq_clamp<T>(buf[l * P + c], ca.delta, fedits, k, H, hit);
         else
-          buf[l * P + c] = freq_project<T>(buf[l * P + c], ca, fedits, k, base + (long long)l * s.Wtot + c, H);
+          buf[l * P + c] =
+              freq_project<T>(buf[l * P + c], ca, fedits, k, base + (long long)l * s.Wtot + c, H, hit);
       }
     }
+    mark_dirty(ca.fdirty, hit);
     __syncthreads();
     fft_tile<T, +1, EPT>(buf, p, P, lg, tid, nthr);
   }
@@ -421,13 +430,15 @@ template <typename T>
 __global__ void k_clamp_freq(c2<T> *__restrict__ spec, long long rows, int Hz, int Hzp, ClampArgs<T> ca,
                              T *__restrict__ fedits, long long H) {
   const long long total = rows * Hz;
+  bool hit = false;
   for (long long it = blockIdx.x * (long long)blockDim.x + threadIdx.x; it < total;
        it += (long long)gridDim.x * blockDim.x) {
     const long long r = it / Hz;
     const int kz = (int)(it - r * Hz);
     c2<T> *ptr = spec + r * Hzp + kz;
-    *ptr = freq_project<T>(*ptr, ca, fedits, it, r * Hzp + kz, H);
+    *ptr = freq_project<T>(*ptr, ca, fedits, it, r * Hzp + kz, H, hit);
   }
+  mark_dirty(ca.fdirty, hit);
 }
 
 // ---------------------------------------------------------------------------

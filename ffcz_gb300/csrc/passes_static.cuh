@@ -384,6 +384,7 @@ __global__ void __launch_bounds__((L / rp_elems(L, CAP)) << LGTW,
     v[i] = live ? cvt<C>(src[(long long)first_pos<L, D0, CAP>(t, i) * s.Wtot]) : mkc<C>(C(0), C(0));
   RRun<C, D0, L, LY, 0, CAP, T>::run(v, buf, t, c, p);
   if (MODE == MODE_FCI || MODE == MODE_FCIX) {
+    bool hit = false;
     if (live) {
 #pragma unroll
       for (int i = 0; i < E; ++i) {
@@ -393,21 +394,22 @@ __global__ void __launch_bounds__((L / rp_elems(L, CAP)) << LGTW,
           const VG g = cvt<T>(v[i]);
           VG h;
           if (MODE == MODE_FCI) {
-            h = freq_clamp<T>(g, ca.delta, fedits, k, H, ca.fdirty);
+            h = freq_clamp<T>(g, ca.delta, fedits, k, H, hit);
           } else {
             const long long pad = (bb * L + l) * s.Wtot + (long long)q * s.Hzp + kz0 + c;
-            h = freq_project<T>(g, ca, fedits, k, pad, H);
+            h = freq_project<T>(g, ca, fedits, k, pad, H, hit);
           }
           if (h.x != g.x) v[i].x = C((double)h.x);
           if (h.y != g.y) v[i].y = C((double)h.y);
         } else if (MODE == MODE_FCI) {
-          v[i] = freq_clamp<T>(v[i], ca.delta, fedits, k, H, ca.fdirty);
+          v[i] = freq_clamp<T>(v[i], ca.delta, fedits, k, H, hit);
         } else {
           const long long pad = (bb * L + l) * s.Wtot + (long long)q * s.Hzp + kz0 + c;
-          v[i] = freq_project<T>(v[i], ca, fedits, k, pad, H);
+          v[i] = freq_project<T>(v[i], ca, fedits, k, pad, H, hit);
         }
       }
     }
+    mark_dirty(ca.fdirty, hit);
     // The inverse's first stage reads the positions the forward's last
     // stage wrote, so the same registers continue.  A barrier separates the
     // forward's last shared reads from the inverse's first shared writes.
