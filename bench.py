@@ -65,7 +65,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default tile of every pass")
     ap.add_argument("--zstd-threads", type=int, default=0,
-                    help="host threads of the ZSTD pool (default: cores - 2, at least 1)")
+                    help="host threads of the ZSTD pool (default: every host core; 16 vs 14 threads "
+                         "on a 16-core host: 2.42 vs 2.12-2.23 GB/s at 256^3)")
     ap.add_argument("--loop", default="graph", choices=["graph", "host"],
                     help="iteration driver; 'host' runs the same kernels outside a graph (for ncu)")
     return ap.parse_args()
@@ -284,7 +285,7 @@ def run_ours(args):
     s.initialize_all_abs_device(dx, fld.eps, fld.delta)
     tune = {} if args.no_autotune else s.autotune(5)
 
-    nzt = args.zstd_threads or max(1, (os.cpu_count() or 2) - 2)
+    nzt = args.zstd_threads or (os.cpu_count() or 1)
     pool = ThreadPoolExecutor(max_workers=nzt)
 
     def zstd_jobs(res):
@@ -550,7 +551,7 @@ def run_batch(args):
     batch = F.Batch(solvers)
     batch.set_stream(torch.cuda.current_stream())
     in_bytes = sum(f.x.nbytes for f in fields)
-    nzt = args.zstd_threads or max(1, (os.cpu_count() or 2) - 2)
+    nzt = args.zstd_threads or (os.cpu_count() or 1)
     pool = ThreadPoolExecutor(max_workers=nzt)
 
     def step(xs, xps):
