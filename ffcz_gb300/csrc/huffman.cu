@@ -42,17 +42,18 @@ __global__ void __launch_bounds__(256) k_hist_u8(const uint8_t *__restrict__ d, 
   if (v) atomicAdd(&hist[threadIdx.x], v);
 }
 
-// 32768 symbols per block, so every packed 16-bit counter stays < 65536.
-__global__ void __launch_bounds__(256) k_hist_u16(const uint16_t *__restrict__ d, long long n,
+// `chunk` symbols per block (a multiple of 8, at most 32768, so every packed
+// 16-bit counter stays < 65536).
+__global__ void __launch_bounds__(256) k_hist_u16(const uint16_t *__restrict__ d, long long n, int chunk,
                                                   unsigned *__restrict__ hist) {
   extern __shared__ __align__(16) unsigned sh16[];  // 32768 words
   for (int w = threadIdx.x; w < 32768; w += blockDim.x) sh16[w] = 0u;
   __syncthreads();
-  const long long base = (long long)blockIdx.x * H16_CHUNK;
-  const long long end = min(base + (long long)H16_CHUNK, n);
-  if (base + H16_CHUNK <= n) {
+  const long long base = (long long)blockIdx.x * chunk;
+  const long long end = min(base + (long long)chunk, n);
+  if (base + chunk <= n) {
     const uint4 *v4 = reinterpret_cast<const uint4 *>(d + base);
-    for (int j = threadIdx.x; j < H16_CHUNK / 8; j += blockDim.x) {
+    for (int j = threadIdx.x; j < chunk / 8; j += blockDim.x) {
       const uint4 q = v4[j];
       const unsigned w[4] = {q.x, q.y, q.z, q.w};
 #pragma unroll
@@ -268,9 +269,12 @@ int huff_encode_device(HuffWorkspace &ws, const void *d_data, size_t n, int symb
     const int grid = (int)std::min<size_t>(ceil_div(n, 256 * 16), 1024);
     k_hist_u8<<<grid, 256, 0, stream>>>((const uint8_t *)d_data, (long long)n, ws.d_hist);
   } else {
-    const size_t grid = ceil_div(n, H16_CHUNK);
+    // enough blocks to fill the SMs (the zeroing and flushing of a block's
+    // 128 KB of counters runs on every SM at once), at most H16_CHUNK each
+    const size_t chunk = std::min<size_t>(H16_CHUNK, std::max<size_t>(4096, round_up(ceil_div(n, (size_t)152), 8)));
+    const size_t grid = ceil_div(n, chunk);
     k_hist_u16<<<(unsigned)grid, 256, 32768 * sizeof(unsigned), stream>>>((const uint16_t *)d_data,
-                                                                           (long long)n, ws.d_hist);
+                                                                           (long long)n, (int)chunk, ws.d_hist);
   }
   ws.launches++;
   FFCZ_CUDA(cudaGetLastError());
