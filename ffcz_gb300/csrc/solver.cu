@@ -1035,6 +1035,32 @@ int strict_finish(ffcz_solver *s, int max_iter, double tol, int max_rounds, int 
   return FFCZ_OK;
 }
 
+// Zeroes `bytes` bytes at p (16-byte aligned) when *dirty != 0: an
+// accumulator whose flag reads 0 is all zeros already (the flag is cleared
+// with the array and set by every path that writes it).
+static __global__ void k_zero_if_dirty(void *__restrict__ p, size_t bytes, const unsigned *__restrict__ dirty) {
+  if (*dirty == 0u) return;
+  uint4 *q = reinterpret_cast<uint4 *>(p);
+  const size_t n4 = bytes / 16;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n4; i += (size_t)gridDim.x * blockDim.x)
+    q[i] = make_uint4(0u, 0u, 0u, 0u);
+  if (blockIdx.x == 0 && threadIdx.x < bytes % 16) reinterpret_cast<unsigned char *>(p)[n4 * 16 + threadIdx.x] = 0;
+}
+
+// reset_edit_accumulators on `st`: each accumulator is zeroed only when it
+// was written since its last clear; the flags are cleared after the zeroing.
+static int clear_accumulators(ffcz_solver *s, cudaStream_t st) {
+  const size_t fb = 2 * s->H * s->es, sb = s->N * s->es;
+  const unsigned gf = (unsigned)std::min<size_t>(std::max<size_t>(ceil_div(fb / 16, (size_t)256), 1), 152 * 8);
+  const unsigned gs = (unsigned)std::min<size_t>(std::max<size_t>(ceil_div(sb / 16, (size_t)256), 1), 152 * 8);
+  k_zero_if_dirty<<<gf, 256, 0, st>>>(s->d_fedits, fb, s->d_fdirty);
+  k_zero_if_dirty<<<gs, 256, 0, st>>>(s->d_sedits, sb, s->d_sdirty);
+  FFCZ_CUDA(cudaGetLastError());
+  FFCZ_CUDA(cudaMemsetAsync(s->d_fdirty, 0, sizeof(unsigned), st));
+  FFCZ_CUDA(cudaMemsetAsync(s->d_sdirty, 0, sizeof(unsigned), st));
+  return FFCZ_OK;
+}
+
 #define DISPATCH(s, fn, ...) ((s)->dtype == FFCZ_F32 ? fn<float>(__VA_ARGS__) : fn<double>(__VA_ARGS__))
 
 extern "C" {
@@ -1316,10 +1342,7 @@ int ffcz_extract(ffcz_solver *s) {
 
 int ffcz_reset_edit_accumulators(ffcz_solver *s) {
   FFCZ_TRY(check_solver(s));
-  FFCZ_CUDA(cudaMemsetAsync(s->d_fedits, 0, 2 * s->H * s->es, s->stream));
-  FFCZ_CUDA(cudaMemsetAsync(s->d_fdirty, 0, sizeof(unsigned), s->stream));
-  FFCZ_CUDA(cudaMemsetAsync(s->d_sedits, 0, s->N * s->es, s->stream));
-  FFCZ_CUDA(cudaMemsetAsync(s->d_sdirty, 0, sizeof(unsigned), s->stream));
+  FFCZ_TRY(clear_accumulators(s, s->stream));
   FFCZ_CUDA(cudaStreamSynchronize(s->stream));
   return FFCZ_OK;
 }
@@ -1802,12 +1825,7 @@ int ffcz_batch_set_stream(ffcz_batch *b, void *stream) {
 int ffcz_batch_reset_edit_accumulators(ffcz_batch *b) {
   if (!b) return fail(FFCZ_ERR_INVALID, "batch is NULL");
   for (ffcz_solver *s : b->f) FFCZ_CUDA(cudaStreamSynchronize(s->stream));
-  for (ffcz_solver *s : b->f) {
-    FFCZ_CUDA(cudaMemsetAsync(s->d_fedits, 0, 2 * s->H * s->es, b->stream));
-    FFCZ_CUDA(cudaMemsetAsync(s->d_fdirty, 0, sizeof(unsigned), b->stream));
-    FFCZ_CUDA(cudaMemsetAsync(s->d_sedits, 0, s->N * s->es, b->stream));
-    FFCZ_CUDA(cudaMemsetAsync(s->d_sdirty, 0, sizeof(unsigned), b->stream));
-  }
+  for (ffcz_solver *s : b->f) FFCZ_TRY(clear_accumulators(s, b->stream));
   FFCZ_CUDA(cudaStreamSynchronize(b->stream));
   return FFCZ_OK;
 }

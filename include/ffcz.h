@@ -155,7 +155,9 @@ int ffcz_project_all_abs_device(ffcz_solver *s, const void *d_err,
 /* extract_compact_representation() -- impl:371-456 (flags, whole-array
  * min/max, scan, compaction, uint16 quantisation, flag packs). */
 int ffcz_extract(ffcz_solver *s);
-/* reset_edit_accumulators() -- impl:133-147. */
+/* reset_edit_accumulators() -- impl:133-147.  Both accumulators are all
+ * zeros afterwards; one nothing has written since its last clear is not
+ * rewritten. */
 int ffcz_reset_edit_accumulators(ffcz_solver *s);
 /* Waits for the solver's stream. */
 int ffcz_solver_synchronize(ffcz_solver *s);
