@@ -153,6 +153,37 @@ struct ffc {
 };
 template <> struct C2<ff> { using type = ffc; };
 
+// Conversions without the FP64 pipe (GB300's FP64 rate is a small fraction
+// of its FP32 rate): the fields of a double split by integer operations.
+// double -> ff: hi = the top 24 significand bits, lo = the other 29 bits
+// (rounded to 24) scaled by the exponent, then renormalised; exact for 48
+// significant bits.  Only doubles whose hi and scaled lo are normal floats
+// (2^-74 <= |d| < 2^127) take this path; zeros and the rest are converted by
+// the FP64 path.
+__device__ __forceinline__ ff ff_from_double(double d) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+  const int ex = (int)((b >> 52) & 0x7ff);
+  if (ex < 949 || ex > 1150) return ff(d);
+  const unsigned sign = (unsigned)(b >> 63) << 31;
+  const unsigned long long mant = b & 0xfffffffffffffull;
+  const float hi = __uint_as_float(sign | ((unsigned)(ex - 1023 + 127) << 23) | (unsigned)(mant >> 29));
+  const float scale = __uint_as_float((unsigned)(ex - 1075 + 127) << 23);  // 2^(ex - 1075)
+  float lo = __fmul_rn(__uint2float_rn((unsigned)(mant & 0x1fffffffull)), scale);
+  if (sign) lo = -lo;
+  return ff_fast_two_sum(hi, lo);
+}
+// Exact widening of a float by its fields (normal floats; others through
+// the conversion instruction).
+__device__ __forceinline__ double f2d_fields(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned e = (u >> 23) & 0xffu;
+  if (e == 0u || e == 0xffu) return (double)f;
+  return __longlong_as_double((long long)(((unsigned long long)(u >> 31) << 63) |
+                                          ((unsigned long long)(e - 127u + 1023u) << 52) |
+                                          ((unsigned long long)(u & 0x7fffffu) << 29)));
+}
+__device__ __forceinline__ double ff_to_double_fast(ff a) { return f2d_fields(a.hi) + f2d_fields(a.lo); }
+
 // Complex conversions between a storage type and a compute type (identity
 // unless one side is ff).
 template <typename To, typename VF>
@@ -162,13 +193,23 @@ __host__ __device__ __forceinline__ c2<To> cvt(const VF &a) {
     return a;
   } else if constexpr (std::is_same<To, ff>::value) {
     c2<To> r;
+#ifdef __CUDA_ARCH__
+    r.x = ff_from_double((double)a.x);
+    r.y = ff_from_double((double)a.y);
+#else
     r.x = ff((double)a.x);
     r.y = ff((double)a.y);
+#endif
     return r;
   } else {
     c2<To> r;
+#ifdef __CUDA_ARCH__
+    r.x = (To)ff_to_double_fast(a.x);
+    r.y = (To)ff_to_double_fast(a.y);
+#else
     r.x = (To)ff_to_double(a.x);
     r.y = (To)ff_to_double(a.y);
+#endif
     return r;
   }
 }

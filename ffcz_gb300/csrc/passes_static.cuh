@@ -382,15 +382,21 @@ __global__ void __launch_bounds__((L / rp_elems(L, CAP)) << LGTW,
 #pragma unroll
   for (int i = 0; i < E; ++i)
     v[i] = live ? cvt<C>(src[(long long)first_pos<L, D0, CAP>(t, i) * s.Wtot]) : mkc<C>(C(0), C(0));
-  RRun<C, D0, L, LY, 0, CAP, T>::run(v, buf, t, c, p);
+  RRun<C, D0, L, LY, 0, CAP, C>::run(v, buf, t, c, p);  // split: p.tw is the float-float table
   if (MODE == MODE_FCI || MODE == MODE_FCIX) {
     bool hit = false;
+    // split FCI: |hi| below this is inside the box (0 when delta is too small
+    // for the margin to mean anything: every coefficient decides in FP64)
+    const float dlo = SPLIT ? (float)((double)ca.delta * (1.0 - 0x1p-20)) : 0.0f;
     if (live) {
 #pragma unroll
       for (int i = 0; i < E; ++i) {
         const int l = last_pos<L, -1, CAP>(t, i);
         const long long k = ((bb * L + l) * (long long)s.Q + q) * s.Hz + kz0 + c;
         if constexpr (SPLIT) {  // the box in FP64; unclamped values keep their split form
+          // hi is within 2^-23 of the value: well inside the box, nothing to
+          // decide in FP64 (the pointwise box always decides in FP64)
+          if (MODE == MODE_FCI && fabsf(v[i].x.hi) < dlo && fabsf(v[i].y.hi) < dlo) continue;
           const VG g = cvt<T>(v[i]);
           VG h;
           if (MODE == MODE_FCI) {
@@ -414,7 +420,7 @@ __global__ void __launch_bounds__((L / rp_elems(L, CAP)) << LGTW,
     // stage wrote, so the same registers continue.  A barrier separates the
     // forward's last shared reads from the inverse's first shared writes.
     __syncthreads();
-    RRun<C, +1, L, LY, 0, CAP, T>::run(v, buf, t, c, p);
+    RRun<C, +1, L, LY, 0, CAP, C>::run(v, buf, t, c, p);
   }
   constexpr int DL = (MODE == MODE_FWD) ? -1 : +1;
   VG *dst = spec + bb * (long long)L * s.Wtot + (long long)q * s.Hzp + kz0 + c;
@@ -469,7 +475,7 @@ __global__ void __launch_bounds__((M / rp_elems(M, 8)) << LGTW) ks_zfwd(const T 
   V v[E];
 #pragma unroll
   for (int i = 0; i < E; ++i) v[i] = cvt<C>(g[i]);
-  RRun<C, -1, M, LY, 0, 8, T>::run(v, buf, t, c, p);
+  RRun<C, -1, M, LY, 0, 8, C>::run(v, buf, t, c, p);  // split: p.tw, post: float-float tables
   // Z in natural order to shared memory, then the real-to-complex split of
   // row c: X[k] = (Z[k] + conj Z[M-k])/2 - i W^k (Z[k] - conj Z[M-k])/2.
   if (rp_nst(M, 8) > 1) __syncthreads();
@@ -483,7 +489,7 @@ __global__ void __launch_bounds__((M / rp_elems(M, 8)) << LGTW) ks_zfwd(const T 
     const int k2 = (k == 0) ? 0 : M - k;
     const V A = buf[LY::idx(k1, c)];
     const V B = cconj(buf[LY::idx(k2, c)]);
-    const V w = cvt<C>(post[k]);
+    const V w = reinterpret_cast<const V *>(post)[k];
     const V sm = cadd(A, B);
     const V d = csub(A, B);
     const V tt = cmul(mkc<C>(-w.y, w.x), d);
@@ -530,7 +536,7 @@ __global__ void __launch_bounds__((M / rp_elems(M, 8)) << LGTW) ks_zinv(const c2
       if (k == 0) {
         v[i] = mkc<C>(xa[i].x + xb[i].x, xa[i].x - xb[i].x);
       } else {
-        const V w = cvt<C>(post[k]);
+        const V w = reinterpret_cast<const V *>(post)[k];
         const V s1 = cadd(xa[i], cconj(xb[i]));
         const V d1 = csub(xa[i], cconj(xb[i]));
         v[i] = cadd(s1, cmul(mkc<C>(w.y, w.x), d1));
@@ -540,9 +546,33 @@ __global__ void __launch_bounds__((M / rp_elems(M, 8)) << LGTW) ks_zinv(const c2
 #pragma unroll
     for (int i = 0; i < E; ++i) v[i] = mkc<C>(C(0), C(0));
   }
-  RRun<C, +1, M, LY, 0, 8, T>::run(v, buf, t, c, p);
+  RRun<C, +1, M, LY, 0, 8, C>::run(v, buf, t, c, p);
   T vmax = T(0);
-  if (live) {
+  if constexpr (SPLIT) {
+    if (live) {
+      // float-float normalisation; the violation in FP64 only where an FP32
+      // look at hi cannot rule it out (|o| <= |hi|(1 + 2^-23) < eps below elo)
+      T *out = e + row * (long long)(2 * M);
+      const C F = cvt<C>(mkc<T>(factor, T(0))).x;
+      const float elo = (float)((double)eps * (1.0 - 0x1p-20));
+#pragma unroll
+      for (int i = 0; i < E; ++i) {
+        V w;
+        w.x = v[i].x * F;
+        w.y = v[i].y * F;
+        const VG o = cvt<T>(w);
+        *reinterpret_cast<VG *>(out + 2 * last_pos<M, +1, 8>(t, i)) = o;
+        if (fabsf(w.x.hi) >= elo) {
+          const T a0 = fabs(o.x);
+          if (a0 > eps) vmax = max(vmax, a0 - eps);
+        }
+        if (fabsf(w.y.hi) >= elo) {
+          const T a1 = fabs(o.y);
+          if (a1 > eps) vmax = max(vmax, a1 - eps);
+        }
+      }
+    }
+  } else if (live) {
     T *out = e + row * (long long)(2 * M);
 #pragma unroll
     for (int i = 0; i < E; ++i) {

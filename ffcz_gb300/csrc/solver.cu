@@ -103,6 +103,9 @@ struct ffcz_solver {
   Launch lyf{}, lxf{};
   AxisPlan pyf{}, pxf{};
   size_t post_off = 0;  // offset (complex entries) of the R2C split twiddles
+  size_t tw_count = 0;  // complex entries of the twiddle table
+  void *d_tw_ff = nullptr;  // the same table in float-float (split FP64 kernels)
+  int zsplit = 0;       // the z passes run float-float kernels (their tables: d_tw_ff)
   ZArgs za{};
   SArgs sy{}, sx{};
   Launch lz_f, lz_i, ly, lx;
@@ -222,16 +225,20 @@ bool apply_static_z(ffcz_solver *s, int var) {
   ZfwdFn<T> f[3];
   ZinvFn<T> fi;
   bool ok = false;
+  int used = 0;
   // float-float kernels first when the solver asks for them and the length
-  // has them, then the native ones
+  // has them (their twiddles: the float-float table), then the native ones
   for (int split = s->split; split >= 0 && !ok; --split) {
     ok = static_zinv<T>(s->M, fi, g, var, split);
     for (int pro = 0; pro < 3 && ok; ++pro) ok = static_zfwd<T>(s->M, pro, f[pro], g, var, split);
+    used = split;
   }
   if (!ok) return false;
   for (int pro = 0; pro < 3; ++pro) s->kzf[pro] = (void *)f[pro];
   s->kzi = (void *)fi;
   s->pz = s->pz_s;
+  s->zsplit = used;
+  if (used) s->pz.tw = s->d_tw_ff;
   s->za.TW = g.TW;
   s->za.log2TW = __builtin_ctz(g.TW);
   s->za.P = g.TW + 1;
@@ -256,9 +263,11 @@ bool apply_static_strided(ffcz_solver *s, int axis, int var) {
   StaticGeom g[4];
   StridedFn<T> f[4];
   bool ok = false;
+  int used = 0;
   for (int split = s->split; split >= 0 && !ok; --split) {
     ok = true;
     for (int m = 0; m < 4 && ok; ++m) ok = static_strided<T>(L, m, f[m], g[m], var, split);
+    used = split;
   }
   if (!ok) return false;
   for (int m = 0; m < 4; ++m) k[m] = (void *)f[m];
@@ -267,7 +276,9 @@ bool apply_static_strided(ffcz_solver *s, int axis, int var) {
     const StaticGeom &gg = g[fam ? MODE_FCI : MODE_FWD];
     SArgs &sa = fam ? (axis == 0 ? s->syf : s->sxf) : (axis == 0 ? s->sy : s->sx);
     Launch &ln = fam ? (axis == 0 ? s->lyf : s->lxf) : (axis == 0 ? s->ly : s->lx);
-    (fam ? (axis == 0 ? s->pyf : s->pxf) : (axis == 0 ? s->py : s->px)) = fam ? psf : ps;
+    AxisPlan &pl = fam ? (axis == 0 ? s->pyf : s->pxf) : (axis == 0 ? s->py : s->px);
+    pl = (fam || used) ? psf : ps;  // float-float kernels: the CAP 16 lists for every pass
+    if (used) pl.tw = s->d_tw_ff;   // and the float-float table
     sa.TW = gg.TW;
     sa.log2TW = __builtin_ctz(gg.TW);
     sa.P = gg.TW + 1;
@@ -294,6 +305,7 @@ int select_kernels(ffcz_solver *s) {
   else generic_strided<T, E>(s->ky);
   if (s->x_ept == kWideEpt) generic_strided<T, kWideEpt>(s->kx);
   else generic_strided<T, E>(s->kx);
+  s->zsplit = 0;  // runtime-planned z kernels compute in the storage type
   // runtime-planned kernels: one tile and plan for every pass of an axis
   s->syf = s->sy;
   s->lyf = s->ly;
@@ -350,6 +362,7 @@ int plan_solver(ffcz_solver *s) {
   if (table.empty()) table.push_back({1.0, 0.0});
   std::vector<c2<T>> tw(table.size());
   for (size_t i = 0; i < table.size(); ++i) tw[i] = mkc<T>((T)table[i].real(), (T)table[i].imag());
+  s->tw_count = tw.size();
   FFCZ_CUDA(cudaMalloc(&s->d_tw, tw.size() * es2));
   FFCZ_CUDA(cudaMemcpy(s->d_tw, tw.data(), tw.size() * es2, cudaMemcpyHostToDevice));
   s->pz.tw = s->py.tw = s->px.tw = s->d_tw;
@@ -422,6 +435,13 @@ int plan_solver(ffcz_solver *s) {
 
 template <typename T> T *tp(void *p) { return (T *)p; }
 
+// R2C split twiddles of the z passes: the float-float copy (same layout,
+// 16-byte entries) when the z passes run the float-float kernels.
+template <typename T>
+const c2<T> *post_table(const ffcz_solver *s) {
+  return (const c2<T> *)(s->zsplit ? s->d_tw_ff : s->d_tw) + s->post_off;
+}
+
 // NVTX range for the duration of a scope (visible to profilers that attach
 // an NVTX tool; a no-op otherwise).
 struct Range {
@@ -467,7 +487,7 @@ void launch_iteration(ffcz_solver *s, cudaStream_t st, int pro, const void *a, c
   const T eps = (T)s->eps;
   const ClampArgs<T> delta = clamp_args<T>(s);
   const int fci = s->cmode == CLAMP_ABS ? MODE_FCI : MODE_FCIX;
-  const c2<T> *post = (const c2<T> *)s->d_tw + s->post_off;
+  const c2<T> *post = post_table<T>(s);
   c2<T> *spec = (c2<T> *)s->d_spec;
   const T *pa = (const T *)a, *pb = (const T *)b;
   const ZfwdFn<T> kzf = (ZfwdFn<T>)s->kzf[pro];
@@ -734,7 +754,7 @@ void free_all(ffcz_solver *s) {
   for (LoopGraph &g : s->lg) g.reset();
   void *bufs[] = {s->d_x, s->d_e, s->d_spec, s->d_fedits, s->d_sedits, s->d_fcompact, s->d_scompact,
                   s->d_fquant, s->d_squant, s->d_fpack, s->d_spack, s->d_tw, s->d_ctl, s->d_ex_rec, s->d_fdirty, s->d_sdirty,
-                  s->d_mnmx};
+                  s->d_mnmx, s->d_tw_ff};
   for (void *p : bufs)
     if (p) cudaFree(p);
   if (s->d_up_blk) cudaFree(s->d_up_blk);
@@ -817,7 +837,7 @@ int reconstruct(ffcz_solver *s, const void *d_decomp, const uint16_t *fq, size_t
     ((StridedFn<T>)s->ky[MODE_INV])<<<s->ly.grid, s->ly.threads, s->ly.smem, st>>>(spec, s->sy, s->py, delta,
                                                                                    tp<T>(s->d_fedits), H);
   }
-  const c2<T> *post = (const c2<T> *)s->d_tw + s->post_off;
+  const c2<T> *post = post_table<T>(s);
   const T factor = T(1) / static_cast<T>(s->N);
   ((ZinvFn<T>)s->kzi)<<<s->lz_i.grid, s->lz_i.threads, s->lz_i.smem, st>>>(spec, tp<T>(s->d_e), (T)s->eps, factor,
                                                                           s->d_ctl, s->za, s->pz, post);
@@ -842,7 +862,7 @@ template <typename T>
 int forward_spectrum(ffcz_solver *s, bool keep_as_orig = true) {
   cudaStream_t st = s->stream;
   c2<T> *spec = (c2<T> *)s->d_spec;
-  const c2<T> *post = (const c2<T> *)s->d_tw + s->post_off;
+  const c2<T> *post = post_table<T>(s);
   const ClampArgs<T> none;
   const long long H = (long long)s->H;
   ((ZfwdFn<T>)s->kzf[PRO_PLAIN])<<<s->lz_f.grid, s->lz_f.threads, s->lz_f.smem, st>>>(
@@ -917,7 +937,7 @@ int autotune(ffcz_solver *s, int reps, double *ms6) {
   } guard{e0, e1};
   const long long H = (long long)s->H;
   c2<T> *spec = (c2<T> *)s->d_spec;
-  const c2<T> *post = (const c2<T> *)s->d_tw + s->post_off;
+  const c2<T> *post = post_table<T>(s);
   ClampArgs<T> ca;
   ca.delta = std::numeric_limits<T>::infinity();
   auto timed = [&](auto launch) -> double {
@@ -1033,6 +1053,15 @@ int strict_finish(ffcz_solver *s, int max_iter, double tol, int max_rounds, int 
   if (smax) *smax = sm;
   if (fmax) *fmax = fm;
   return FFCZ_OK;
+}
+
+static __global__ void k_to_ff(const double2 *__restrict__ src, ffc *__restrict__ dst, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    ffc r;
+    r.x = ff(src[i].x);
+    r.y = ff(src[i].y);
+    dst[i] = r;
+  }
 }
 
 // Zeroes `bytes` bytes at p (16-byte aligned) when *dirty != 0: an
@@ -1492,6 +1521,13 @@ int ffcz_solver_set_precision(ffcz_solver *s, int precision) {
                                                : fail(FFCZ_ERR_UNSUPPORTED, "split precision applies to FP64 solvers");
   FFCZ_CUDA(cudaStreamSynchronize(s->stream));
   s->split = precision == FFCZ_PRECISION_SPLIT ? 1 : 0;
+  if (s->split && !s->d_tw_ff) {  // the twiddle table in float-float, same layout
+    FFCZ_CUDA(cudaMalloc(&s->d_tw_ff, s->tw_count * sizeof(ffc)));
+    const unsigned g = (unsigned)std::min<size_t>(ceil_div(s->tw_count, (size_t)256), 1024);
+    k_to_ff<<<g, 256, 0, s->stream>>>((const double2 *)s->d_tw, (ffc *)s->d_tw_ff, (long long)s->tw_count);
+    FFCZ_CUDA(cudaGetLastError());
+    FFCZ_CUDA(cudaStreamSynchronize(s->stream));
+  }
   FFCZ_TRY(select_kernels<double>(s));
   for (LoopGraph &g : s->lg) g.reset();  // the cached loops hold the previous kernels
   ++s->kernel_gen;

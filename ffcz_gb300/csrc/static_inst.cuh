@@ -73,9 +73,11 @@ bool zinv_for(ZinvFn<T> &fn, StaticGeom &g) {
 
 // The plain passes (forward, inverse) take the plain_cap(L) stage list, the
 // fused ones (forward + clamp + inverse) the CAP 16 list.
+// (Float-float kernels take the CAP 16 lists for every pass: 8 values per
+// thread fit them in 118 registers, the 16 of [16,16,2] spill.)
 template <typename T, int L, int VAR, bool FUSED, bool SPLIT = false>
 bool strided_for_family(int mode, StridedFn<T> &fn, StaticGeom &g) {
-  constexpr int CAP = FUSED ? 16 : plain_cap(L);
+  constexpr int CAP = (FUSED || SPLIT) ? 16 : plain_cap(L);
   using C = Cfg<T, L, CAP, VAR>;
   if (VAR && C::TW == Cfg<T, L, CAP, 0>::TW) return false;
   if constexpr (FUSED) {
