@@ -67,6 +67,8 @@ def parse():
     ap.add_argument("--zstd-threads", type=int, default=0,
                     help="host threads of the ZSTD pool (default: every host core; 16 vs 14 threads "
                          "on a 16-core host: 2.42 vs 2.12-2.23 GB/s at 256^3)")
+    ap.add_argument("--precision", default="native", choices=["native", "split"],
+                    help="FP64 fields: pass kernels in FP64 (native) or float-float on the FP32 pipes (split)")
     ap.add_argument("--loop", default="graph", choices=["graph", "host"],
                     help="iteration driver; 'host' runs the same kernels outside a graph (for ncu)")
     return ap.parse_args()
@@ -258,7 +260,10 @@ def config(args, fld, its):
                         f"E={fld.eps:.4g}, Delta={fld.delta:.4g}, max_iter 100, tol 1e-7",
             "iterations": its, "zstd_level": args.zstd_level, "zstd_mode": args.zstd_mode,
             "l2": "inputs and working set (x, x', e, spectrum, edits: >400 MB) larger than L2",
-            "parallelism": f"replicas x{args.gpus}", "loop": getattr(args, "loop", "graph")}
+            "parallelism": f"replicas x{args.gpus}", "loop": getattr(args, "loop", "graph"),
+            **({"precision": "split: float-float passes on the FP32 pipes, FP64 storage, boxes and checks"
+                if getattr(args, "precision", "native") == "split" else "native FP64"}
+               if fld.x.dtype == np.float64 else {})}
 
 
 # --------------------------------------------------------------------------- GPU leg
@@ -279,6 +284,8 @@ def run_ours(args):
     dx = x_h.cuda()
     dxp = torch.from_numpy(fld.xp.reshape(-1)).cuda()
     s = F.ProjectionSolver(*fld.shape, dtype=dt)
+    if dt == np.float64 and args.precision == "split":
+        s.set_precision(F.FFCZ_PRECISION_SPLIT)
     s.set_stream(torch.cuda.current_stream())
     s.set_loop_driver(F.FFCZ_LOOP_HOST if args.loop == "host" else F.FFCZ_LOOP_GRAPH)
     s.set_profiling(True)
