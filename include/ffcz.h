@@ -218,8 +218,9 @@ int ffcz_solver_autotune(ffcz_solver *s, int reps, double *ms6);
  * lengths 128..512 keep FP64 in memory but compute in float-float (pairs of
  * FP32 values, ~48-bit significand, relative rounding ~1e-14 per operation)
  * on the FP32 pipes; other lengths stay FP64; the frequency and spatial
- * boxes and the violation are evaluated in FP64; ffcz_verify_bounds and
- * ffcz_strict_finish keep checking in FP64.  Reselects the kernels (the
+ * boxes and the violation are evaluated in FP64 (FP32 pre-checks skip the
+ * values far inside them); ffcz_verify_bounds and ffcz_strict_finish keep
+ * checking in FP64.  About 2x faster than native at 512^3.  Reselects the kernels (the
  * autotuner's choice is reset).  FP32 solvers accept NATIVE only. */
 #define FFCZ_PRECISION_NATIVE 0
 #define FFCZ_PRECISION_SPLIT  1
