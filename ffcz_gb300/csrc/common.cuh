@@ -168,7 +168,13 @@ __device__ __forceinline__ ff ff_from_double(double d) {
   const unsigned long long mant = b & 0xfffffffffffffull;
   const float hi = __uint_as_float(sign | ((unsigned)(ex - 1023 + 127) << 23) | (unsigned)(mant >> 29));
   const float scale = __uint_as_float((unsigned)(ex - 1075 + 127) << 23);  // 2^(ex - 1075)
-  float lo = __fmul_rn(__uint2float_rn((unsigned)(mant & 0x1fffffffull)), scale);
+  // the 29 low bits as a float without a conversion instruction: the top 23
+  // and the last 6 placed in float significands (2^23 + v - 2^23 is exact),
+  // then one rounding (the same as converting the 29-bit integer)
+  const unsigned r = (unsigned)(mant & 0x1fffffffull);
+  const float r1 = __fsub_rn(__uint_as_float(0x4b000000u | (r >> 6)), 8388608.0f);
+  const float r0 = __fsub_rn(__uint_as_float(0x4b000000u | (r & 63u)), 8388608.0f);
+  float lo = __fmul_rn(__fmaf_rn(r1, 64.0f, r0), scale);
   if (sign) lo = -lo;
   return ff_fast_two_sum(hi, lo);
 }

@@ -104,6 +104,8 @@ WORKLOADS = {
     "precision512": ((512, 512, 512), 3.0, 2, 1e-4, 1e-4, 0.0, False, np.float32, 100),
     "large1024x1024x512": ((1024, 1024, 512), 11 / 3, 3, 5e-5, 2e-4, 0.0, True, np.float32, 500),
     "fp64_512": ((512, 512, 512), 11 / 3, 4, 5e-5, 2e-4, 0.0, True, np.float64, 500),
+    # the FP64 variant at 256^3: a case small enough for full kernel profiles
+    "fp64_256": ((256, 256, 256), 11 / 3, 4, 5e-5, 2e-4, 0.0, True, np.float64, 500),
 }
 
 
