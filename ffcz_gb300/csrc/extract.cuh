@@ -2,9 +2,9 @@
 // projection_algorithm.cu:365-379, 382-405, 427-457, 459-550) instead of the
 // reference's flag kernels, two CUB reductions, a CUB scan, the scatter
 // kernel and two bool-pack kernels.  The solver uses the single-read form
-// further down (k_ex_part + k_ex_place); the three-launch form below
-// serves the no-allocation entry point, whose caller-provided scratch has no
-// room for the compacted values:
+// further down (k_ex_part, k_ex_scan_rec, k_ex_place); the two-read form
+// below serves the no-allocation entry point, whose caller-provided scratch
+// has no room for the compacted values:
 //   k_ex_stats   : per 4096-element chunk: #(|v| > thr), min, max   (R n*s)
 //   k_ex_scan    : one block: chunk offsets (exclusive scan), global
 //                  min/max, active count                        (tiny)
