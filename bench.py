@@ -1,30 +1,47 @@
-"""Benchmark: input GB/s of project + encode on one GB300.
+"""Benchmark: input GB/s of project + encode on one GB300, the chosen form
+against the plain FP32 form, with both bounds met in FP64.
+
+Default workload: the precision field, 512x512x512 float32 (seed 2, P(k) ~
+k^-3, E = 1e-4 range, Delta = 1e-4 max|F(x)|, max_iter 100, tol 1e-7).
+Other workloads: --workload plain256 (256^3, seed 1, k^-11/3, E = 1e-4
+range, Delta = 5e-4 max|F(x)|, +0.3E noise), large1024x1024x512, fp64_512,
+small64, batch48 (48 fields of uneven shapes in one graph launch).
 
 One step = one field through the whole path: reset of the edit
-accumulators, the alternating projections (iterated to the reference's
-termination rule), compaction + uint16 quantisation + flag packs, and the
+accumulators, the alternating projections (the reference's termination
+rule), the strict finish (|e_i| <= E and |Re/Im F(e)_k| <= Delta in FP64:
+a clamp to the largest value <= E, then the certificate of the solver's own
+transform with a bound on its rounding, an FP64 transform only where that
+cannot decide), compaction + uint16 quantisation + flag packs, and the
 four-stream Huffman encode with ZSTD (level 20, as projection_example.cu
 uses), ending with the compressed bytes in host memory.
 
-  value : x and x' resident in HBM when the timed region starts
-          (ffcz_solve_all_abs_pair_device + ffcz_solver_encode);
-  e2e   : the reference-facing C ABI with host buffers -- initialize_all_abs
-          (H2D of x) + solve_all_abs (H2D of e0 = x' - x) + encode, so the
-          host->device copies are inside the timed region.
+  value   : x and x' resident in HBM when the timed region starts
+            (ffcz_solve_all_abs_pair_device + ffcz_strict_finish +
+            ffcz_solver_encode), device-event timed;
+  e2e     : the reference-facing C ABI with host buffers -- initialize_all_abs
+            (H2D of x) + solve_all_abs (H2D of e0 = x' - x) + strict finish +
+            encode, so the host->device copies are inside the timed region;
+  gpu_only: the value step without ZSTD (project + strict + Huffman).
 Input bytes per step = N * sizeof(T) of the original field.
+
+forms: the same three numbers for the chosen form (five HBM passes per 3D
+iteration) and for the plain FP32 form (six: x forward + clamp and x
+inverse as separate passes), and their ratios.
+cufft_reference: the reference's own cuFFT build (unmodified sources,
+oracle/ref_solver) timed on the same GPU and field.
+stress: the field with Delta = E sqrt(N/6), where frequency clamps fire.
 
 The K steps run as a pipeline: while the GPU projects and Huffman-codes
 field i, host threads run the ZSTD stage (one ZSTD_compress per stream, the
-reference's call, so the bytes are unchanged) of the earlier fields; the
-timed region ends when the last stream is compressed.  `step_latency_ms`
-reports one step run alone.
+reference's call, so the bytes are unchanged) of the earlier fields.
 
 --impl reference times the CPU restatement of the same path (FP64 pocketfft
 loop with scipy workers = all host cores, C compaction/quantiser/Huffman,
-libzstd) on the same workload.
+libzstd) on the same workload, within a time budget.
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                       [--workload plain256] [--zstd-mode single|chunked]
+                       [--workload precision512] [--no-plain] [--no-strict] [--no-cufft-reference]
 """
 from __future__ import annotations
 
@@ -47,8 +64,8 @@ sys.path.insert(0, str(ROOT))
 METRIC = "Input GB/s (project+encode) on 1 GB300, mixed-prec vs plain FP32, bounds met"
 PEAKS = ROOT / "MEASURED_PEAKS.json"
 # DRAM bytes read + written per launch of each pass, from one
-# `ncu --set full` capture of the same workload (profiles/passes_plain256_ncu.md;
-# cold-cache replays, writes still dirty in L2 at kernel exit not counted).
+# `ncu --set full` capture of the same workload (cold-cache replays, writes
+# still dirty in L2 at kernel exit not counted).
 TRAFFIC = {"plain256": {"zfwd_r2c": 169.0e6, "y_fwd": 89.3e6, "x_fwd_clamp_inv": 91.5e6, "y_inv": 89.3e6,
                         "zinv_c2r_viol": 98.2e6}}
 
@@ -59,10 +76,17 @@ def parse():
     ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="plain256")
+    ap.add_argument("--workload", default="precision512")
     ap.add_argument("--zstd-level", type=int, default=20)
     ap.add_argument("--zstd-mode", default="single", choices=["single", "chunked"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-strict", action="store_true",
+                    help="leave out the strict FP64 bounds finish (the reference schedule's bounds only)")
+    ap.add_argument("--no-plain", action="store_true", help="leave out the plain FP32 (six-pass) form")
+    ap.add_argument("--reference-budget-s", type=float, default=90.0,
+                    help="--impl reference: time budget of its timed steps")
+    ap.add_argument("--no-cufft-reference", action="store_true",
+                    help="leave out the timing of the reference's own cuFFT build")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default tile of every pass")
     ap.add_argument("--zstd-threads", type=int, default=0,
                     help="host threads of the ZSTD pool (default: every host core; 16 vs 14 threads "
@@ -149,14 +173,17 @@ def peak_hbm():
 
 
 # --------------------------------------------------------------------------- CPU leg
-def cpu_step(fld, max_iter, level, pool=None):
+def cpu_step(fld, max_iter, level, pool=None, keep=None):
     """One project+encode pass of the oracle restatement.  With a pool the
-    ZSTD stage is submitted to it; returns (seconds, iterations, jobs)."""
+    ZSTD stage is submitted to it; returns (seconds, iterations, jobs).  With
+    a dict `keep`, its "e" receives the FP64 loop's corrected error."""
     from oracle import ffcz_oracle as O
 
     t0 = time.perf_counter()
-    e0 = fld.xp.astype(np.float64) - fld.x.astype(np.float64)
-    r = O.solve_all_abs(e0.astype(fld.x.dtype), fld.shape, fld.eps, fld.delta, max_iter, 1e-7, np.float64)
+    e0 = (fld.xp - fld.x).astype(fld.x.dtype)  # as projection_example.cu:173-176
+    r = O.solve_all_abs(e0, fld.shape, fld.eps, fld.delta, max_iter, 1e-7, np.float64)
+    if keep is not None:
+        keep["e"] = r["e"]
     fe = O.extract(r["freq_edits"].astype(fld.x.dtype))
     se = O.extract(r["spatial_edits"].astype(fld.x.dtype))
     jobs = []
@@ -172,17 +199,19 @@ def cpu_step(fld, max_iter, level, pool=None):
     return time.perf_counter() - t0, r["iterations"], jobs
 
 
-def cpu_baseline(fld, max_iter, level, budget_s=25.0):
+def cpu_baseline(fld, max_iter, level, budget_s=25.0, return_e=False):
     times, its = [], 0
+    keep = {}
     t_start = time.perf_counter()
     while not times or (time.perf_counter() - t_start < budget_s and len(times) < 3):
-        t, its, _ = cpu_step(fld, max_iter, level)
+        t, its, _ = cpu_step(fld, max_iter, level, keep=keep)
         times.append(t)
     nbytes = fld.x.nbytes
-    return {"value": nbytes / statistics.median(times) / 1e9, "unit": "GB/s", "cores": os.cpu_count(),
-            "kind": "port",
-            "sample": f"{len(times)} full project+encode step(s) of the same field ({its} iteration(s), FP64 "
-                      f"pocketfft with {os.cpu_count()} workers, C compaction/Huffman, libzstd level {level})"}
+    out = {"value": nbytes / statistics.median(times) / 1e9, "unit": "GB/s", "cores": os.cpu_count(),
+           "kind": "port",
+           "sample": f"{len(times)} full project+encode step(s) of the same field ({its} iteration(s), FP64 "
+                     f"pocketfft with {os.cpu_count()} workers, C compaction/Huffman, libzstd level {level})"}
+    return (out, keep.get("e")) if return_e else out
 
 
 def run_reference(args):
@@ -195,29 +224,37 @@ def run_reference(args):
         return run_reference_batch(args)
     fld, max_iter = load_workload(args.workload)
     pool = ThreadPoolExecutor(max_workers=os.cpu_count())
-    for _ in range(args.warmup):
+    # A step is one full project+encode pass of the field; a 512^3 step takes
+    # several seconds on the host cores, so warm-up and timed steps are
+    # capped by a time budget (the line reports the steps actually timed).
+    budget = args.reference_budget_s
+    t0 = time.perf_counter()
+    for _ in range(min(args.warmup, 1)):
         for f in cpu_step(fld, max_iter, args.zstd_level, pool)[2]:
             f.result()
+    warm = time.perf_counter() - t0
+    steps = max(1, min(args.steps, int(budget / max(warm, 1e-3)) if warm else args.steps))
     its = 0
     jobs = []
     t0 = time.perf_counter()
-    for _ in range(args.steps):
+    for _ in range(steps):
         _, its, j = cpu_step(fld, max_iter, args.zstd_level, pool)
         jobs += j
     for f in jobs:
         f.result()
     total = time.perf_counter() - t0
     pool.shutdown()
-    v = fld.x.nbytes * args.steps / total / 1e9
-    line = {"metric": METRIC, "value": v, "unit": "GB/s", "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+    v = fld.x.nbytes * steps / total / 1e9
+    line = {"metric": METRIC, "value": v, "unit": "GB/s", "n_gpus": args.gpus, "steps": steps,
+            "steps_requested": args.steps, "warmup": min(args.warmup, 1), "ms_per_step": 1e3 * total / steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "impl": "reference",
-            "config": config(args, fld, its),
+            "config": config(args, fld, its, max_iter),
             "cpu_baseline": {"value": v, "unit": "GB/s", "cores": os.cpu_count(), "kind": "port",
-                             "sample": f"{args.steps} full project+encode steps of the workload "
-                                       f"({its} iteration(s) each) on {os.cpu_count()} host threads, "
-                                       "ZSTD of earlier steps overlapped on a thread pool"},
+                             "sample": f"{steps} full project+encode steps of the workload "
+                                       f"({its} iteration(s) each; steps capped by a {budget:g} s budget) on "
+                                       f"{os.cpu_count()} host threads, ZSTD of earlier steps overlapped on a "
+                                       "thread pool"},
             "e2e": {"value": v, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
@@ -255,11 +292,12 @@ def run_reference_batch(args):
     print(json.dumps(line))
 
 
-def config(args, fld, its):
+def config(args, fld, its, max_iter=100, strict=False):
     return {"workload": f"{args.workload}: {'x'.join(map(str, fld.shape))} {fld.x.dtype}, "
-                        f"E={fld.eps:.4g}, Delta={fld.delta:.4g}, max_iter 100, tol 1e-7",
+                        f"E={fld.eps:.4g}, Delta={fld.delta:.4g}, max_iter {max_iter}, tol 1e-7",
             "iterations": its, "zstd_level": args.zstd_level, "zstd_mode": args.zstd_mode,
-            "l2": "inputs and working set (x, x', e, spectrum, edits: >400 MB) larger than L2",
+            "strict_bounds": bool(strict),
+            "l2": "inputs and working set (x, x', e, spectrum, edits) larger than L2",
             "parallelism": f"replicas x{args.gpus}", "loop": getattr(args, "loop", "graph"),
             **({"precision": "split: float-float passes on the FP32 pipes, FP64 storage, boxes and checks"
                 if getattr(args, "precision", "native") == "split" else "native FP64"}
@@ -278,173 +316,301 @@ def run_ours(args):
     zmode = F.FFCZ_ZSTD_CHUNKED if args.zstd_mode == "chunked" else F.FFCZ_ZSTD_SINGLE
     dt = fld.x.dtype
     N = fld.x.size
+    in_bytes = N * dt.itemsize
     x_h = torch.from_numpy(fld.x.reshape(-1)).pin_memory()
+    # e0 = x' - x in T on the host, as projection_example.cu:173-176 computes it
     e0_np = (fld.xp - fld.x).astype(dt).reshape(-1)
     e0_h = torch.from_numpy(e0_np).pin_memory()
     dx = x_h.cuda()
     dxp = torch.from_numpy(fld.xp.reshape(-1)).cuda()
-    s = F.ProjectionSolver(*fld.shape, dtype=dt)
-    if dt == np.float64 and args.precision == "split":
-        s.set_precision(F.FFCZ_PRECISION_SPLIT)
-    s.set_stream(torch.cuda.current_stream())
-    s.set_loop_driver(F.FFCZ_LOOP_HOST if args.loop == "host" else F.FFCZ_LOOP_GRAPH)
-    s.set_profiling(True)
-    s.initialize_all_abs_device(dx, fld.eps, fld.delta)
-    tune = {} if args.no_autotune else s.autotune(5)
-
     nzt = args.zstd_threads or (os.cpu_count() or 1)
     pool = ThreadPoolExecutor(max_workers=nzt)
+    strict = not args.no_strict
 
     def zstd_jobs(res):
         return [pool.submit(F.zstd_compress, r.bitstream, args.zstd_level, zmode) for r in res if r is not None]
 
-    def step_device():
-        s.reset_edit_accumulators()
-        s.solve_all_abs_pair_device(dx, dxp, max_iter, 1e-7)
-        res = s.encode(args.zstd_level, F.FFCZ_ZSTD_NONE)  # Huffman bitstreams; ZSTD on the pool
-        return s.launch_count(), res, zstd_jobs(res)
+    def make_solver(form, delta=None):
+        s = F.ProjectionSolver(*fld.shape, dtype=dt)
+        if dt == np.float64 and args.precision == "split":
+            s.set_precision(F.FFCZ_PRECISION_SPLIT)
+        s.set_form(form)
+        s.set_stream(torch.cuda.current_stream())
+        s.set_loop_driver(F.FFCZ_LOOP_HOST if args.loop == "host" else F.FFCZ_LOOP_GRAPH)
+        s.set_profiling(True)
+        s.initialize_all_abs_device(dx, fld.eps, fld.delta if delta is None else delta)
+        tune = {} if args.no_autotune else s.autotune(5)
+        return s, tune
 
-    def step_e2e():
-        s.reset_edit_accumulators()
-        s.initialize_all_abs(x_h.numpy(), fld.eps, fld.delta)
-        s.solve_all_abs(e0_h.numpy(), max_iter, 1e-7)
-        res = s.encode(args.zstd_level, F.FFCZ_ZSTD_NONE)
-        return res, zstd_jobs(res)
+    def measure_form(s):
+        """One step = reset, projections (+ strict FP64 bounds), compaction,
+        Huffman, ZSTD on the host pool; three timings of it."""
+        rep = {}
 
-    for _ in range(args.warmup):
-        for f in step_device()[2]:
+        def step_device(zstd=True):
+            s.reset_edit_accumulators()
+            s.solve_all_abs_pair_device(dx, dxp, max_iter, 1e-7)
+            st = s.strict_finish(max_iter, 1e-7, 4) if strict else None
+            res = s.encode(args.zstd_level, F.FFCZ_ZSTD_NONE)  # Huffman bitstreams; ZSTD on the pool
+            return s.launch_count(), res, (zstd_jobs(res) if zstd else []), st
+
+        def step_e2e():
+            s.reset_edit_accumulators()
+            s.initialize_all_abs(x_h.numpy(), fld.eps, fld.delta)
+            s.solve_all_abs(e0_h.numpy(), max_iter, 1e-7)
+            if strict:
+                s.strict_finish(max_iter, 1e-7, 4)
+            res = s.encode(args.zstd_level, F.FFCZ_ZSTD_NONE)
+            return res, zstd_jobs(res)
+
+        for _ in range(args.warmup):
+            for f in step_device()[2]:
+                f.result()
+        torch.cuda.synchronize()
+        # value: x and x' resident in HBM, project + strict + encode incl. ZSTD
+        clocks = Clocks()
+        barrier(world)
+        torch.cuda.synchronize()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record()
+        jobs, launches, pass_ms, st = [], 0, {}, None
+        for _ in range(args.steps):
+            n, out, j, st = step_device()
+            jobs += j
+            launches += n
+            for i, (ms, by) in enumerate(s.pass_times()):
+                pass_ms.setdefault(i, []).append((ms, by))
+        comp = [f.result() for f in jobs]
+        ev1.record()
+        torch.cuda.synchronize()
+        barrier(world)
+        t_dev = max_over_ranks(ev0.elapsed_time(ev1) / 1e3, world)
+        rep["clocks"] = clocks.stop()
+        rep["t_dev"] = t_dev
+        rep["ms_per_step"] = 1e3 * t_dev / args.steps
+        rep["value"] = in_bytes * args.steps * world / t_dev / 1e9
+        rep["launches"] = launches
+        rep["pass_ms"] = pass_ms
+        rep["strict"] = st
+        rep["compressed_bytes"] = sum(len(c) for c in comp[-len(j):]) if j else 0
+        rep["out"] = out
+        # GPU-only: project + strict + Huffman, no ZSTD
+        torch.cuda.synchronize()
+        ev0.record()
+        for _ in range(args.steps):
+            step_device(zstd=False)
+        ev1.record()
+        torch.cuda.synchronize()
+        rep["gpu_only"] = in_bytes * args.steps * world / max_over_ranks(ev0.elapsed_time(ev1) / 1e3, world) / 1e9
+        # e2e through the reference-facing API with host buffers
+        for _ in range(max(1, args.warmup // 2)):
+            for f in step_e2e()[1]:
+                f.result()
+        torch.cuda.synchronize()
+        barrier(world)
+        t0 = time.perf_counter()
+        jobs = []
+        out_e = []
+        for _ in range(args.steps):
+            out_e, j = step_e2e()
+            jobs += j
+        for f in jobs:
             f.result()
+        torch.cuda.synchronize()
+        t_e2e = max_over_ranks(time.perf_counter() - t0, world)
+        rep["e2e"] = in_bytes * args.steps * world / t_e2e / 1e9
+        rep["d2h"] = sum(len(r.bitstream) for r in out_e if r is not None) + 8 * 4
+        rep["its"] = s.iterations
+        rep["counts"] = s.active_counts()
+        return rep
+
+    chosen, tune = make_solver(F.FFCZ_FORM_FUSED)
+    rc = measure_form(chosen)
+    its = rc["its"]
+    counts = rc["counts"]
+    e_fin = chosen.get_results()
+    # one step alone (latency) and where its host time goes
     torch.cuda.synchronize()
-    # one step alone (latency), and a check that the pipeline's bytes are
-    # ZSTD_compress's bytes
     t0 = time.perf_counter()
-    _, res1, jobs1 = step_device()
-    comp1 = [f.result() for f in jobs1]
-    step_latency = time.perf_counter() - t0
-    serial = s.encode(args.zstd_level, zmode)
-    assert [r.compressed_data for r in serial if r is not None] == comp1
-    torch.cuda.synchronize()
-    # where the host-side time of one step goes
-    tb = [time.perf_counter()]
-    s.reset_edit_accumulators()
-    tb.append(time.perf_counter())
-    s.solve_all_abs_pair_device(dx, dxp, max_iter, 1e-7)
-    tb.append(time.perf_counter())
-    res_b = s.encode(args.zstd_level, F.FFCZ_ZSTD_NONE)
-    tb.append(time.perf_counter())
-    s.pass_times()
-    tb.append(time.perf_counter())
-    jobs_b = zstd_jobs(res_b)
-    tb.append(time.perf_counter())
-    for f in jobs_b:
+    chosen.reset_edit_accumulators()
+    chosen.solve_all_abs_pair_device(dx, dxp, max_iter, 1e-7)
+    t1 = time.perf_counter()
+    if strict:
+        chosen.strict_finish(max_iter, 1e-7, 4)
+    t2 = time.perf_counter()
+    res_b = chosen.encode(args.zstd_level, F.FFCZ_ZSTD_NONE)
+    t3 = time.perf_counter()
+    for f in zstd_jobs(res_b):
         f.result()
-    tb.append(time.perf_counter())
-    breakdown = dict(zip(["reset", "solve", "huffman", "pass_times", "submit", "zstd_wait"],
-                         [round(1e3 * (b - a), 2) for a, b in zip(tb, tb[1:])]))
-    clocks = Clocks()
-    barrier(world)
-    torch.cuda.synchronize()
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    launches = 0
-    pass_ms = {}
-    ev0.record()
-    jobs = []
-    t_host0 = time.perf_counter()
-    for _ in range(args.steps):
-        n, out, j = step_device()
-        jobs += j
-        launches += n
-        for i, (ms, by) in enumerate(s.pass_times()):
-            pass_ms.setdefault(i, []).append((ms, by))
-    t_serial = (time.perf_counter() - t_host0) / args.steps
-    comp = [f.result() for f in jobs]
-    ev1.record()
-    torch.cuda.synchronize()
-    barrier(world)
-    t_dev = ev0.elapsed_time(ev1) / 1e3
-    t_dev = max_over_ranks(t_dev, world)
-    clk = clocks.stop()
-    comp_bytes = sum(len(c) for c in comp[-len(j):]) if j else 0
-    its = s.iterations
-    counts = s.active_counts()
-    # FP64 check of both bounds on the corrected field x^ = x + e
-    from oracle import ffcz_oracle as O  # checker only, outside the timed region
+    t4 = time.perf_counter()
+    breakdown = {"solve": round(1e3 * (t1 - t0), 3), "strict": round(1e3 * (t2 - t1), 3),
+                 "huffman": round(1e3 * (t3 - t2), 3), "zstd_wait": round(1e3 * (t4 - t3), 3)}
+    serial = chosen.encode(args.zstd_level, zmode)
+    assert [r.compressed_data for r in serial if r is not None] == [
+        F.zstd_compress(r.bitstream, args.zstd_level, zmode) for r in res_b if r is not None]
+    decode = measure_decode(F, torch, chosen, fld, dxp, args)
+    modes = measure_modes(F, chosen, fld, e0_np, dx) if N <= 256 ** 3 else {"note": "measured at 256^3 and below"}
+    chosen.close()
 
-    e_fin = s.get_results()
-    bchk = O.check_bounds(np.zeros(1), e_fin.astype(np.float64), fld.eps, fld.delta)
-    dsm, dfm = s.verify_bounds()
-    bounds = {"spatial_max_over_E": bchk["spatial_max"] / fld.eps, "freq_max_over_Delta": bchk["freq_max"] / fld.delta,
-              "met": bool(bchk["spatial_excess"] <= 1e-7 and bchk["freq_excess"] <= 0.0),
-              "rule": "reference schedule: spatial within E + tol (1e-7), frequency within Delta",
-              "check": "FP64 numpy on the host; the device check (ffcz_verify_bounds) beside it",
-              "device": {"spatial_max_over_E": dsm / fld.eps, "freq_max_over_Delta": dfm / fld.delta}}
+    plain = None
+    if not args.no_plain:
+        ps, _ = make_solver(F.FFCZ_FORM_PLAIN)
+        plain = measure_form(ps)
+        e_plain = ps.get_results()
+        plain["max_abs_diff_vs_chosen"] = float(np.abs(e_plain.astype(np.float64) - e_fin).max())
+        ps.close()
 
-    # e2e through the reference-facing API with host buffers
-    for _ in range(max(1, args.warmup // 2)):
-        for f in step_e2e()[1]:
-            f.result()
-    torch.cuda.synchronize()
-    barrier(world)
-    t0 = time.perf_counter()
-    jobs = []
-    for _ in range(args.steps):
-        out_e, j = step_e2e()
-        jobs += j
-    for f in jobs:
-        f.result()
-    torch.cuda.synchronize()
-    t_e2e = max_over_ranks(time.perf_counter() - t0, world)
-    d2h = sum(len(r.bitstream) for r in out_e if r is not None) + 8 * 4
+    stress = measure_stress(F, torch, fld, dx, dxp, max_iter, strict, args)
 
-    # the decoder on the last step's streams (GPU Huffman decode + reconstruction)
-    decode = measure_decode(F, torch, s, fld, dxp, args)
-    # the other constraint modes on the same field: fused-pass time and iterations
-    modes = measure_modes(F, s, fld, e0_np, dx)
-    # strict bounds after the reference schedule: the field as configured and
-    # a frequency-active stress variant
-    strict = measure_strict(F, torch, fld, e0_np)
-
-    # dominant pass of the first iteration, from the events inside the graph
+    # dominant pass of the chosen form (first iteration's events inside the graph)
     peak, peak_kind = peak_hbm()
     names = pass_names(fld.shape)
-    avg = {i: (statistics.mean(m for m, _ in v), v[0][1]) for i, v in pass_ms.items()}
+    avg = {i: (statistics.mean(m for m, _ in v), v[0][1]) for i, v in rc["pass_ms"].items()}
     dom = max(avg, key=lambda i: avg[i][0])
     ms_dom, by_dom = avg[dom]
     achieved = by_dom / (ms_dom / 1e3) / 1e9
-    # GPU-only (project + Huffman, no ZSTD) for reference
-    value = N * dt.itemsize * args.steps * world / t_dev / 1e9
+    traffic = TRAFFIC.get(args.workload, {}).get(names[dom])
+
+    # FP64 check of both bounds on the output e (numpy, after the timed region)
+    from oracle import ffcz_oracle as O  # checker only
+
+    chk = O.check_bounds(np.zeros(1), e_fin.astype(np.float64), fld.eps, fld.delta)
+    st = rc["strict"] or {}
+    bounds = {"met": bool(chk["spatial_max"] <= fld.eps and chk["freq_max"] <= fld.delta),
+              "spatial_max_over_E": chk["spatial_max"] / fld.eps, "freq_max_over_Delta": chk["freq_max"] / fld.delta,
+              "rule": "|e_i| <= E and |Re/Im rfftn(e)_k| <= Delta in FP64, no slack" if strict else
+                      "reference schedule (no strict finish): |e_i| <= E + tol",
+              "check": "numpy FP64 on the host after the timed region",
+              "in_step": ({"decided_by": "certificate" if st.get("certified") else "FP64 transform",
+                           "met": st.get("met"), "rounds": st.get("rounds"),
+                           "cert_freq_max_over_Delta": st.get("cert_freq_max", 0.0) / fld.delta,
+                           "cert_bound_over_Delta": st.get("cert_bound", 0.0) / fld.delta} if strict else None)}
     line = {
-        "metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": 1e3 * t_dev / args.steps, "higher_is_better": True,
+        "metric": METRIC, "value": rc["value"], "unit": "GB/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * rc["t_dev"] / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32" if dt == np.float32 else "f64",
-        "data": "synthetic", "config": config(args, fld, its),
-        "e2e": {"value": N * dt.itemsize * args.steps * world / t_e2e / 1e9, "unit": "GB/s",
-                "h2d_bytes_per_step": 2 * N * dt.itemsize, "d2h_bytes_per_step": d2h},
+        "data": "synthetic", "config": config(args, fld, its, max_iter, strict),
+        "e2e": {"value": rc["e2e"], "unit": "GB/s", "h2d_bytes_per_step": 2 * in_bytes, "d2h_bytes_per_step": rc["d2h"]},
+        "forms": form_report(rc, plain),
+        "gpu_only": {"value": rc["gpu_only"], "unit": "GB/s",
+                     "what": "project + strict bounds + compaction + Huffman, device-resident inputs, no ZSTD"},
         "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": f"{peak_kind} hbm_gbs",
-                     "traffic": TRAFFIC.get(args.workload, {}).get(names[dom]),
-                     "algorithmic_bytes_per_launch": by_dom, "avg_launch_ms": ms_dom},
+                     "traffic": traffic, "algorithmic_bytes_per_launch": by_dom, "avg_launch_ms": ms_dom},
         "passes": {names[i]: {"ms": round(m, 5), "GB/s": round(b / (m / 1e3) / 1e9, 1)} for i, (m, b) in avg.items()},
-        "gpu_launches": launches,
+        "gpu_launches": rc["launches"],
         "autotune_ms": {k: [round(v[0], 4), round(v[1], 4)] for k, v in tune.items()},
-        "decode": decode,
-        "modes": modes,
-        "strict": strict,
-        "step_latency_ms": 1e3 * step_latency,
-        "serial_ms_per_step": 1e3 * t_serial,
-        "serial_breakdown_ms": breakdown,
-        "zstd_threads": nzt,
+        "iterations": its,
         "active_edits": {"freq": counts[0], "spatial": counts[1]},
         "bounds_fp64": bounds,
-        "compressed_bytes": comp_bytes,
-        "clocks": clk,
+        "stress": stress,
+        "decode": decode,
+        "modes": modes,
+        "serial_breakdown_ms": breakdown,
+        "compressed_bytes": rc["compressed_bytes"],
+        "zstd_threads": nzt,
+        "clocks": rc["clocks"],
     }
+    if rank == 0 and world == 1 and not args.no_cufft_reference:
+        line["cufft_reference"] = cufft_reference(fld, max_iter, args)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(fld, max_iter, args.zstd_level)
+        cb, e64 = cpu_baseline(fld, max_iter, args.zstd_level, return_e=True)
+        line["cpu_baseline"] = cb
+        if e64 is not None:
+            err = float(np.abs(e_fin.astype(np.float64).reshape(-1) - e64.reshape(-1)).max())
+            line["max_err_vs_fp64_oracle"] = {
+                "max_abs": err, "over_E": err / fld.eps, "over_max_abs_e": err / float(np.abs(e64).max()),
+                "note": "e of the chosen form (after the strict finish) against the FP64 oracle's e "
+                        "(the reference loop in FP64, pocketfft)"}
     if rank == 0:
         print(json.dumps(line))
     pool.shutdown()
-    s.close()
+
+
+def form_report(rc, plain):
+    def one(r):
+        return {"value": r["value"], "e2e": r["e2e"], "gpu_only": r["gpu_only"], "ms_per_step": r["ms_per_step"],
+                "passes_per_iteration": len(r["pass_ms"]), "iterations": r["its"], "clocks": r["clocks"]}
+
+    out = {"chosen": dict(one(rc), form="fused: five HBM passes per 3D iteration (x forward + clamp + x inverse "
+                                        "in one pass), graph-captured loop, strict FP64 bounds by certificate "
+                                        "or FP64 transform")}
+    if plain is not None:
+        out["plain_fp32"] = dict(one(plain), form="plain FP32: six HBM passes per 3D iteration (x forward + "
+                                                  "clamp and x inverse separate), same kernels otherwise",
+                                 max_abs_diff_vs_chosen=plain["max_abs_diff_vs_chosen"])
+        out["ratio_value"] = rc["value"] / plain["value"]
+        out["ratio_e2e"] = rc["e2e"] / plain["e2e"]
+        out["ratio_gpu_only"] = rc["gpu_only"] / plain["gpu_only"]
+    return out
+
+
+def measure_stress(F, torch, fld, dx, dxp, max_iter, strict, args, c=1.0):
+    """The field with Delta = c E sqrt(N/6), where frequency clamps fire:
+    one step (project + strict + Huffman, no ZSTD) after one warm-up,
+    device events."""
+    from ffcz_gb300 import synth
+
+    delta = synth.stress_delta(fld, c)
+    with F.ProjectionSolver(*fld.shape, dtype=fld.x.dtype) as m:
+        m.set_stream(torch.cuda.current_stream())
+        m.initialize_all_abs_device(dx, fld.eps, delta)
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ms = []
+        for k in range(2):
+            m.reset_edit_accumulators()
+            torch.cuda.synchronize()
+            ev0.record()
+            m.solve_all_abs_pair_device(dx, dxp, max_iter, 1e-7)
+            its = m.iterations
+            st = m.strict_finish(max_iter, 1e-7, 4) if strict else {}
+            res = m.encode(args.zstd_level, F.FFCZ_ZSTD_NONE)
+            ev1.record()
+            torch.cuda.synchronize()
+            ms.append(ev0.elapsed_time(ev1))
+        nf, ns = m.active_counts()
+        return {"delta_rule": f"Delta = {c:g} E sqrt(N/6)", "Delta": delta, "ms": round(ms[-1], 3),
+                "GB/s": fld.x.nbytes / (ms[-1] / 1e3) / 1e9, "iterations": its, "iterations_after_strict": m.iterations,
+                "freq_edits": nf, "spatial_edits": ns, "strict": st,
+                "bitstream_bytes": sum(len(r.bitstream) for r in res if r is not None),
+                "what": "project + strict bounds + compaction + Huffman (no ZSTD), device-resident inputs"}
+
+
+def cufft_reference(fld, max_iter, args):
+    """The reference's own cuFFT build (oracle/ref_solver, built from the
+    unmodified reference sources) timed on this GPU on the same field:
+    reset + initialize_all_abs (H2D of x) + solve_all_abs (H2D of e0, the
+    loop, the compaction) + the four getters + cudaHuffmanZstdCompress of the
+    non-empty streams (projection_example.cu:157-246)."""
+    harness = ROOT / "oracle" / "_ref" / "ref_solver"
+    if not harness.exists():
+        return {"unavailable": "oracle/_ref/ref_solver not built (reference sources absent at build time)"}
+    nx, ny, nz = fld.shape
+    with tempfile.TemporaryDirectory() as t:
+        t = Path(t)
+        fld.x.tofile(t / "x.bin")
+        fld.xp.tofile(t / "xp.bin")
+        steps = max(1, min(args.steps, 10))
+        clocks = Clocks()
+        r = subprocess.run([str(harness), "bench", "f64" if fld.x.dtype == np.float64 else "f32", str(nx), str(ny),
+                            str(nz), str(t / "x.bin"), str(t / "xp.bin"), repr(fld.eps), repr(fld.delta),
+                            str(max_iter), "1e-07", str(args.zstd_level), str(steps), "1"],
+                           capture_output=True, text=True, timeout=900)
+        clk = clocks.stop()
+    if r.returncode != 0:
+        return {"unavailable": f"harness exit {r.returncode}: {r.stderr.strip()[-300:]}"}
+    j = json.loads(r.stdout.strip().splitlines()[-1])
+    nb = fld.x.nbytes
+    path = j["solve_ms"] + j["getters_ms"] + j["huffman_zstd_ms"]
+    return {"value": nb / ((path + j["init_ms"]) / 1e3) / 1e9, "unit": "GB/s",
+            "what": "reset + initialize_all_abs + solve_all_abs + getters + Huffman/ZSTD of the non-empty streams "
+                    "(host buffers, the same work as this line's e2e)",
+            "value_without_init": nb / (path / 1e3) / 1e9,
+            "cli_formula_ms": 3 * j["getters_ms"] + j["solve_ms"],
+            "ms": {k: j[k] for k in ("init_ms", "solve_ms", "getters_ms", "huffman_zstd_ms")},
+            "iterations": j["iterations"], "active_edits": {"freq": j["active_freq"], "spatial": j["active_spatial"]},
+            "steps": j["steps"], "build": "unmodified reference sources, nvcc -O3 -rdc=true sm_103a, cuFFT 12, CUB, "
+                                         "Thrust, libzstd", "clocks": clk}
 
 
 def measure_decode(F, torch, s, fld, dxp, args, reps=5):
@@ -488,31 +654,6 @@ def measure_modes(F, s, fld, e0_np, dx):
         pt = m.pass_times()
         res["all_ptw"] = {"iterations": it, "delta_ptw": 0.05,
                           "passes_ms": [round(ms, 5) for ms, _ in pt]}
-    return res
-
-
-def measure_strict(F, torch, fld, e0_np):
-    """ffcz_strict_finish after an all-abs solve: wall time of the finish
-    (clamp, FP64 check on the device, re-runs on a shrunk box), rounds, and
-    the FP64 maxima over the bounds the solver holds.  Run on the field as
-    configured and with Delta = E sqrt(N/6), where frequency clamps are
-    active."""
-    from ffcz_gb300 import synth
-
-    res = {}
-    T = fld.x.dtype.type
-    for name, delta in (("config", fld.delta), ("stress_c1", synth.stress_delta(fld, 1.0))):
-        with F.ProjectionSolver(*fld.shape, dtype=fld.x.dtype) as m:
-            m.initialize_all_abs(fld.x, fld.eps, delta)
-            it = m.solve_all_abs(e0_np, 100, 1e-7)
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            st = m.strict_finish(100, 1e-7, 4)
-            ms = (time.perf_counter() - t0) * 1e3
-            E, D = float(T(fld.eps)), float(T(delta))
-            res[name] = {"ms": round(ms, 3), "rounds": st["rounds"], "met": st["met"],
-                         "iterations": [it, m.iterations], "freq_edits": m.active_counts()[0],
-                         "spatial_max_over_E": st["spatial_max"] / E, "freq_max_over_Delta": st["freq_max"] / D}
     return res
 
 

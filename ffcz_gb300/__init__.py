@@ -31,6 +31,9 @@ FFCZ_MODE_ALL_ABS, FFCZ_MODE_DIRECT, FFCZ_MODE_ALL_PTW, FFCZ_MODE_PARTIAL_PTW = 
 FFCZ_LOOP_GRAPH, FFCZ_LOOP_HOST = 0, 1
 FFCZ_PRECISION_NATIVE, FFCZ_PRECISION_SPLIT = 0, 1
 FFCZ_ZSTD_SINGLE, FFCZ_ZSTD_CHUNKED, FFCZ_ZSTD_NONE = 0, 1, 2
+FFCZ_FORM_FUSED, FFCZ_FORM_PLAIN = 0, 1
+FFCZ_ERR_INVALID, FFCZ_ERR_CUDA, FFCZ_ERR_UNSUPPORTED, FFCZ_ERR_NOT_INITIALIZED = -1, -2, -3, -4
+FFCZ_ERR_ZSTD, FFCZ_ERR_CAPACITY, FFCZ_ERR_CODE_TOO_LONG, FFCZ_ERR_EMPTY, FFCZ_ERR_IO = -5, -6, -7, -8, -9
 ERRORS = {-1: "INVALID", -2: "CUDA", -3: "UNSUPPORTED", -4: "NOT_INITIALIZED", -5: "ZSTD",
           -6: "CAPACITY", -7: "CODE_TOO_LONG", -8: "EMPTY", -9: "IO"}
 
@@ -64,6 +67,7 @@ _i = C.c_int
 _d = C.c_double
 _PP = C.POINTER(C.c_void_p)
 _SP = C.POINTER(C.c_size_t)
+_DP = C.POINTER(C.c_double)
 
 # name -> argtypes (all return int unless listed in _RET)
 SIGNATURES = {
@@ -72,6 +76,7 @@ SIGNATURES = {
     "ffcz_solver_set_stream": [_p, _p],
     "ffcz_solver_set_loop_driver": [_p, _i],
     "ffcz_solver_set_pack_mode": [_p, _i],
+    "ffcz_solver_set_form": [_p, _i],
     "ffcz_init_all_abs": [_p, _p, _d, _d],
     "ffcz_init_all_abs_device": [_p, _p, _d, _d],
     "ffcz_solve_all_abs": [_p, _p, _i, _d],
@@ -80,6 +85,7 @@ SIGNATURES = {
     "ffcz_project_all_abs_device": [_p, _p, _i, _d],
     "ffcz_extract": [_p],
     "ffcz_reset_edit_accumulators": [_p],
+    "ffcz_set_edit_accumulators": [_p, _p, _p],
     "ffcz_solver_synchronize": [_p],
     "ffcz_get_iterations": [_p, C.POINTER(C.c_int)],
     "ffcz_get_convergence": [_p, C.POINTER(C.c_double)],
@@ -136,6 +142,8 @@ SIGNATURES = {
     "ffcz_get_orig_spectrum": [_p, _p, _sz],
     "ffcz_verify_bounds": [_p, C.POINTER(C.c_double), C.POINTER(C.c_double)],
     "ffcz_strict_finish": [_p, _i, _d, _i, _p, _p, _p, _p],
+    "ffcz_certify_bounds": [_p, _DP, _DP, _DP, C.POINTER(C.c_int)],
+    "ffcz_get_strict_report": [_p, C.POINTER(C.c_int), _DP, _DP],
     "ffcz_solver_autotune": [_p, _i, _p],
     "ffcz_solver_set_precision": [_p, _i],
     "ffcz_init_all_ptw": [_p, _p, _d, _d],
@@ -235,6 +243,11 @@ class ProjectionSolver:
     def set_pack_mode(self, mode: int) -> None:
         _check(lib().ffcz_solver_set_pack_mode(self._h, mode))
 
+    def set_form(self, form: int) -> None:
+        """FFCZ_FORM_FUSED (five passes per 3D iteration) or FFCZ_FORM_PLAIN
+        (six: x forward + clamp and x inverse as separate passes)."""
+        _check(lib().ffcz_solver_set_form(self._h, int(form)))
+
     # -- reference API -------------------------------------------------------
     def _host(self, a) -> np.ndarray:
         a = np.ascontiguousarray(a, dtype=self.dtype).reshape(-1)
@@ -314,7 +327,17 @@ class ProjectionSolver:
         _check(lib().ffcz_strict_finish(self._h, int(max_iterations), float(tol), int(max_rounds), C.byref(r),
                                         C.byref(m), C.byref(a), C.byref(b)))
         self._iters()
-        return {"rounds": r.value, "met": bool(m.value), "spatial_max": a.value, "freq_max": b.value}
+        c, f, bd = C.c_int(), C.c_double(), C.c_double()
+        _check(lib().ffcz_get_strict_report(self._h, C.byref(c), C.byref(f), C.byref(bd)))
+        return {"rounds": r.value, "met": bool(m.value), "spatial_max": a.value, "freq_max": b.value,
+                "certified": bool(c.value), "cert_freq_max": f.value, "cert_bound": bd.value}
+
+    def certify_bounds(self) -> dict:
+        """Certificate of both bounds from the solver's own transform of e and
+        a bound on its rounding (no FP64 transform); e is not changed."""
+        a, f, bd, c = C.c_double(), C.c_double(), C.c_double(), C.c_int()
+        _check(lib().ffcz_certify_bounds(self._h, C.byref(a), C.byref(f), C.byref(bd), C.byref(c)))
+        return {"spatial_max": a.value, "freq_max": f.value, "bound": bd.value, "certified": bool(c.value)}
 
     def get_orig_spectrum(self) -> np.ndarray:
         """The spectrum of x the pointwise modes compare against (H complex)."""
@@ -345,6 +368,22 @@ class ProjectionSolver:
 
     def reset_edit_accumulators(self) -> None:
         _check(lib().ffcz_reset_edit_accumulators(self._h))
+
+    def set_edit_accumulators(self, freq_edits=None, spatial_edits=None) -> None:
+        """Loads edit arrays computed elsewhere (2H planar frequency edits,
+        N spatial edits; None keeps an accumulator) for extract / encode."""
+        keep = []
+        ptrs = []
+        for a, n in ((freq_edits, 2 * self.H), (spatial_edits, self.N)):
+            if a is None:
+                ptrs.append(None)
+                continue
+            a = np.ascontiguousarray(a, self.dtype).reshape(-1)
+            if a.size != n:
+                raise ValueError(f"edit array of {a.size} elements, expected {n}")
+            keep.append(a)
+            ptrs.append(_np_ptr(a))
+        _check(lib().ffcz_set_edit_accumulators(self._h, *ptrs))
 
     def synchronize(self) -> None:
         _check(lib().ffcz_solver_synchronize(self._h))

@@ -11,18 +11,21 @@
 // counts, minima, maxima and the result words) in the fixed array below,
 // which every GPU that loads the library holds until the process exits.
 //
-// Set-up: the first call on each device, with that device current, resolves
-// the array's device address with cudaGetSymbolAddress (host code cannot use
-// the array's name as a device address).  Make that first call before any
-// stream capture starts.
+// Set-up: every call resolves the array's device address on the current
+// device with cudaGetSymbolAddress (host code cannot use the array's name as
+// a device address).  Resolving it per call, rather than caching it per
+// device index, keeps the address right when the caller destroys and
+// re-creates the device's primary context (cudaDeviceReset reloads the
+// module, which moves the array); the lookup is negligible next to the
+// stream synchronisation every call ends with.  The first call on a device
+// may load the library's device code, so make it before any stream capture
+// starts.
 //
 // Sharing: all calls on a device use the same array and it keeps the last
 // call's contents.  Every scratch word a call reads is written earlier in
 // the same call, so nothing needs clearing, but calls whose work overlaps
 // on the GPU (different streams or host threads without ordering) race on
 // the array and give wrong results.
-#include <mutex>
-
 #include "extract.cuh"
 
 namespace ffcz {
@@ -39,20 +42,12 @@ static_assert(kScratchBytes == FFCZ_NOALLOC_SCRATCH_BYTES, "scratch size in ffcz
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
 namespace {
-std::mutex g_mu;
-unsigned char *g_scratch_addr[64];  // device address per device, 0 until set up
 
+// Device address of the scratch array on the current device and context.
 int scratch_for_current_device(unsigned char **out) {
-  int dev = 0;
-  FFCZ_CUDA(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= 64) return fail(FFCZ_ERR_INVALID, "device index out of range");
-  std::lock_guard<std::mutex> lk(g_mu);
-  if (!g_scratch_addr[dev]) {
-    void *p = nullptr;
-    FFCZ_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
-    g_scratch_addr[dev] = (unsigned char *)p;
-  }
-  *out = g_scratch_addr[dev];
+  void *p = nullptr;
+  FFCZ_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+  *out = (unsigned char *)p;
   return FFCZ_OK;
 }
 
@@ -113,6 +108,13 @@ extern "C" int ffcz_compact_quantize_noalloc(const void *d_edits, size_t n, int 
     return fail(FFCZ_ERR_CAPACITY, "ffcz_compact_quantize_noalloc: n = " + std::to_string(n) +
                                        " exceeds the fixed scratch limit of " +
                                        std::to_string((size_t)FFCZ_NOALLOC_MAX_ELEMS) + " elements");
+  // The kernels read d_edits with 16-byte vector loads, write the flag pack
+  // as 32-bit words and the compact values and codes as whole elements; a
+  // misaligned pointer is rejected here instead of faulting on the device.
+  if (((uintptr_t)d_edits) & 15) return fail(FFCZ_ERR_INVALID, "d_edits must be 16-byte aligned");
+  if (((uintptr_t)d_compact) & (dtype == FFCZ_F32 ? 3 : 7))
+    return fail(FFCZ_ERR_INVALID, "d_compact must be aligned to its element size");
+  if (((uintptr_t)d_quant) & 1) return fail(FFCZ_ERR_INVALID, "d_quant must be 2-byte aligned");
   if (((uintptr_t)d_pack) & 3) return fail(FFCZ_ERR_INVALID, "d_pack must be 4-byte aligned");
   unsigned char *scr = nullptr;
   FFCZ_TRY(scratch_for_current_device(&scr));

@@ -26,8 +26,11 @@ namespace ffcz {
 enum { PRO_PLAIN = 0, PRO_DIFF = 1, PRO_CLAMP = 2 };
 // MODE_FCI: fused forward / all-abs clamp / inverse; MODE_FCIX: the same
 // with the other constraint modes (a kernel of its own, so that the all-abs
-// kernel keeps the code and registers of a plain clamp).
-enum { MODE_FWD = 0, MODE_INV = 1, MODE_FCI = 2, MODE_FCIX = 3 };
+// kernel keeps the code and registers of a plain clamp).  MODE_FC: forward
+// with the all-abs clamp in its epilogue, stored to HBM (the plain form's
+// last forward pass; the inverse is a MODE_INV pass of its own).
+enum { MODE_FWD = 0, MODE_INV = 1, MODE_FCI = 2, MODE_FCIX = 3, MODE_FC = 4 };
+constexpr int kStridedModes = 5;
 
 struct ZArgs {
   long long rows;  // Nx*Ny
@@ -399,14 +402,14 @@ __global__ void __launch_bounds__(sizeof(T) == 4 ? 512 : 256) k_strided(c2<T> *_
   } else {
     fft_tile<T, -1, EPT>(buf, p, P, lg, tid, nthr);
   }
-  if (MODE == MODE_FCI || MODE == MODE_FCIX) {
+  if (MODE == MODE_FCI || MODE == MODE_FCIX || MODE == MODE_FC) {
     bool hit = false;
     for (int it = tid; it < total; it += nthr) {
       const int l = it >> lg;
       const int c = it & (TW - 1);
       if (c < ncol) {
         const long long k = ((bb * s.L + l) * (long long)s.Q + q) * s.Hz + kz0 + c;
-        if (MODE == MODE_FCI)
+        if (MODE == MODE_FCI || MODE == MODE_FC)
           buf[l * P + c] = freq_clamp<T>(buf[l * P + c], ca.delta, fedits, k, H, hit);
         else
           buf[l * P + c] =
@@ -415,7 +418,7 @@ __global__ void __launch_bounds__(sizeof(T) == 4 ? 512 : 256) k_strided(c2<T> *_
     }
     mark_dirty(ca.fdirty, hit);
     __syncthreads();
-    fft_tile<T, +1, EPT>(buf, p, P, lg, tid, nthr);
+    if (MODE != MODE_FC) fft_tile<T, +1, EPT>(buf, p, P, lg, tid, nthr);
   }
   for (int it = tid; it < total; it += nthr) {
     const int l = it >> lg;

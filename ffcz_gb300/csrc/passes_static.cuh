@@ -383,7 +383,8 @@ __global__ void __launch_bounds__((L / rp_elems(L, CAP)) << LGTW,
   for (int i = 0; i < E; ++i)
     v[i] = live ? cvt<C>(src[(long long)first_pos<L, D0, CAP>(t, i) * s.Wtot]) : mkc<C>(C(0), C(0));
   RRun<C, D0, L, LY, 0, CAP, C>::run(v, buf, t, c, p);  // split: p.tw is the float-float table
-  if (MODE == MODE_FCI || MODE == MODE_FCIX) {
+  if (MODE == MODE_FCI || MODE == MODE_FCIX || MODE == MODE_FC) {
+    constexpr bool ABS = MODE == MODE_FCI || MODE == MODE_FC;  // the all-abs box
     bool hit = false;
     // split FCI: |hi| below this is inside the box (0 when delta is too small
     // for the margin to mean anything: every coefficient decides in FP64)
@@ -396,10 +397,10 @@ __global__ void __launch_bounds__((L / rp_elems(L, CAP)) << LGTW,
         if constexpr (SPLIT) {  // the box in FP64; unclamped values keep their split form
           // hi is within 2^-23 of the value: well inside the box, nothing to
           // decide in FP64 (the pointwise box always decides in FP64)
-          if (MODE == MODE_FCI && fabsf(v[i].x.hi) < dlo && fabsf(v[i].y.hi) < dlo) continue;
+          if (ABS && fabsf(v[i].x.hi) < dlo && fabsf(v[i].y.hi) < dlo) continue;
           const VG g = cvt<T>(v[i]);
           VG h;
-          if (MODE == MODE_FCI) {
+          if (ABS) {
             h = freq_clamp<T>(g, ca.delta, fedits, k, H, hit);
           } else {
             const long long pad = (bb * L + l) * s.Wtot + (long long)q * s.Hzp + kz0 + c;
@@ -407,7 +408,7 @@ __global__ void __launch_bounds__((L / rp_elems(L, CAP)) << LGTW,
           }
           if (h.x != g.x) v[i].x = C((double)h.x);
           if (h.y != g.y) v[i].y = C((double)h.y);
-        } else if (MODE == MODE_FCI) {
+        } else if (ABS) {
           v[i] = freq_clamp<T>(v[i], ca.delta, fedits, k, H, hit);
         } else {
           const long long pad = (bb * L + l) * s.Wtot + (long long)q * s.Hzp + kz0 + c;
@@ -419,10 +420,12 @@ __global__ void __launch_bounds__((L / rp_elems(L, CAP)) << LGTW,
     // The inverse's first stage reads the positions the forward's last
     // stage wrote, so the same registers continue.  A barrier separates the
     // forward's last shared reads from the inverse's first shared writes.
-    __syncthreads();
-    RRun<C, +1, L, LY, 0, CAP, C>::run(v, buf, t, c, p);
+    if constexpr (MODE != MODE_FC) {
+      __syncthreads();
+      RRun<C, +1, L, LY, 0, CAP, C>::run(v, buf, t, c, p);
+    }
   }
-  constexpr int DL = (MODE == MODE_FWD) ? -1 : +1;
+  constexpr int DL = (MODE == MODE_FWD || MODE == MODE_FC) ? -1 : +1;
   VG *dst = spec + bb * (long long)L * s.Wtot + (long long)q * s.Hzp + kz0 + c;
   if (live) {
 #pragma unroll

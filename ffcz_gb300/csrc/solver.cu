@@ -75,6 +75,7 @@ struct ffcz_solver {
   cudaStream_t cap = nullptr;         // private capture stream
   int loop_driver = FFCZ_LOOP_GRAPH;
   int pack_mode = FFCZ_PACK_CORRECT;
+  int form = FFCZ_FORM_FUSED;  // FFCZ_FORM_PLAIN: the six-pass all-abs iteration
   // device arrays
   void *d_x = nullptr, *d_e = nullptr, *d_spec = nullptr;
   void *d_fedits = nullptr, *d_sedits = nullptr;
@@ -111,7 +112,7 @@ struct ffcz_solver {
   Launch lz_f, lz_i, ly, lx;
   int has_x = 0, has_y = 0, fused = 0;  // fused: 0 none, 1 y, 2 x
   // kernels of each pass (generic or compile-time-sized), typed at launch
-  void *kzf[3] = {}, *kzi = nullptr, *ky[4] = {}, *kx[4] = {};
+  void *kzf[3] = {}, *kzi = nullptr, *ky[kStridedModes] = {}, *kx[kStridedModes] = {};
   int static_z = 0, static_y = 0, static_x = 0;
   bool z_generic = true, y_generic = true, x_generic = true;  // runtime-planned tile fits
   int z_ept = 0, y_ept = 0, x_ept = 0;  // values per thread of the runtime-planned tiles
@@ -136,6 +137,11 @@ struct ffcz_solver {
   int partial_dc = 0;
   ffcz_solver *verifier = nullptr;   // FP64 twin of ffcz_verify_bounds
   unsigned long long *d_vmax = nullptr;
+  void *d_cert = nullptr;            // certificate: per-block sums of squares, two maxima
+  // last strict finish: decided by the certificate (1) or the FP64 check (0),
+  // the certificate's max |Re/Im| of the spectrum and its error bound
+  int cert_ok = 0;
+  double cert_fmax = 0.0, cert_bound = 0.0, cert_smax = 0.0;
   bool extracted = false;
   // the two most recently used loop graphs (a strict-bounds re-run on a
   // shrunk box keeps the regular solve's graph)
@@ -186,6 +192,7 @@ int set_smem_attrs_e() {
   FFCZ_CUDA(cudaFuncSetAttribute(k_strided<T, MODE_INV, E>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
   FFCZ_CUDA(cudaFuncSetAttribute(k_strided<T, MODE_FCI, E>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
   FFCZ_CUDA(cudaFuncSetAttribute(k_strided<T, MODE_FCIX, E>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+  FFCZ_CUDA(cudaFuncSetAttribute(k_strided<T, MODE_FC, E>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
   return FFCZ_OK;
 }
 
@@ -214,6 +221,7 @@ void generic_strided(void **k) {
   k[MODE_INV] = (void *)k_strided<T, MODE_INV, E>;
   k[MODE_FCI] = (void *)k_strided<T, MODE_FCI, E>;
   k[MODE_FCIX] = (void *)k_strided<T, MODE_FCIX, E>;
+  k[MODE_FC] = (void *)k_strided<T, MODE_FC, E>;
 }
 
 // Compile-time kernels of the z passes (tile variant var); false when the
@@ -271,6 +279,14 @@ bool apply_static_strided(ffcz_solver *s, int axis, int var) {
   }
   if (!ok) return false;
   for (int m = 0; m < 4; ++m) k[m] = (void *)f[m];
+  // the plain form's forward-with-clamp pass shares MODE_FWD's tile; none
+  // for the float-float kernels (the plain form then is unavailable)
+  StridedFn<T> ffc = nullptr;
+  StaticGeom gfc;
+  k[MODE_FC] = (!used && static_strided_fc<T>(L, ffc, gfc, var) && gfc.TW == g[MODE_FWD].TW &&
+                gfc.threads == g[MODE_FWD].threads)
+                   ? (void *)ffc
+                   : nullptr;
   // plain passes: geometry of MODE_FWD (= MODE_INV); fused: of MODE_FCI
   for (int fam = 0; fam < 2; ++fam) {
     const StaticGeom &gg = g[fam ? MODE_FCI : MODE_FWD];
@@ -502,7 +518,34 @@ void launch_iteration(ffcz_solver *s, cudaStream_t st, int pro, const void *a, c
                                                               s->za, s->pz, post);
   mark();
   const long long H = (long long)s->H;
-  if (s->fused == 2) {
+  const bool plain = s->form == FFCZ_FORM_PLAIN && s->cmode == CLAMP_ABS &&
+                     (s->fused == 2 ? s->kx[MODE_FC] != nullptr : s->fused != 1 || s->ky[MODE_FC] != nullptr);
+  if (plain && s->fused == 2) {
+    // six passes: y forward, x forward + clamp, x inverse, y inverse
+    if (s->has_y) {
+      ((StridedFn<T>)s->ky[MODE_FWD])<<<s->ly.grid, s->ly.threads, s->ly.smem, st>>>(spec, s->sy, s->py, delta,
+                                                                                     tp<T>(s->d_fedits), H);
+      mark();
+    }
+    ((StridedFn<T>)s->kx[MODE_FC])<<<s->lx.grid, s->lx.threads, s->lx.smem, st>>>(spec, s->sx, s->px, delta,
+                                                                                   tp<T>(s->d_fedits), H);
+    mark();
+    ((StridedFn<T>)s->kx[MODE_INV])<<<s->lx.grid, s->lx.threads, s->lx.smem, st>>>(spec, s->sx, s->px, delta,
+                                                                                    tp<T>(s->d_fedits), H);
+    mark();
+    if (s->has_y) {
+      ((StridedFn<T>)s->ky[MODE_INV])<<<s->ly.grid, s->ly.threads, s->ly.smem, st>>>(spec, s->sy, s->py, delta,
+                                                                                     tp<T>(s->d_fedits), H);
+      mark();
+    }
+  } else if (plain && s->fused == 1) {
+    ((StridedFn<T>)s->ky[MODE_FC])<<<s->ly.grid, s->ly.threads, s->ly.smem, st>>>(spec, s->sy, s->py, delta,
+                                                                                   tp<T>(s->d_fedits), H);
+    mark();
+    ((StridedFn<T>)s->ky[MODE_INV])<<<s->ly.grid, s->ly.threads, s->ly.smem, st>>>(spec, s->sy, s->py, delta,
+                                                                                    tp<T>(s->d_fedits), H);
+    mark();
+  } else if (s->fused == 2) {
     if (s->has_y) {
       ((StridedFn<T>)s->ky[MODE_FWD])<<<s->ly.grid, s->ly.threads, s->ly.smem, st>>>(spec, s->sy, s->py, delta,
                                                                                      tp<T>(s->d_fedits), H);
@@ -759,6 +802,7 @@ void free_all(ffcz_solver *s) {
     if (p) cudaFree(p);
   if (s->d_up_blk) cudaFree(s->d_up_blk);
   if (s->d_vmax) cudaFree(s->d_vmax);
+  if (s->d_cert) cudaFree(s->d_cert);
   if (s->verifier) {
     free_all(s->verifier);
     delete s->verifier;
@@ -859,14 +903,14 @@ int reconstruct(ffcz_solver *s, const void *d_decomp, const uint16_t *fq, size_t
 // R2C of x with the solver's forward passes into d_orig (padded layout), the
 // spectrum the pointwise modes compare against (impl:612-623).
 template <typename T>
-int forward_spectrum(ffcz_solver *s, bool keep_as_orig = true) {
+int forward_spectrum(ffcz_solver *s, bool keep_as_orig = true, const void *src = nullptr) {
   cudaStream_t st = s->stream;
   c2<T> *spec = (c2<T> *)s->d_spec;
   const c2<T> *post = post_table<T>(s);
   const ClampArgs<T> none;
   const long long H = (long long)s->H;
   ((ZfwdFn<T>)s->kzf[PRO_PLAIN])<<<s->lz_f.grid, s->lz_f.threads, s->lz_f.smem, st>>>(
-      (const T *)s->d_x, nullptr, tp<T>(s->d_sedits), (T)s->eps, spec, s->za, s->pz, post);
+      (const T *)(src ? src : s->d_x), nullptr, tp<T>(s->d_sedits), (T)s->eps, spec, s->za, s->pz, post);
   if (s->has_y)
     ((StridedFn<T>)s->ky[MODE_FWD])<<<s->ly.grid, s->ly.threads, s->ly.smem, st>>>(spec, s->sy, s->py, none,
                                                                                    tp<T>(s->d_fedits), H);
@@ -915,6 +959,63 @@ __global__ void k_spec_absmax(const double2 *__restrict__ spec, long long rows, 
   }
   for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_down_sync(0xffffffffu, m, o));
   if ((threadIdx.x & 31) == 0) atomic_max_abs(mx, m);
+}
+
+// The same over a spectrum in the solver's own precision.
+template <typename T>
+__global__ void k_spec_absmax_t(const c2<T> *__restrict__ spec, long long rows, int Hz, int Hzp,
+                                unsigned long long *__restrict__ mx) {
+  double m = 0.0;
+  const long long total = rows * Hz;
+  for (long long it = (long long)blockIdx.x * blockDim.x + threadIdx.x; it < total;
+       it += (long long)gridDim.x * blockDim.x) {
+    const long long r = it / Hz;
+    const c2<T> v = spec[r * Hzp + (it - r * Hz)];
+    m = fmax(m, fmax(fabs((double)v.x), fabs((double)v.y)));
+  }
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_down_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomic_max_abs(mx, m);
+}
+
+// Clamps e to [-eps, eps] (the clamp deltas go to the spatial edits, and a
+// warp that clamped marks the accumulator written), then per block the sum
+// of the squares of the result in FP64 (written to partial[block]: the host
+// adds them in block order, so the sum is reproducible) and max |e|.
+template <typename T>
+__global__ void __launch_bounds__(256) k_clamp_sumsq(T *__restrict__ e, T *__restrict__ sedits, T eps, long long n,
+                                                     unsigned *sdirty, double *__restrict__ partial,
+                                                     unsigned long long *__restrict__ mx) {
+  __shared__ double ws[8];
+  double acc = 0.0, m = 0.0;
+  bool hit = false;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    T v = e[i];
+    if (v > eps || v < -eps) {
+      v = spatial_clamp(v, eps, sedits, i);
+      e[i] = v;
+      hit = true;
+    }
+    const double d = (double)v;
+    acc = fma(d, d, acc);
+    m = fmax(m, fabs(d));
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    acc += __shfl_down_sync(0xffffffffu, acc, o);
+    m = fmax(m, __shfl_down_sync(0xffffffffu, m, o));
+  }
+  const bool any = __any_sync(0xffffffffu, hit);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) {
+    ws[warp] = acc;
+    atomic_max_abs(mx, m);
+    if (any) *sdirty = 1u;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += ws[w];
+    partial[blockIdx.x] = t;
+  }
 }
 
 // Times the default and the alternative tile of each compile-time pass on
@@ -1007,6 +1108,60 @@ int autotune(ffcz_solver *s, int reps, double *ms6) {
 
 }  // namespace
 
+// Certificate of both bounds from the solver's own transform.  The forward
+// transform's rounding error is bounded a posteriori: for a radix-2 FFT with
+// correctly rounded twiddles ||fl(Fe) - Fe||_2 <= log2(n) eta ||Fe||_2,
+// eta = u + gamma_4 (sqrt(2) + u) ~ 6.7 u (Higham, Accuracy and Stability of
+// Numerical Algorithms, 2nd ed., Thm 24.2), stage errors adding along a
+// transform's levels; no coefficient's error exceeds that 2-norm, and
+// ||Fe||_2 = sqrt(N) ||e||_2 (Parseval; the half spectrum is part of it).
+// The certificate takes
+//   B = 16 u L sqrt(N sum e_i^2),  L = sum over the axes of ceil(log2 n_a) + 2
+// (+2: the R2C split and the final rounding), 2.4 times the theorem's
+// constant to cover the radix-3/5/16 butterflies and the twiddle tables;
+// u = 2^-24 (FP32), 2^-53 (FP64), 2^-44 (float-float passes).  Both bounds
+// hold in exact arithmetic when max|e| <= E and max|Re/Im| + B <= Delta.
+// With clamp set, e is first clamped to [-eps_t, eps_t] (edits recorded).
+template <typename T>
+int certify(ffcz_solver *s, bool clamp, T eps_t, double *smax, double *fmax, double *bound, int *ok) {
+  cudaStream_t st = s->stream;
+  const unsigned g = (unsigned)std::min<size_t>(ceil_div(s->N, 256), 152 * 16);
+  if (!s->d_cert) FFCZ_CUDA(cudaMalloc(&s->d_cert, (152 * 16 + 2) * sizeof(double)));
+  double *partial = (double *)s->d_cert;
+  unsigned long long *mx = (unsigned long long *)(partial + 152 * 16);
+  FFCZ_CUDA(cudaMemsetAsync(mx, 0, 2 * sizeof(unsigned long long), st));
+  const T lim = clamp ? eps_t : std::numeric_limits<T>::infinity();
+  k_clamp_sumsq<T><<<g, 256, 0, st>>>(tp<T>(s->d_e), tp<T>(s->d_sedits), lim, (long long)s->N, s->d_sdirty, partial,
+                                      mx);
+  FFCZ_CUDA(cudaGetLastError());
+  FFCZ_TRY(forward_spectrum<T>(s, false, s->d_e));
+  const unsigned g2 = (unsigned)std::min<size_t>(ceil_div(s->H, 256), 152 * 16);
+  k_spec_absmax_t<T><<<g2, 256, 0, st>>>((const c2<T> *)s->d_spec, (long long)s->rows, s->Hz, s->Hzp, mx + 1);
+  FFCZ_CUDA(cudaGetLastError());
+  std::vector<double> h(g + 2);
+  FFCZ_CUDA(cudaMemcpyAsync(h.data(), partial, g * sizeof(double), cudaMemcpyDeviceToHost, st));
+  FFCZ_CUDA(cudaMemcpyAsync(h.data() + g, mx, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
+  FFCZ_CUDA(cudaStreamSynchronize(st));
+  double sumsq = 0.0;
+  for (unsigned i = 0; i < g; ++i) sumsq += h[i];
+  unsigned long long bits[2];
+  std::memcpy(bits, h.data() + g, sizeof(bits));
+  std::memcpy(smax, &bits[0], 8);
+  std::memcpy(fmax, &bits[1], 8);
+  auto clog2 = [](size_t n) {
+    int l = 0;
+    while (((size_t)1 << l) < n) ++l;
+    return l;
+  };
+  const int L = clog2(s->nx) + clog2(s->ny) + clog2(s->nz) + 2;
+  const double u = sizeof(T) == 4 ? 0x1p-24 : (s->split ? 0x1p-44 : 0x1p-53);
+  // the sum carries its own relative rounding of at most N u_64; 1.001 covers it
+  *bound = 16.0 * u * (double)L * std::sqrt((double)s->N * sumsq * 1.001);
+  const double fb = std::nextafter(*fmax + *bound, std::numeric_limits<double>::infinity());
+  *ok = (*smax <= s->eps && fb <= s->delta) ? 1 : 0;
+  return FFCZ_OK;
+}
+
 // Strict bounds after an all-abs solve (ffcz_strict_finish in ffcz.h):
 // clamp to the largest T <= eps, FP64 check, re-runs on a shrunk frequency
 // box while a coefficient exceeds delta.
@@ -1025,7 +1180,21 @@ int strict_finish(ffcz_solver *s, int max_iter, double tol, int max_rounds, int 
   const unsigned g = (unsigned)std::min<size_t>(ceil_div(s->N, 256), 152 * 16);
   int total = s->h_ctl->iterations, r = 0, rc = FFCZ_OK;
   double sm = 0.0, fm = 0.0, dt = D;
-  for (;;) {
+  // the clamp and the certificate in the solver's own precision decide
+  // unless a coefficient comes within the rounding bound of Delta
+  double cs = 0.0, cf = 0.0, cb = 0.0;
+  int cok = 0;
+  FFCZ_TRY(certify<T>(s, true, Et, &cs, &cf, &cb, &cok));
+  s->extracted = false;
+  s->cert_ok = cok;
+  s->cert_smax = cs;
+  s->cert_fmax = cf;
+  s->cert_bound = cb;
+  if (cok) {
+    sm = cs;
+    fm = std::nextafter(cf + cb, std::numeric_limits<double>::infinity());
+  }
+  for (; !cok;) {
     k_final_clamp<T><<<g, 256, 0, st>>>(tp<T>(s->d_e), tp<T>(s->d_sedits), Et, (long long)s->N, nullptr,
                                         s->d_sdirty);
     FFCZ_CUDA(cudaGetLastError());
@@ -1207,6 +1376,17 @@ int ffcz_solver_set_pack_mode(ffcz_solver *s, int mode) {
   return FFCZ_OK;
 }
 
+int ffcz_solver_set_form(ffcz_solver *s, int form) {
+  FFCZ_TRY(check_solver(s));
+  if (form != FFCZ_FORM_FUSED && form != FFCZ_FORM_PLAIN) return fail(FFCZ_ERR_INVALID, "unknown form");
+  if (form == FFCZ_FORM_PLAIN && ((s->fused == 2 && !s->kx[MODE_FC]) || (s->fused == 1 && !s->ky[MODE_FC])))
+    return fail(FFCZ_ERR_UNSUPPORTED, "no forward-with-clamp kernel for this shape and precision");
+  if (form != s->form)
+    for (LoopGraph &g : s->lg) g.reset();
+  s->form = form;
+  return FFCZ_OK;
+}
+
 static double round_t(const ffcz_solver *s, double v) { return s->dtype == FFCZ_F32 ? (double)(float)v : v; }
 
 // Copies x and stores eps rounded to the solver type (the reference's T
@@ -1373,6 +1553,22 @@ int ffcz_reset_edit_accumulators(ffcz_solver *s) {
   FFCZ_TRY(check_solver(s));
   FFCZ_TRY(clear_accumulators(s, s->stream));
   FFCZ_CUDA(cudaStreamSynchronize(s->stream));
+  return FFCZ_OK;
+}
+
+int ffcz_set_edit_accumulators(ffcz_solver *s, const void *h_freq_edits, const void *h_spatial_edits) {
+  FFCZ_TRY(check_solver(s));
+  static const unsigned one = 1u;
+  if (h_freq_edits) {
+    FFCZ_CUDA(cudaMemcpyAsync(s->d_fedits, h_freq_edits, 2 * s->H * s->es, cudaMemcpyHostToDevice, s->stream));
+    FFCZ_CUDA(cudaMemcpyAsync(s->d_fdirty, &one, sizeof(unsigned), cudaMemcpyHostToDevice, s->stream));
+  }
+  if (h_spatial_edits) {
+    FFCZ_CUDA(cudaMemcpyAsync(s->d_sedits, h_spatial_edits, s->N * s->es, cudaMemcpyHostToDevice, s->stream));
+    FFCZ_CUDA(cudaMemcpyAsync(s->d_sdirty, &one, sizeof(unsigned), cudaMemcpyHostToDevice, s->stream));
+  }
+  FFCZ_CUDA(cudaStreamSynchronize(s->stream));
+  s->extracted = false;
   return FFCZ_OK;
 }
 
@@ -1576,6 +1772,25 @@ int ffcz_strict_finish(ffcz_solver *s, int max_iter, double tol, int max_rounds,
                        double *spatial_max, double *freq_max) {
   FFCZ_TRY(check_solver(s));
   return DISPATCH(s, strict_finish, s, max_iter, tol, max_rounds, rounds, met, spatial_max, freq_max);
+}
+
+int ffcz_certify_bounds(ffcz_solver *s, double *spatial_max, double *freq_max, double *bound, int *certified) {
+  FFCZ_TRY(check_solver(s));
+  if (!spatial_max || !freq_max || !bound || !certified) return fail(FFCZ_ERR_INVALID, "NULL argument");
+  if (!s->initialized) return fail(FFCZ_ERR_NOT_INITIALIZED, "Solver not initialized");
+  Range r("ffcz:certify_bounds");
+  s->extracted = false;  // the certificate's transform uses the spectrum buffer
+  return s->dtype == FFCZ_F32 ? certify<float>(s, false, 0.0f, spatial_max, freq_max, bound, certified)
+                              : certify<double>(s, false, 0.0, spatial_max, freq_max, bound, certified);
+}
+
+int ffcz_get_strict_report(ffcz_solver *s, int *certified, double *freq_max, double *bound) {
+  FFCZ_TRY(check_solver(s));
+  if (!certified || !freq_max || !bound) return fail(FFCZ_ERR_INVALID, "NULL argument");
+  *certified = s->cert_ok;
+  *freq_max = s->cert_fmax;
+  *bound = s->cert_bound;
+  return FFCZ_OK;
 }
 
 int ffcz_get_orig_spectrum(ffcz_solver *s, void *h_dst, size_t cap_complex) {

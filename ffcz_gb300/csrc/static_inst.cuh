@@ -92,6 +92,17 @@ bool strided_for_family(int mode, StridedFn<T> &fn, StaticGeom &g) {
   g.smem = (size_t)sl_size(L, C::TW, sizeof(T)) * sizeof(c2<T>);
   return set_smem(fn, g.smem) == FFCZ_OK;
 }
+template <typename T, int L, int VAR>
+bool strided_fc_for(StridedFn<T> &fn, StaticGeom &g) {
+  constexpr int CAP = plain_cap(L);
+  using C = Cfg<T, L, CAP, VAR>;
+  if (VAR && C::TW == Cfg<T, L, CAP, 0>::TW) return false;
+  fn = ks_strided<T, MODE_FC, L, C::LGTW, CAP, false>;
+  g.TW = C::TW;
+  g.threads = C::NT;
+  g.smem = (size_t)sl_size(L, C::TW, sizeof(T)) * sizeof(c2<T>);
+  return set_smem(fn, g.smem) == FFCZ_OK;
+}
 template <typename T, int L, int VAR, bool SPLIT = false>
 bool strided_for(int mode, StridedFn<T> &fn, StaticGeom &g) {
   return (mode == MODE_FWD || mode == MODE_INV) ? strided_for_family<T, L, VAR, false, SPLIT>(mode, fn, g)
@@ -136,6 +147,16 @@ template <typename T> bool split_strided(int L, int mode, StridedFn<T> &fn, Stat
       default: return false;                                                      \
     }                                                                             \
   }
+
+#define DEFINE_FC_LOOKUP(T, CASES)                                                \
+  template <>                                                                     \
+  bool static_strided_fc<T>(int L, StridedFn<T> &fn, StaticGeom &g, int var) {    \
+    switch (L) {                                                                  \
+      CASES(SFC)                                                                  \
+      default: return false;                                                      \
+    }                                                                             \
+  }
+#define SFC(n) case n: return var ? strided_fc_for<TT, n, 1>(fn, g) : strided_fc_for<TT, n, 0>(fn, g);
 
 #define ZF(n) case n: return var ? zfwd_for<TT, n, 1>(pro, fn, g) : zfwd_for<TT, n, 0>(pro, fn, g);
 #define ZI(n) case n: return var ? zinv_for<TT, n, 1>(fn, g) : zinv_for<TT, n, 0>(fn, g);

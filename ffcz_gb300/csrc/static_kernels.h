@@ -43,5 +43,9 @@ template <typename T> bool static_zfwd(int M, int pro, ZfwdFn<T> &fn, StaticGeom
 template <typename T> bool static_zinv(int M, ZinvFn<T> &fn, StaticGeom &g, int var = 0, int split = 0);
 template <typename T>
 bool static_strided(int L, int mode, StridedFn<T> &fn, StaticGeom &g, int var = 0, int split = 0);
+// The plain form's forward pass with the all-abs clamp in its epilogue
+// (MODE_FC): the plain stage-list family and tile of MODE_FWD, so it shares
+// that pass's geometry.  No float-float variant.
+template <typename T> bool static_strided_fc(int L, StridedFn<T> &fn, StaticGeom &g, int var = 0);
 
 }  // namespace ffcz

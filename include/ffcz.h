@@ -87,6 +87,21 @@ int ffcz_solver_set_stream(ffcz_solver *s, void *stream);
 int ffcz_solver_set_loop_driver(ffcz_solver *s, int driver);
 /* FFCZ_PACK_CORRECT (default) or FFCZ_PACK_REFERENCE. */
 int ffcz_solver_set_pack_mode(ffcz_solver *s, int mode);
+/* Iteration form of the all-abs loop (no counterpart in the reference,
+ * whose iteration is cuFFT R2C + clamp kernel + cuFFT C2R + normalise,
+ * projection_algorithm_impl.cuh:201-249):
+ *   FFCZ_FORM_FUSED (default): five HBM passes per 3D iteration -- z R2C
+ *     (spatial-clamp prologue), y forward, x forward + frequency clamp + x
+ *     inverse in one pass, y inverse, z C2R (normalisation, violation);
+ *   FFCZ_FORM_PLAIN: six -- the x forward pass stores the clamped spectrum
+ *     and the x inverse is a pass of its own (2D: the same on y).
+ * Both compute the reference's iteration; results agree to FP32 rounding
+ * (the passes' stage lists differ).  Other constraint modes always run the
+ * fused form.  FFCZ_ERR_UNSUPPORTED where no forward-with-clamp kernel
+ * exists (float-float FP64 passes). */
+#define FFCZ_FORM_FUSED 0
+#define FFCZ_FORM_PLAIN 1
+int ffcz_solver_set_form(ffcz_solver *s, int form);
 
 /* initialize_all_abs(h_orig, eps, delta) -- impl:639-668.  x is a host
  * array of Nx*Ny*Nz elements of the solver's dtype; eps and delta are
@@ -159,6 +174,15 @@ int ffcz_extract(ffcz_solver *s);
  * zeros afterwards; one nothing has written since its last clear is not
  * rewritten. */
 int ffcz_reset_edit_accumulators(ffcz_solver *s);
+/* Loads host arrays into the edit accumulators (2H planar frequency edits,
+ * N spatial edits; either may be NULL to keep that accumulator), so that
+ * ffcz_extract / ffcz_solver_encode compact and code edits produced
+ * elsewhere.  The reference keeps its accumulators private
+ * (projection_algorithm.cuh:77-78); this stands in for a caller writing
+ * results_.d_freq_edits / d_spatial_edits before
+ * extract_compact_representation (impl:371-456). */
+int ffcz_set_edit_accumulators(ffcz_solver *s, const void *h_freq_edits,
+                               const void *h_spatial_edits);
 /* Waits for the solver's stream. */
 int ffcz_solver_synchronize(ffcz_solver *s);
 
@@ -237,7 +261,10 @@ int ffcz_verify_bounds(ffcz_solver *s, double *spatial_max, double *freq_max);
  * and meets delta only up to the FFT's rounding).  After an all-abs solve:
  *   1. e is clamped to E_T, the largest value of the solver's type <= eps
  *      (clamps recorded in the spatial edits);
- *   2. both bounds are checked in FP64 (ffcz_verify_bounds);
+ *   2. the certificate of ffcz_certify_bounds (the solver's own transform
+ *      and a bound on its rounding) decides both bounds unless a
+ *      coefficient comes within that bound of delta; then both bounds are
+ *      checked in FP64 (ffcz_verify_bounds);
  *   3. while some |Re/Im F(e)_k| > delta, the loop runs again from the
  *      current e (max_iter, tol) on a frequency box shrunk by twice the worst
  *      overshoot (frequency edits accumulate as usual), then 1-2 again; at
@@ -248,6 +275,20 @@ int ffcz_verify_bounds(ffcz_solver *s, double *spatial_max, double *freq_max);
  * to its type at initialisation).  Any out pointer may be NULL. */
 int ffcz_strict_finish(ffcz_solver *s, int max_iter, double tol, int max_rounds, int *rounds, int *met,
                        double *spatial_max, double *freq_max);
+/* Certificate of both bounds without an FP64 transform (an addition): the
+ * forward transform of e in the solver's own precision, max |Re/Im| over
+ * the half spectrum (freq_max), and an a-posteriori bound on that
+ * transform's rounding error (bound = 16 u L sqrt(N sum e_i^2), L = sum of
+ * ceil(log2 n) over the axes + 2, u the unit roundoff of the passes; from
+ * the FFT error analysis of Higham, Accuracy and Stability of Numerical
+ * Algorithms, Thm 24.2, with 2.4x its constant).  *certified = 1 when
+ * spatial_max <= eps and freq_max + bound <= delta: then both bounds hold
+ * in exact arithmetic.  e and the accumulators are not changed; the
+ * spectrum buffer is (a later ffcz_extract recomputes the compaction). */
+int ffcz_certify_bounds(ffcz_solver *s, double *spatial_max, double *freq_max, double *bound, int *certified);
+/* How the last ffcz_strict_finish decided: *certified = 1 when the
+ * certificate did (no FP64 transform ran), with its freq_max and bound. */
+int ffcz_get_strict_report(ffcz_solver *s, int *certified, double *freq_max, double *bound);
 /* The spectrum of x of the pointwise modes (d_orig_freq, impl:612-623):
  * H interleaved complex values of the solver's dtype. */
 int ffcz_get_orig_spectrum(ffcz_solver *s, void *h_dst, size_t cap_complex);
@@ -477,17 +518,22 @@ int ffcz_container_read(const char *path, ffcz_container_header *h,
  * implicit device synchronisation of cudaMalloc/cudaFree.  It calls no
  * allocator; its scratch is a fixed FFCZ_NOALLOC_SCRATCH_BYTES device array
  * inside the library, held by every GPU that loads it until process exit.
- *   d_edits   : n values of dtype (FFCZ_F32 / FFCZ_F64), device memory;
+ *   d_edits   : n values of dtype (FFCZ_F32 / FFCZ_F64), device memory,
+ *               16-byte aligned (read with 16-byte vector loads);
  *               n <= FFCZ_NOALLOC_MAX_ELEMS, else FFCZ_ERR_CAPACITY.
- *   d_compact : room for n values of dtype; receives the active values.
- *   d_quant   : room for n uint16; receives their codes.
+ *   d_compact : room for n values of dtype, aligned to the element size;
+ *               receives the active values.
+ *   d_quant   : room for n uint16, 2-byte aligned; receives their codes.
  *   d_pack    : 4-byte aligned, room for 4*ceil(n/32) bytes; receives the
  *               flag pack (FFCZ_PACK_CORRECT or FFCZ_PACK_REFERENCE).
  *   count, min_edit, max_edit : host outputs (min/max may be NULL).
- * The call runs on `stream` and returns after it finished.  The first call
- * on a device (with that device current) resolves the scratch array's
- * device address; make it before any stream capture.  All calls on a device
- * share the scratch, so calls that overlap on the GPU race. */
+ * A misaligned pointer returns FFCZ_ERR_INVALID before anything runs.
+ * The call runs on `stream` and returns after it finished.  Every call
+ * resolves the scratch array's device address on the current device (so
+ * it stays right after cudaDeviceReset); the first call on a device may
+ * load the library's device code, so make it before any stream capture.
+ * All calls on a device share the scratch, so calls that overlap on the
+ * GPU race. */
 #define FFCZ_NOALLOC_MAX_ELEMS 67108864u      /* 16384 blocks of 4096 values */
 #define FFCZ_NOALLOC_SCRATCH_BYTES 328192u
 int ffcz_compact_quantize_noalloc(const void *d_edits, size_t n, int dtype,

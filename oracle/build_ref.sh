@@ -1,11 +1,15 @@
 #!/bin/sh
-# Builds oracle/_ref/ref_harness from the reference sources where they lie
-# (FFCZ_REF, default /root/reference): HuffmanZSTDCoder.cuh with thrust on
-# its CPP backend (host only, no GPU) and fileIO.cpp, against the system
+# Builds oracle/_ref/ref_harness from the reference sources in the
+# directory FFCZ_REF names: HuffmanZSTDCoder.cuh with thrust on its CPP
+# backend (host only, no GPU) and fileIO.cpp, against the system
 # libzstd.so.1.  Test infrastructure; outputs go to oracle/_ref/ only.
 set -e
+if [ -z "$FFCZ_REF" ]; then
+  echo "FFCZ_REF is not set: give the directory holding the reference sources" >&2
+  exit 2
+fi
 HERE=$(cd "$(dirname "$0")" && pwd)
-REF=${FFCZ_REF:-/root/reference}
+REF=$FFCZ_REF
 NVCC=${NVCC:-/usr/local/cuda/bin/nvcc}
 ZLIB=$(ls /usr/lib/*-linux-gnu/libzstd.so.1 2>/dev/null | head -1)
 mkdir -p "$HERE/_ref"

@@ -21,10 +21,12 @@ The product never imports this module.
 * ``check_bounds`` is the FP64 check of both bounds.
 
 Pinning: the Huffman codebook and decoder are checked against the
-reference's own functions (tests/golden, generated by oracle/ref_harness.cu
-compiled from the reference sources).  The projection loop has no reference
-golden vectors (the reference ships none and its cuFFT build needs a GPU):
-its FFT is pinned by known-answer transforms and by numpy.fft.
+reference's own functions (tests/golden/huffman_reference.npz, generated by
+oracle/ref_harness.cu compiled from the reference sources); the projection
+loop, the compaction, the quantiser, the flag packs and the coder are
+checked against the reference's own cuFFT build run on a GPU
+(tests/golden/ref_*.npz, generated by oracle/ref_solver.cu).  The
+reference ships no golden vectors of its own.
 """
 from __future__ import annotations
 
@@ -53,6 +55,16 @@ except ImportError:  # pragma: no cover
 HERE = Path(__file__).resolve().parent
 LIB = HERE / "_build" / "liboracle.so"
 THRESHOLD = 1e-7  # projection_algorithm_impl.cuh:389, 398
+
+
+def reference_sources() -> Path | None:
+    """The directory holding the reference sources: FFCZ_REF when set, else
+    the repository's git-ignored copy baseline/_ref when present, else None."""
+    env = os.environ.get("FFCZ_REF")
+    if env:
+        return Path(env)
+    local = HERE.parent / "baseline" / "_ref"
+    return local if (local / "projection_algorithm.cuh").exists() else None
 
 
 def build() -> Path:

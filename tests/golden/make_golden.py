@@ -1,6 +1,6 @@
 """Generates the golden fixtures in tests/golden/ from the reference itself.
 
-Needs the reference sources (FFCZ_REF, default /root/reference) and nvcc:
+Needs the reference sources (FFCZ_REF: the directory holding them) and nvcc:
 oracle/build_ref.sh compiles the reference's Huffman host code
 (HuffmanZSTDCoder.cuh:48-178, 378-450, thrust on its CPP backend) and
 fileIO.cpp into oracle/_ref/ref_harness.  For each symbol stream below the

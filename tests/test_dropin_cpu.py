@@ -3,7 +3,6 @@
 includes resolve to include/) builds against include/ and links libffcz.so
 with no change.  Needs nvcc and the reference sources; skipped without
 them.  Also: argument errors of our fftz CLI print the reference's usage."""
-import os
 import shutil
 import subprocess
 from pathlib import Path
@@ -11,14 +10,15 @@ from pathlib import Path
 import pytest
 
 import ffcz_gb300 as F
+from oracle import ffcz_oracle as O
 
 ROOT = Path(__file__).resolve().parents[1]
-REF = Path(os.environ.get("FFCZ_REF", "/root/reference"))
+REF = O.reference_sources() or Path("/nonexistent")
 NVCC = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
 
 
 @pytest.mark.skipif(not (REF / "projection_example.cu").exists() or not Path(NVCC).exists(),
-                    reason="reference sources or nvcc not available")
+                    reason="reference sources (FFCZ_REF or baseline/_ref) or nvcc not available")
 def test_reference_cli_builds_against_dropin_headers(tmp_path):
     src = tmp_path / "projection_example.cu"
     shutil.copy(REF / "projection_example.cu", src)

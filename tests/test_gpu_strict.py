@@ -40,7 +40,10 @@ def test_strict_finish_meets_both_bounds_in_fp64(cuda, shape, dtype, c):
         assert st["met"], (st, chk)
         assert chk["spatial_max"] <= E and chk["freq_max"] <= D
         assert st["spatial_max"] == chk["spatial_max"]
-        assert abs(st["freq_max"] - chk["freq_max"]) <= 1e-12 * D
+        if st["certified"]:  # the certificate's value bounds the FP64 one
+            assert chk["freq_max"] <= st["freq_max"] <= D
+        else:
+            assert abs(st["freq_max"] - chk["freq_max"]) <= 1e-12 * D
         if before["spatial_excess"] <= 0 and before["freq_excess"] <= 0:
             assert st["rounds"] == 0
         if before["freq_excess"] > 0:

@@ -85,3 +85,61 @@ def test_noalloc_rejects_oversized_input(cuda):
                                                None, C.byref(count), None, None)
     assert rc == -6
     assert "exceeds the fixed scratch limit" in F.lib().ffcz_last_error().decode()
+
+
+def test_noalloc_rejects_misaligned_edits(cuda):
+    """An edit pointer off a 16-byte boundary (an offset sub-array) is
+    rejected on the host: the kernels read it with 16-byte vector loads."""
+    torch = cuda
+    buf = torch.zeros(256, dtype=torch.float32, device="cuda")
+    out = torch.empty(256, dtype=torch.float32, device="cuda")
+    quant = torch.empty(256, dtype=torch.int16, device="cuda")
+    pack = torch.empty(64, dtype=torch.uint8, device="cuda")
+    count = C.c_size_t(12345)
+    rc = F.lib().ffcz_compact_quantize_noalloc(
+        C.c_void_p(buf.data_ptr() + 4), 200, F.FFCZ_F32, C.c_void_p(out.data_ptr()), C.c_void_p(quant.data_ptr()),
+        C.c_void_p(pack.data_ptr()), F.FFCZ_PACK_CORRECT, None, C.byref(count), None, None)
+    assert rc == F.FFCZ_ERR_INVALID
+    assert "16-byte aligned" in F.lib().ffcz_last_error().decode()
+    assert count.value == 12345  # nothing ran
+
+
+@pytest.mark.parametrize("pack_mode", [F.FFCZ_PACK_CORRECT, F.FFCZ_PACK_REFERENCE])
+def test_noalloc_large_sparse_against_oracle(cuda, pack_mode):
+    """More than 1024 chunks of 4096 values, so the one-block scan carries
+    its running offset across rounds; compared with the C restatement of
+    the reference's compaction (projection_algorithm.cu:365-550)."""
+    from oracle import ffcz_oracle as O
+
+    torch = cuda
+    n = 6_000_001
+    rng = np.random.default_rng(77)
+    a = np.zeros(n, np.float32)
+    idx = rng.choice(n, 450_000, replace=False)
+    a[idx] = (rng.standard_normal(idx.size) * 1e-3).astype(np.float32)
+    a[rng.choice(n, 5_000, replace=False)] = np.float32(5e-8)  # below the activity threshold
+    d = torch.from_numpy(a).cuda()
+    stream = torch.cuda.current_stream().cuda_stream
+    got = _noalloc(torch, d.data_ptr(), n, np.float32, pack_mode, stream)
+    ex = O.extract(a, pack_mode)
+    assert got["count"] == ex["count"]
+    assert got["min"] == ex["min"] and got["max"] == ex["max"]
+    assert np.array_equal(got["compact"], ex["compact"])
+    assert np.array_equal(got["quant"], ex["quant"])
+    assert np.array_equal(got["pack"], ex["pack"])
+
+
+def test_noalloc_all_below_threshold_reference_pack(cuda):
+    """No active value: count 0, min/max still over the whole array, and the
+    reference pack mode leaves the pack zero (pack_bools is not launched
+    for an empty stream, projection_algorithm_impl.cuh:429-449)."""
+    torch = cuda
+    n = 50_000
+    a = np.zeros(n, np.float64)
+    a[::7] = 9e-8
+    a[3::11] = -4e-8
+    d = torch.from_numpy(a).cuda()
+    got = _noalloc(torch, d.data_ptr(), n, np.float64, F.FFCZ_PACK_REFERENCE, torch.cuda.current_stream().cuda_stream)
+    assert got["count"] == 0
+    assert got["min"] == -4e-8 and got["max"] == 9e-8
+    assert not got["pack"].any()
