@@ -73,7 +73,7 @@ TRAFFIC = {"plain256": {"zfwd_r2c": 169.0e6, "y_fwd": 89.3e6, "x_fwd_clamp_inv":
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="precision512")
@@ -132,7 +132,7 @@ class Clocks:
         dev = os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0] or "0"
         try:
             self.p = subprocess.Popen(["nvidia-smi", f"--id={dev}", f"--query-gpu={q}", "--format=csv,noheader,nounits",
-                                       "-lms", "100"], stdout=self.f, stderr=subprocess.DEVNULL)
+                                       "-lms", "50"], stdout=self.f, stderr=subprocess.DEVNULL)
         except Exception:
             self.p = None
 

@@ -86,6 +86,8 @@ SIGNATURES = {
     "ffcz_extract": [_p],
     "ffcz_reset_edit_accumulators": [_p],
     "ffcz_set_edit_accumulators": [_p, _p, _p],
+    "ffcz_huff_histogram_device": [_p, _sz, _i, _p, _p],
+    "ffcz_huff_tree": [_p, _sz, _p, _p, _p, _p],
     "ffcz_solver_synchronize": [_p],
     "ffcz_get_iterations": [_p, C.POINTER(C.c_int)],
     "ffcz_get_convergence": [_p, C.POINTER(C.c_double)],
@@ -330,7 +332,9 @@ class ProjectionSolver:
         c, f, bd = C.c_int(), C.c_double(), C.c_double()
         _check(lib().ffcz_get_strict_report(self._h, C.byref(c), C.byref(f), C.byref(bd)))
         return {"rounds": r.value, "met": bool(m.value), "spatial_max": a.value, "freq_max": b.value,
-                "certified": bool(c.value), "cert_freq_max": f.value, "cert_bound": bd.value}
+                "certified": bool(c.value),
+                "certified_by": {0: None, 1: "transform", 2: "recorded clamp maximum"}[c.value],
+                "cert_freq_max": f.value, "cert_bound": bd.value}
 
     def certify_bounds(self) -> dict:
         """Certificate of both bounds from the solver's own transform of e and

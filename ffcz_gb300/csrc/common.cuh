@@ -237,6 +237,10 @@ struct LoopCtl {
   unsigned long long total_bits; // Huffman bitstream length
   int err;                       // device-side error word (0 = none)
   int pad2;
+  // max over the spectrum of max(|Re|, |Im|) after the all-abs frequency
+  // clamp, as the bits of an FP32 value rounded up: of the running
+  // iteration, and of the last finished one
+  unsigned fmax_cur, fmax_last;
 };
 
 template <typename T> __device__ __forceinline__ unsigned long long to_bits(T v);

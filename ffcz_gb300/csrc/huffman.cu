@@ -256,14 +256,9 @@ static int ws_prepare(HuffWorkspace &ws) {
   return FFCZ_OK;
 }
 
-int huff_encode_device(HuffWorkspace &ws, const void *d_data, size_t n, int symbol_bytes,
-                       cudaStream_t stream, ffcz_huff_result &res) {
-  if (n == 0) return fail(FFCZ_ERR_EMPTY, "Empty data");
-  if (symbol_bytes != 1 && symbol_bytes != 2) return fail(FFCZ_ERR_INVALID, "symbol_bytes must be 1 or 2");
-  if (((uintptr_t)d_data) & 15) return fail(FFCZ_ERR_INVALID, "device symbols must be 16-byte aligned");
-  FFCZ_TRY(ws_prepare(ws));
+// Dense histogram of n symbols (256 or 65536 bins) into ws.d_hist.
+static int launch_histogram(HuffWorkspace &ws, const void *d_data, size_t n, int symbol_bytes, cudaStream_t stream) {
   const size_t nbins = symbol_bytes == 1 ? 256 : 65536;
-  ws.launches = 0;
   FFCZ_CUDA(cudaMemsetAsync(ws.d_hist, 0, nbins * sizeof(unsigned), stream));
   if (symbol_bytes == 1) {
     const int grid = (int)std::min<size_t>(ceil_div(n, 256 * 16), 1024);
@@ -278,6 +273,18 @@ int huff_encode_device(HuffWorkspace &ws, const void *d_data, size_t n, int symb
   }
   ws.launches++;
   FFCZ_CUDA(cudaGetLastError());
+  return FFCZ_OK;
+}
+
+int huff_encode_device(HuffWorkspace &ws, const void *d_data, size_t n, int symbol_bytes,
+                       cudaStream_t stream, ffcz_huff_result &res) {
+  if (n == 0) return fail(FFCZ_ERR_EMPTY, "Empty data");
+  if (symbol_bytes != 1 && symbol_bytes != 2) return fail(FFCZ_ERR_INVALID, "symbol_bytes must be 1 or 2");
+  if (((uintptr_t)d_data) & 15) return fail(FFCZ_ERR_INVALID, "device symbols must be 16-byte aligned");
+  FFCZ_TRY(ws_prepare(ws));
+  const size_t nbins = symbol_bytes == 1 ? 256 : 65536;
+  ws.launches = 0;
+  FFCZ_TRY(launch_histogram(ws, d_data, n, symbol_bytes, stream));
   FFCZ_CUDA(cudaMemcpyAsync(ws.h_hist, ws.d_hist, nbins * sizeof(unsigned), cudaMemcpyDeviceToHost, stream));
   FFCZ_CUDA(cudaStreamSynchronize(stream));
 
@@ -413,6 +420,54 @@ int ffcz_huff_compress_device(const void *d_data, size_t n, int symbol_bytes, in
   return global_encode(d_data, n, symbol_bytes, false, zstd_level, zstd_mode, (cudaStream_t)stream, out);
 }
 void ffcz_huff_result_free(ffcz_huff_result *r) { delete r; }
+
+int ffcz_huff_histogram_device(const void *d_data, size_t n, int symbol_bytes, void *stream, uint32_t *h_hist) {
+  if (!d_data || !h_hist) return fail(FFCZ_ERR_INVALID, "NULL argument");
+  if (symbol_bytes != 1 && symbol_bytes != 2) return fail(FFCZ_ERR_INVALID, "symbol_bytes must be 1 or 2");
+  if (((uintptr_t)d_data) & 15) return fail(FFCZ_ERR_INVALID, "device symbols must be 16-byte aligned");
+  const size_t nbins = symbol_bytes == 1 ? 256 : 65536;
+  if (n == 0) {
+    std::memset(h_hist, 0, nbins * sizeof(uint32_t));
+    return FFCZ_OK;
+  }
+  int dev = 0;
+  FFCZ_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return fail(FFCZ_ERR_INVALID, "device index out of range");
+  std::lock_guard<std::mutex> lk(g_ws_mu);
+  if (!g_ws[dev]) {
+    g_ws[dev] = new HuffWorkspace();
+    FFCZ_CUDA(cudaStreamCreateWithFlags(&g_stream[dev], cudaStreamNonBlocking));
+  }
+  HuffWorkspace &ws = *g_ws[dev];
+  FFCZ_TRY(ws_prepare(ws));
+  cudaStream_t st = (cudaStream_t)stream;
+  FFCZ_TRY(launch_histogram(ws, d_data, n, symbol_bytes, st));
+  FFCZ_CUDA(cudaMemcpyAsync(ws.h_hist, ws.d_hist, nbins * sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+  FFCZ_CUDA(cudaStreamSynchronize(st));
+  std::memcpy(h_hist, ws.h_hist, nbins * sizeof(uint32_t));
+  return FFCZ_OK;
+}
+
+int ffcz_huff_tree(const uint32_t *freqs, size_t n, int32_t *left, int32_t *right, uint64_t *weights,
+                   int32_t *root) {
+  if (!root || (n && (!freqs || !left || !right || !weights))) return fail(FFCZ_ERR_INVALID, "NULL argument");
+  if (n > (size_t)1 << 30) return fail(FFCZ_ERR_INVALID, "too many symbols");
+  if (n == 0) {
+    *root = -1;
+    return FFCZ_OK;
+  }
+  std::vector<int> l, r;
+  std::vector<uint64_t> w;
+  build_tree(freqs, (int)n, l, r, w);
+  const size_t nodes = 2 * n - 1;
+  for (size_t i = 0; i < nodes; ++i) {
+    left[i] = l[i];
+    right[i] = r[i];
+    weights[i] = w[i];
+  }
+  *root = (int32_t)(nodes - 1);
+  return FFCZ_OK;
+}
 
 size_t ffcz_zstd_bound(size_t n) { return zstd_bound(n); }
 

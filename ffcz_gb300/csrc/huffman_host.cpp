@@ -35,20 +35,49 @@ void build_codebook(const uint32_t *hist, size_t nbins, Codebook &cb) {
     cb.max_len = 1;
     return;
   }
+  std::vector<int> left, right;
+  std::vector<uint64_t> wt;
+  build_tree(cb.freq.data(), n, left, right, wt);
+  const int root = 2 * n - 2;
+  // Iterative depth-first walk from the root.
+  struct Item { int node; uint32_t code; int len; };
+  std::vector<Item> stack;
+  stack.push_back({root, 0u, 0});
+  while (!stack.empty()) {
+    const Item it = stack.back();
+    stack.pop_back();
+    if (left[it.node] < 0 && right[it.node] < 0) {
+      cb.code[it.node] = it.code;
+      cb.len[it.node] = it.len ? it.len : 1;
+      cb.max_len = std::max(cb.max_len, cb.len[it.node]);
+      continue;
+    }
+    if (right[it.node] >= 0) stack.push_back({right[it.node], (it.code << 1) | 1u, it.len + 1});
+    if (left[it.node] >= 0) stack.push_back({left[it.node], it.code << 1, it.len + 1});
+  }
+}
+
+void build_tree(const uint32_t *freq, int n, std::vector<int> &left, std::vector<int> &right,
+                std::vector<uint64_t> &wt) {
   // Nodes: leaves 0..n-1, internal n..2n-2.  The reference pops the two
   // smallest (freq, node index) keys of a min-heap.  The same sequence comes
   // from two queues: the leaves sorted by (freq, index), and the internal
   // nodes in creation order, whose keys are already sorted (merged weights
   // never decrease and indices grow); the smaller head is the heap's top.
-  std::vector<int> left(2 * n - 1, -1), right(2 * n - 1, -1);
-  std::vector<uint64_t> wt(2 * n - 1, 0);
+  left.assign(std::max(2 * n - 1, 1), -1);
+  right.assign(std::max(2 * n - 1, 1), -1);
+  wt.assign(std::max(2 * n - 1, 1), 0);
+  if (n <= 1) {
+    if (n == 1) wt[0] = freq[0];
+    return;
+  }
   // (freq, index) packed so that it sorts as the pair; LSD radix sort in
   // 16-bit digits over the bits in use
   std::vector<uint64_t> key(n), tmp(n);
   uint64_t all = 0;
   for (int i = 0; i < n; ++i) {
-    wt[i] = cb.freq[i];
-    key[i] = ((uint64_t)cb.freq[i] << 32) | (uint32_t)i;
+    wt[i] = freq[i];
+    key[i] = ((uint64_t)freq[i] << 32) | (uint32_t)i;
     all |= key[i];
   }
   std::vector<uint32_t> count(1u << 16);
@@ -81,23 +110,6 @@ void build_codebook(const uint32_t *hist, size_t nbins, Codebook &cb) {
     right[next] = b;
     wt[next] = wt[a] + wt[b];
     ++next;
-  }
-  const int root = 2 * n - 2;
-  // Iterative depth-first walk from the root.
-  struct Item { int node; uint32_t code; int len; };
-  std::vector<Item> stack;
-  stack.push_back({root, 0u, 0});
-  while (!stack.empty()) {
-    const Item it = stack.back();
-    stack.pop_back();
-    if (left[it.node] < 0 && right[it.node] < 0) {
-      cb.code[it.node] = it.code;
-      cb.len[it.node] = it.len ? it.len : 1;
-      cb.max_len = std::max(cb.max_len, cb.len[it.node]);
-      continue;
-    }
-    if (right[it.node] >= 0) stack.push_back({right[it.node], (it.code << 1) | 1u, it.len + 1});
-    if (left[it.node] >= 0) stack.push_back({left[it.node], it.code << 1, it.len + 1});
   }
 }
 

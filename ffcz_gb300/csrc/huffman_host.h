@@ -32,6 +32,12 @@ struct Codebook {
 // the root MSB-first in 32-bit words (longer codes keep their low 32 bits,
 // as the reference's uint32 shift does); one symbol gets code 0, length 1.
 void build_codebook(const uint32_t *hist, size_t nbins, Codebook &cb);
+// The tree of that codebook in the reference's node numbering
+// (HuffmanZSTDCoder.cuh:85-152): leaves 0..n-1 with weights freq[0..n-1],
+// internal nodes n..2n-2 in merge order, left = the first of the two
+// popped nodes, -1 for no child; the root is 2n-2 (0 for one leaf).
+void build_tree(const uint32_t *freq, int n, std::vector<int> &left, std::vector<int> &right,
+                std::vector<uint64_t> &wt);
 
 // Prefix decode of HuffmanZSTDCoder.cuh:394-449 over `bits` bytes: stops at
 // num_elements symbols or at the end of the stream; where no code of length

@@ -97,6 +97,16 @@ __device__ __forceinline__ void mark_dirty(unsigned *dirty, bool hit) {
   if (hit && dirty && (int)(threadIdx.x & 31) == __ffs(m) - 1 && *dirty == 0u) *dirty = 1u;
 }
 
+// Publishes the active lanes' max(|Re|, |Im|) once per warp: the FP32 bits
+// of a non-negative value order like the value, so one warp reduction and
+// one atomicMax of the first active lane.  m is rounded up to FP32.
+__device__ __forceinline__ void record_fmax(unsigned *dst, float m) {
+  const unsigned act = __activemask();
+  const unsigned b = __reduce_max_sync(act, __float_as_uint(m));
+  if (dst && (int)(threadIdx.x & 31) == __ffs(act) - 1) atomicMax(dst, b);
+}
+__device__ __forceinline__ void record_fmax(unsigned *dst, double m) { record_fmax(dst, __double2float_ru(m)); }
+
 // Frequency projection of every constraint mode, applied where the forward
 // transform's last pass holds coefficient k (flat index) at padded offset p:
 //   CLAMP_ABS    all coefficients, +-delta (projection_algorithm.cu:148-188)
@@ -117,6 +127,9 @@ struct ClampArgs {
   const unsigned char *mask = nullptr; // PTW: constrained coefficients
   T sp = T(0), sm = T(0), lo = T(0), hi = T(0), cd = T(0);  // PTW constants
   unsigned *fdirty = nullptr;          // set when a frequency edit is written
+  // all-abs clamp: receives max(|Re|, |Im|) of the clamped coefficients
+  // (FP32 bits of the value rounded up, atomicMax); null: not recorded
+  unsigned *fmax = nullptr;
 };
 
 __device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
@@ -404,19 +417,24 @@ __global__ void __launch_bounds__(sizeof(T) == 4 ? 512 : 256) k_strided(c2<T> *_
   }
   if (MODE == MODE_FCI || MODE == MODE_FCIX || MODE == MODE_FC) {
     bool hit = false;
+    double fm = 0.0;
     for (int it = tid; it < total; it += nthr) {
       const int l = it >> lg;
       const int c = it & (TW - 1);
       if (c < ncol) {
         const long long k = ((bb * s.L + l) * (long long)s.Q + q) * s.Hz + kz0 + c;
-        if (MODE == MODE_FCI || MODE == MODE_FC)
-          buf[l * P + c] = freq_clamp<T>(buf[l * P + c], ca.delta, fedits, k, H, hit);
-        else
+        if (MODE == MODE_FCI || MODE == MODE_FC) {
+          const c2<T> w = freq_clamp<T>(buf[l * P + c], ca.delta, fedits, k, H, hit);
+          buf[l * P + c] = w;
+          fm = fmax(fm, (double)fmax(fabs(w.x), fabs(w.y)));
+        } else {
           buf[l * P + c] =
               freq_project<T>(buf[l * P + c], ca, fedits, k, base + (long long)l * s.Wtot + c, H, hit);
+        }
       }
     }
     mark_dirty(ca.fdirty, hit);
+    if (MODE != MODE_FCIX) record_fmax(ca.fmax, fm);
     __syncthreads();
     if (MODE != MODE_FC) fft_tile<T, +1, EPT>(buf, p, P, lg, tid, nthr);
   }
@@ -434,18 +452,24 @@ __global__ void k_clamp_freq(c2<T> *__restrict__ spec, long long rows, int Hz, i
                              T *__restrict__ fedits, long long H) {
   const long long total = rows * Hz;
   bool hit = false;
+  double fm = 0.0;
   for (long long it = blockIdx.x * (long long)blockDim.x + threadIdx.x; it < total;
        it += (long long)gridDim.x * blockDim.x) {
     const long long r = it / Hz;
     const int kz = (int)(it - r * Hz);
     c2<T> *ptr = spec + r * Hzp + kz;
-    *ptr = freq_project<T>(*ptr, ca, fedits, it, r * Hzp + kz, H, hit);
+    const c2<T> w = freq_project<T>(*ptr, ca, fedits, it, r * Hzp + kz, H, hit);
+    *ptr = w;
+    fm = fmax(fm, (double)fmax(fabs(w.x), fabs(w.y)));
   }
   mark_dirty(ca.fdirty, hit);
+  if (ca.mode == CLAMP_ABS) record_fmax(ca.fmax, fm);
 }
 
 // ---------------------------------------------------------------------------
 static __global__ void k_init_ctl(LoopCtl *ctl) {
+  ctl->fmax_cur = 0u;
+  ctl->fmax_last = 0u;
   ctl->viol_bits = 0ull;
   ctl->last_viol = 0.0;
   ctl->iterations = 0;
@@ -462,6 +486,8 @@ __global__ void k_check(LoopCtl *ctl, T tol, int max_iter, cudaGraphConditionalH
                         int use_graph, unsigned *sdirty) {
   const T v = from_bits<T>(ctl->viol_bits);
   ctl->viol_bits = 0ull;
+  ctl->fmax_last = ctl->fmax_cur;
+  ctl->fmax_cur = 0u;
   ctl->last_viol = (double)v;
   const int it = ctl->iterations + 1;
   ctl->iterations = it;

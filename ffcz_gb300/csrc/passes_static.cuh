@@ -386,6 +386,7 @@ __global__ void __launch_bounds__((L / rp_elems(L, CAP)) << LGTW,
   if (MODE == MODE_FCI || MODE == MODE_FCIX || MODE == MODE_FC) {
     constexpr bool ABS = MODE == MODE_FCI || MODE == MODE_FC;  // the all-abs box
     bool hit = false;
+    T fm = T(0);  // max(|Re|, |Im|) after the all-abs clamp
     // split FCI: |hi| below this is inside the box (0 when delta is too small
     // for the margin to mean anything: every coefficient decides in FP64)
     const float dlo = SPLIT ? (float)((double)ca.delta * (1.0 - 0x1p-20)) : 0.0f;
@@ -410,6 +411,7 @@ __global__ void __launch_bounds__((L / rp_elems(L, CAP)) << LGTW,
           if (h.y != g.y) v[i].y = C((double)h.y);
         } else if (ABS) {
           v[i] = freq_clamp<T>(v[i], ca.delta, fedits, k, H, hit);
+          if constexpr (!SPLIT) fm = fmax(fm, fmax(fabs((T)v[i].x), fabs((T)v[i].y)));
         } else {
           const long long pad = (bb * L + l) * s.Wtot + (long long)q * s.Hzp + kz0 + c;
           v[i] = freq_project<T>(v[i], ca, fedits, k, pad, H, hit);
@@ -417,6 +419,7 @@ __global__ void __launch_bounds__((L / rp_elems(L, CAP)) << LGTW,
       }
     }
     mark_dirty(ca.fdirty, hit);
+    if constexpr (ABS && !SPLIT) record_fmax(ca.fmax, fm);
     // The inverse's first stage reads the positions the forward's last
     // stage wrote, so the same registers continue.  A barrier separates the
     // forward's last shared reads from the inverse's first shared writes.

@@ -140,7 +140,7 @@ struct ffcz_solver {
   void *d_cert = nullptr;            // certificate: per-block sums of squares, two maxima
   // last strict finish: decided by the certificate (1) or the FP64 check (0),
   // the certificate's max |Re/Im| of the spectrum and its error bound
-  int cert_ok = 0;
+  int cert_ok = 0, cert_how = 0;
   double cert_fmax = 0.0, cert_bound = 0.0, cert_smax = 0.0;
   bool extracted = false;
   // the two most recently used loop graphs (a strict-bounds re-run on a
@@ -473,6 +473,7 @@ ClampArgs<T> clamp_args(const ffcz_solver *s) {
   ca.mode = s->cmode;
   ca.delta = (T)s->delta;
   ca.fdirty = s->d_fdirty;
+  ca.fmax = &s->d_ctl->fmax_cur;
   ca.bound = (const T *)s->d_bound;
   ca.orig = (const c2<T> *)s->d_orig;
   if (s->cmode == CLAMP_PTW) {
@@ -978,43 +979,51 @@ __global__ void k_spec_absmax_t(const c2<T> *__restrict__ spec, long long rows, 
 }
 
 // Clamps e to [-eps, eps] (the clamp deltas go to the spatial edits, and a
-// warp that clamped marks the accumulator written), then per block the sum
-// of the squares of the result in FP64 (written to partial[block]: the host
-// adds them in block order, so the sum is reproducible) and max |e|.
+// warp that clamped marks the accumulator written), and per block, in FP64,
+// the sums of the squares before and after the clamp and of the clamp's
+// |changes| (written to partial[3 block + 0..2]: the host adds them in
+// block order, so the sums are reproducible), and max |e| after it.
 template <typename T>
-__global__ void __launch_bounds__(256) k_clamp_sumsq(T *__restrict__ e, T *__restrict__ sedits, T eps, long long n,
+__global__ void __launch_bounds__(256) k_clamp_stats(T *__restrict__ e, T *__restrict__ sedits, T eps, long long n,
                                                      unsigned *sdirty, double *__restrict__ partial,
                                                      unsigned long long *__restrict__ mx) {
-  __shared__ double ws[8];
-  double acc = 0.0, m = 0.0;
+  __shared__ double ws[3][8];
+  double pre = 0.0, post = 0.0, chg = 0.0, m = 0.0;
   bool hit = false;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    T v = e[i];
+    const T v0 = e[i];
+    T v = v0;
     if (v > eps || v < -eps) {
       v = spatial_clamp(v, eps, sedits, i);
       e[i] = v;
       hit = true;
     }
-    const double d = (double)v;
-    acc = fma(d, d, acc);
+    const double d0 = (double)v0, d = (double)v;
+    pre = fma(d0, d0, pre);
+    post = fma(d, d, post);
+    chg += fabs(d0 - d);
     m = fmax(m, fabs(d));
   }
   for (int o = 16; o > 0; o >>= 1) {
-    acc += __shfl_down_sync(0xffffffffu, acc, o);
+    pre += __shfl_down_sync(0xffffffffu, pre, o);
+    post += __shfl_down_sync(0xffffffffu, post, o);
+    chg += __shfl_down_sync(0xffffffffu, chg, o);
     m = fmax(m, __shfl_down_sync(0xffffffffu, m, o));
   }
   const bool any = __any_sync(0xffffffffu, hit);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if (lane == 0) {
-    ws[warp] = acc;
+    ws[0][warp] = pre;
+    ws[1][warp] = post;
+    ws[2][warp] = chg;
     atomic_max_abs(mx, m);
     if (any) *sdirty = 1u;
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
+  if (threadIdx.x < 3) {
     double t = 0.0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += ws[w];
-    partial[blockIdx.x] = t;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += ws[threadIdx.x][w];
+    partial[3 * blockIdx.x + threadIdx.x] = t;
   }
 }
 
@@ -1108,46 +1117,53 @@ int autotune(ffcz_solver *s, int reps, double *ms6) {
 
 }  // namespace
 
-// Certificate of both bounds from the solver's own transform.  The forward
-// transform's rounding error is bounded a posteriori: for a radix-2 FFT with
-// correctly rounded twiddles ||fl(Fe) - Fe||_2 <= log2(n) eta ||Fe||_2,
+// Certificate of both bounds without an FP64 transform.  The rounding of
+// the solver's own transforms is bounded a posteriori: for a radix-2 FFT
+// with correctly rounded twiddles ||fl(Fx) - Fx||_2 <= log2(n) eta ||Fx||_2,
 // eta = u + gamma_4 (sqrt(2) + u) ~ 6.7 u (Higham, Accuracy and Stability of
-// Numerical Algorithms, 2nd ed., Thm 24.2), stage errors adding along a
-// transform's levels; no coefficient's error exceeds that 2-norm, and
-// ||Fe||_2 = sqrt(N) ||e||_2 (Parseval; the half spectrum is part of it).
-// The certificate takes
-//   B = 16 u L sqrt(N sum e_i^2),  L = sum over the axes of ceil(log2 n_a) + 2
-// (+2: the R2C split and the final rounding), 2.4 times the theorem's
-// constant to cover the radix-3/5/16 butterflies and the twiddle tables;
-// u = 2^-24 (FP32), 2^-53 (FP64), 2^-44 (float-float passes).  Both bounds
-// hold in exact arithmetic when max|e| <= E and max|Re/Im| + B <= Delta.
-// With clamp set, e is first clamped to [-eps_t, eps_t] (edits recorded).
+// Numerical Algorithms, 2nd ed., Thm 24.2; the inverse transform alike),
+// stage errors adding along a transform's levels; no coefficient's error
+// exceeds that 2-norm, and ||Fx||_2 = sqrt(N) ||x||_2 (Parseval; the half
+// spectrum is part of the full one).  The certificate takes
+//   beta = 16 u L,  L = sum over the axes of ceil(log2 n_a) + 2
+// (+2: the R2C split or C2R merge and the normalisation), 2.4 times the
+// theorem's constant to cover the radix-3/5/16 butterflies and the twiddle
+// tables; u = 2^-24 (FP32), 2^-53 (FP64), 2^-44 (float-float passes).
+// e is first clamped to [-eps_t, eps_t] (edits recorded), so max |e| <= E.
+//   recorded (after a converged loop): the last iteration's inverse turned
+//     the clamped spectrum F' into e^ = C2R(F')/N + d, ||d||_2 <= beta
+//     ||e^||_2 / (1 - beta); C2R keeps only the Hermitian part of F', whose
+//     Re and Im are at most fmax' = max |Re/Im F'| (recorded by the clamp
+//     pass); the final clamp changes e^ by c.  So every |Re/Im F(e)_k| <=
+//     fmax' + sqrt(N) beta ||e^||_2 / (1 - beta) + ||c||_1.
+//   transform: F(e) in the solver's precision, fmax = max |Re/Im|, and
+//     |Re/Im F(e)_k| <= fmax + beta sqrt(N) ||e||_2.
+// Both bounds hold in exact arithmetic when the right-hand side is <= Delta;
+// *how = 2 (recorded), 1 (transform), 0 (undecided).
 template <typename T>
-int certify(ffcz_solver *s, bool clamp, T eps_t, double *smax, double *fmax, double *bound, int *ok) {
+int certify(ffcz_solver *s, bool clamp, T eps_t, bool use_recorded, double *smax, double *fmax, double *bound,
+            int *ok, int *how) {
   cudaStream_t st = s->stream;
   const unsigned g = (unsigned)std::min<size_t>(ceil_div(s->N, 256), 152 * 16);
-  if (!s->d_cert) FFCZ_CUDA(cudaMalloc(&s->d_cert, (152 * 16 + 2) * sizeof(double)));
+  if (!s->d_cert) FFCZ_CUDA(cudaMalloc(&s->d_cert, (3 * 152 * 16 + 2) * sizeof(double)));
   double *partial = (double *)s->d_cert;
-  unsigned long long *mx = (unsigned long long *)(partial + 152 * 16);
+  unsigned long long *mx = (unsigned long long *)(partial + 3 * 152 * 16);
   FFCZ_CUDA(cudaMemsetAsync(mx, 0, 2 * sizeof(unsigned long long), st));
   const T lim = clamp ? eps_t : std::numeric_limits<T>::infinity();
-  k_clamp_sumsq<T><<<g, 256, 0, st>>>(tp<T>(s->d_e), tp<T>(s->d_sedits), lim, (long long)s->N, s->d_sdirty, partial,
+  k_clamp_stats<T><<<g, 256, 0, st>>>(tp<T>(s->d_e), tp<T>(s->d_sedits), lim, (long long)s->N, s->d_sdirty, partial,
                                       mx);
   FFCZ_CUDA(cudaGetLastError());
-  FFCZ_TRY(forward_spectrum<T>(s, false, s->d_e));
-  const unsigned g2 = (unsigned)std::min<size_t>(ceil_div(s->H, 256), 152 * 16);
-  k_spec_absmax_t<T><<<g2, 256, 0, st>>>((const c2<T> *)s->d_spec, (long long)s->rows, s->Hz, s->Hzp, mx + 1);
-  FFCZ_CUDA(cudaGetLastError());
-  std::vector<double> h(g + 2);
-  FFCZ_CUDA(cudaMemcpyAsync(h.data(), partial, g * sizeof(double), cudaMemcpyDeviceToHost, st));
-  FFCZ_CUDA(cudaMemcpyAsync(h.data() + g, mx, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
+  std::vector<double> h(3 * g + 1);
+  FFCZ_CUDA(cudaMemcpyAsync(h.data(), partial, 3 * g * sizeof(double), cudaMemcpyDeviceToHost, st));
+  FFCZ_CUDA(cudaMemcpyAsync(h.data() + 3 * g, mx, sizeof(double), cudaMemcpyDeviceToHost, st));
   FFCZ_CUDA(cudaStreamSynchronize(st));
-  double sumsq = 0.0;
-  for (unsigned i = 0; i < g; ++i) sumsq += h[i];
-  unsigned long long bits[2];
-  std::memcpy(bits, h.data() + g, sizeof(bits));
-  std::memcpy(smax, &bits[0], 8);
-  std::memcpy(fmax, &bits[1], 8);
+  double pre = 0.0, post = 0.0, chg = 0.0;
+  for (unsigned i = 0; i < g; ++i) {
+    pre += h[3 * i];
+    post += h[3 * i + 1];
+    chg += h[3 * i + 2];
+  }
+  std::memcpy(smax, &h[3 * g], 8);
   auto clog2 = [](size_t n) {
     int l = 0;
     while (((size_t)1 << l) < n) ++l;
@@ -1155,10 +1171,31 @@ int certify(ffcz_solver *s, bool clamp, T eps_t, double *smax, double *fmax, dou
   };
   const int L = clog2(s->nx) + clog2(s->ny) + clog2(s->nz) + 2;
   const double u = sizeof(T) == 4 ? 0x1p-24 : (s->split ? 0x1p-44 : 0x1p-53);
-  // the sum carries its own relative rounding of at most N u_64; 1.001 covers it
-  *bound = 16.0 * u * (double)L * std::sqrt((double)s->N * sumsq * 1.001);
-  const double fb = std::nextafter(*fmax + *bound, std::numeric_limits<double>::infinity());
-  *ok = (*smax <= s->eps && fb <= s->delta) ? 1 : 0;
+  const double beta = 16.0 * u * (double)L;
+  const double N = (double)s->N;
+  const double inf = std::numeric_limits<double>::infinity();
+  // the FP64 sums carry their own relative rounding of at most N u_64: 1.001
+  if (use_recorded) {
+    float fr = 0.0f;
+    std::memcpy(&fr, &s->h_ctl->fmax_last, 4);
+    *fmax = (double)fr;
+    *bound = std::nextafter(std::sqrt(N * pre * 1.001) * beta / (1.0 - beta) + chg * 1.001, inf);
+    *how = 2;
+    *ok = (*smax <= s->eps && std::nextafter(*fmax + *bound, inf) <= s->delta) ? 1 : 0;
+    if (*ok) return FFCZ_OK;
+  }
+  FFCZ_TRY(forward_spectrum<T>(s, false, s->d_e));
+  const unsigned g2 = (unsigned)std::min<size_t>(ceil_div(s->H, 256), 152 * 16);
+  k_spec_absmax_t<T><<<g2, 256, 0, st>>>((const c2<T> *)s->d_spec, (long long)s->rows, s->Hz, s->Hzp, mx + 1);
+  FFCZ_CUDA(cudaGetLastError());
+  unsigned long long bits = 0;
+  FFCZ_CUDA(cudaMemcpyAsync(&bits, mx + 1, sizeof(bits), cudaMemcpyDeviceToHost, st));
+  FFCZ_CUDA(cudaStreamSynchronize(st));
+  std::memcpy(fmax, &bits, 8);
+  *bound = std::nextafter(beta * std::sqrt(N * post * 1.001), inf);
+  *how = 1;
+  *ok = (*smax <= s->eps && std::nextafter(*fmax + *bound, inf) <= s->delta) ? 1 : 0;
+  if (!*ok) *how = 0;
   return FFCZ_OK;
 }
 
@@ -1183,10 +1220,14 @@ int strict_finish(ffcz_solver *s, int max_iter, double tol, int max_rounds, int 
   // the clamp and the certificate in the solver's own precision decide
   // unless a coefficient comes within the rounding bound of Delta
   double cs = 0.0, cf = 0.0, cb = 0.0;
-  int cok = 0;
-  FFCZ_TRY(certify<T>(s, true, Et, &cs, &cf, &cb, &cok));
+  int cok = 0, how = 0;
+  // the clamp pass's recorded maximum describes e only after a loop that
+  // converged on a frequency projection (no final spatial clamp since)
+  const bool recorded = !s->split && s->h_ctl->converged && s->h_ctl->iterations >= 1;
+  FFCZ_TRY(certify<T>(s, true, Et, recorded, &cs, &cf, &cb, &cok, &how));
   s->extracted = false;
   s->cert_ok = cok;
+  s->cert_how = how;
   s->cert_smax = cs;
   s->cert_fmax = cf;
   s->cert_bound = cb;
@@ -1780,14 +1821,15 @@ int ffcz_certify_bounds(ffcz_solver *s, double *spatial_max, double *freq_max, d
   if (!s->initialized) return fail(FFCZ_ERR_NOT_INITIALIZED, "Solver not initialized");
   Range r("ffcz:certify_bounds");
   s->extracted = false;  // the certificate's transform uses the spectrum buffer
-  return s->dtype == FFCZ_F32 ? certify<float>(s, false, 0.0f, spatial_max, freq_max, bound, certified)
-                              : certify<double>(s, false, 0.0, spatial_max, freq_max, bound, certified);
+  int how = 0;
+  return s->dtype == FFCZ_F32 ? certify<float>(s, false, 0.0f, false, spatial_max, freq_max, bound, certified, &how)
+                              : certify<double>(s, false, 0.0, false, spatial_max, freq_max, bound, certified, &how);
 }
 
 int ffcz_get_strict_report(ffcz_solver *s, int *certified, double *freq_max, double *bound) {
   FFCZ_TRY(check_solver(s));
   if (!certified || !freq_max || !bound) return fail(FFCZ_ERR_INVALID, "NULL argument");
-  *certified = s->cert_ok;
+  *certified = s->cert_ok ? s->cert_how : 0;
   *freq_max = s->cert_fmax;
   *bound = s->cert_bound;
   return FFCZ_OK;

@@ -365,6 +365,20 @@ int ffcz_huff_compress_device(const void *d_data, size_t n, int symbol_bytes,
                               int zstd_level, int zstd_mode, void *stream,
                               ffcz_huff_result **out);
 void ffcz_huff_result_free(ffcz_huff_result *r);
+/* Symbol histogram of n device-resident symbols (1 or 2 bytes each,
+ * 16-byte aligned) into h_hist (256 or 65536 counts), computed on the GPU
+ * with the encoder's shared-memory histogram on `stream`; the work of
+ * cudaFrequencyCount (HuffmanZSTDCoder.cuh:48-83) before its compaction to
+ * ascending (symbol, count) pairs. */
+int ffcz_huff_histogram_device(const void *d_data, size_t n, int symbol_bytes, void *stream,
+                               uint32_t *h_hist);
+/* The Huffman tree of buildHuffmanTree (HuffmanZSTDCoder.cuh:85-152) for n
+ * leaves of weights freqs[0..n-1] (the ascending symbols' counts): 2n-1
+ * nodes, leaves first, internal nodes in merge order, each merging the two
+ * smallest (weight, node index) pairs with the first as its left (0)
+ * child; -1 for no child.  *root = 2n-2 (0 for one leaf, -1 for none). */
+int ffcz_huff_tree(const uint32_t *freqs, size_t n, int32_t *left, int32_t *right, uint64_t *weights,
+                   int32_t *root);
 /* CompressionResult fields (:240-246). */
 int ffcz_huff_result_sizes(const ffcz_huff_result *r, size_t *compressed_bytes,
                            size_t *bitstream_bytes, size_t *num_elements,

@@ -120,71 +120,9 @@ struct IterationResults {
 };
 
 #ifdef __CUDACC__
-// Kernel declarations (projection_algorithm.cuh:111-235); definitions and
-// float/double instantiations live in libffcz.so.
-template <typename T>
-__global__ void normalize_kernel(T *data, T factor, size_t size);
-
-template <typename T>
-__global__ void project_frequency_constraints_direct(typename CufftTraits<T>::ComplexType *curr_freq_err,
-                                                     const size_t *freq_constraint_indices, const T *delta_k,
-                                                     T *freq_edits, size_t Nx, size_t Ny, size_t Nz,
-                                                     size_t max_freq_size, size_t num_constraints);
-
-template <typename T>
-__global__ void project_frequency_constraints_all_abs(typename CufftTraits<T>::ComplexType *curr_freq_err,
-                                                      const T delta, T *freq_edits, size_t Nx, size_t Ny,
-                                                      size_t Nz, size_t max_freq_size);
-
-template <typename T>
-__global__ void project_frequency_constraints_all_ptw(typename CufftTraits<T>::ComplexType *curr_freq_err,
-                                                      const typename CufftTraits<T>::ComplexType *orig_freq,
-                                                      const T delta_ptw, T *freq_edits, size_t Nx, size_t Ny,
-                                                      size_t Nz, size_t max_freq_size);
-
-template <typename T>
-__global__ void project_frequency_constraints_partial_ptw(
-    typename CufftTraits<T>::ComplexType *curr_freq_err, const typename CufftTraits<T>::ComplexType *orig_freq,
-    const size_t *freq_constraint_indices, const T delta_ptw, T *freq_edits, size_t Nx, size_t Ny, size_t Nz,
-    size_t max_freq_size, size_t num_constraints);
-
-template <typename T>
-__global__ void project_spatial_constraints_direct(T *spatial_error, T spatial_epsilon, T *spatial_edits,
-                                                   size_t total_size);
-
-template <typename T>
-__global__ void extract_active_flags(const T *edit_array, bool *flag_array, int *int_flag_array,
-                                     size_t total_size, T threshold = T(0));
-
-__global__ void pack_bools(const bool *__restrict__ flag, uint8_t *__restrict__ flag_pack, size_t num_bytes);
-
-template <typename T>
-__global__ void compact_with_prefix_positions(const T *edit_array, const bool *flag_array,
-                                              const int *prefix_positions, T *compact_values, size_t total_size);
-
-template <typename T>
-__global__ void compact_and_quantize_with_prefix_positions(const T *edit_array, const bool *flag_array,
-                                                           const int *prefix_positions, T *compact_values,
-                                                           T *min_edit, T *max_edit, uint16_t *quant_values,
-                                                           size_t total_size);
-
-template <typename T>
-__global__ void reset_accumulators(T *freq_edits, T *spatial_edits, size_t freq_size, size_t spatial_size);
-
-template <typename T>
-__global__ void compute_convergence_metric(const T *spatial_error, T spatial_epsilon, T *convergence_result,
-                                           size_t total_size);
-
-template <typename T>
-__global__ void quantize_and_dequantize(const T *org_arr, T *dequant_arr, T min_val, T max_val, size_t total_size,
-                                        T threshold = T(1e-7));
-
-template <typename T>
-__global__ void frequency_float_to_complex(const T *freq_split, typename CufftTraits<T>::ComplexType *freq_complex,
-                                           size_t total_size);
-
-template <typename T>
-__global__ void add_two_arrays(const T *arr1, T *arr2, size_t total_size);
+// The kernels of projection_algorithm.cuh:111-235, defined in a header (see
+// there) with the float/double instantiations also in libffcz.so.
+#include "projection_kernels.cuh"
 #endif  // __CUDACC__
 
 // projection_algorithm.cu:459-550 (device arrays; min, max and count to

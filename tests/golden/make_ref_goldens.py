@@ -9,6 +9,9 @@ ref_cases.py it writes the case's inputs to a scratch directory, runs
     cudaHuffmanZstdCompress of the four streams at ZSTD level 20);
   * extract cases: `ref_solver extract` -- extract_compact_representation
     and the same four coder calls on the case's synthetic accumulators;
+  * the reference's kernels: `legacy_kernels_ref` (tests/legacy_kernels_driver.cu
+    built against the reference's header and projection_algorithm.cu) ->
+    ref_legacy_kernels.npz;
 
 and stores what the parity tests compare: the iteration count, the active
 counts and min/max, the corrected error e (whole, or a fixed sample plus
@@ -155,6 +158,18 @@ def finish(out: Path, name: str, meta: dict, st: Store):
           f"{meta['num_active_spatial']}) -> {out / f'ref_{name}.npz'}", flush=True)
 
 
+def legacy_kernels(out: Path, tmp: Path):
+    """The reference's own kernels (projection_algorithm.cu:85-673) and host
+    compaction (:459-550) run by tests/legacy_kernels_driver.cu."""
+    exe = ROOT / "oracle" / "_ref" / "legacy_kernels_ref"
+    if not exe.exists():
+        raise SystemExit(f"{exe} is missing: run oracle/build_ref_solver.sh")
+    run([exe, tmp / "legacy.bin"])
+    rec = RC.read_records(tmp / "legacy.bin")
+    np.savez_compressed(out / "ref_legacy_kernels.npz", **rec)
+    print(f"legacy kernels: {len(rec)} outputs -> {out / 'ref_legacy_kernels.npz'}", flush=True)
+
+
 def main():
     out = Path(sys.argv[1]) if len(sys.argv) > 1 else Path(__file__).resolve().parent
     out.mkdir(parents=True, exist_ok=True)
@@ -169,6 +184,8 @@ def main():
         for name in RC.EXTRACT_CASES:
             if not only or name in only:
                 extract_case(name, out, tmp)
+        if not only or "legacy_kernels" in only:
+            legacy_kernels(out, tmp)
 
 
 if __name__ == "__main__":

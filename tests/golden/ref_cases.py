@@ -13,6 +13,7 @@ versions.
 from __future__ import annotations
 
 import hashlib
+import struct
 
 import numpy as np
 
@@ -113,3 +114,21 @@ def checksums(a: np.ndarray) -> np.ndarray:
     a = a.astype(np.float64).reshape(-1)
     return np.array([a.sum(), np.abs(a).sum(), (a * a).sum(), np.abs(a).max() if a.size else 0.0,
                      float(np.count_nonzero(a))])
+
+
+def read_records(path) -> dict:
+    """Records of tests/legacy_kernels_driver.cu: u32 name length, name, u32
+    element bytes, u64 byte count, bytes -> {name: uint8 array}."""
+    with open(path, "rb") as f:
+        b = f.read()
+    out, i = {}, 0
+    while i < len(b):
+        (n,) = struct.unpack_from("<I", b, i)
+        i += 4
+        name = b[i:i + n].decode()
+        i += n
+        _, nbytes = struct.unpack_from("<IQ", b, i)
+        i += 12
+        out[name] = np.frombuffer(b[i:i + nbytes], np.uint8).copy()
+        i += nbytes
+    return out

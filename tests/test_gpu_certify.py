@@ -1,6 +1,8 @@
-"""The strict finish's certificate: the forward transform in the solver's
-own precision plus an a-posteriori bound on its rounding error decides both
-bounds without an FP64 transform when no coefficient is near Delta.
+"""The strict finish's certificate: the solver's own transforms plus an
+a-posteriori bound on their rounding error decide both bounds without an
+FP64 transform when no coefficient is near Delta -- either from the maximum
+the last clamp pass recorded (after a converged loop) or from a forward
+transform of e.
 
 The bound, B = 16 u L sqrt(N sum e_i^2) (L = sum of ceil(log2 n) over the
 axes + 2), is checked against the measured rounding of the solver's own
@@ -79,6 +81,9 @@ def test_certificate_decides_when_delta_is_far(cuda):
         s.solve_all_abs(e0, max_iter, 1e-7)
         st = s.strict_finish(max_iter, 1e-7, 4)
         assert st["met"] and st["certified"] and st["rounds"] == 0
+        # the loop converged on a frequency projection: the clamp pass's
+        # recorded maximum decides without another transform
+        assert st["certified_by"] == "recorded clamp maximum"
         chk = O.check_bounds(np.zeros(1), s.get_results(), fld.eps, fld.delta)
         assert chk["spatial_max"] <= fld.eps and chk["freq_max"] <= fld.delta
         assert chk["freq_max"] <= st["freq_max"]  # the certified value bounds the FP64 one
