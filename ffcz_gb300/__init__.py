@@ -32,6 +32,7 @@ FFCZ_LOOP_GRAPH, FFCZ_LOOP_HOST = 0, 1
 FFCZ_PRECISION_NATIVE, FFCZ_PRECISION_SPLIT = 0, 1
 FFCZ_ZSTD_SINGLE, FFCZ_ZSTD_CHUNKED, FFCZ_ZSTD_NONE = 0, 1, 2
 FFCZ_FORM_FUSED, FFCZ_FORM_PLAIN = 0, 1
+FFCZ_DFT_SIMT, FFCZ_DFT_TENSOR = 0, 1
 FFCZ_ERR_INVALID, FFCZ_ERR_CUDA, FFCZ_ERR_UNSUPPORTED, FFCZ_ERR_NOT_INITIALIZED = -1, -2, -3, -4
 FFCZ_ERR_ZSTD, FFCZ_ERR_CAPACITY, FFCZ_ERR_CODE_TOO_LONG, FFCZ_ERR_EMPTY, FFCZ_ERR_IO = -5, -6, -7, -8, -9
 ERRORS = {-1: "INVALID", -2: "CUDA", -3: "UNSUPPORTED", -4: "NOT_INITIALIZED", -5: "ZSTD",
@@ -77,6 +78,7 @@ SIGNATURES = {
     "ffcz_solver_set_loop_driver": [_p, _i],
     "ffcz_solver_set_pack_mode": [_p, _i],
     "ffcz_solver_set_form": [_p, _i],
+    "ffcz_solver_set_dft_stages": [_p, _i],
     "ffcz_init_all_abs": [_p, _p, _d, _d],
     "ffcz_init_all_abs_device": [_p, _p, _d, _d],
     "ffcz_solve_all_abs": [_p, _p, _i, _d],
@@ -249,6 +251,11 @@ class ProjectionSolver:
         """FFCZ_FORM_FUSED (five passes per 3D iteration) or FFCZ_FORM_PLAIN
         (six: x forward + clamp and x inverse as separate passes)."""
         _check(lib().ffcz_solver_set_form(self._h, int(form)))
+
+    def set_dft_stages(self, stages: int) -> None:
+        """FFCZ_DFT_SIMT or FFCZ_DFT_TENSOR (radix-16 stages of the FP32
+        strided passes of length 256/512 as tensor-core DFT matrix products)."""
+        _check(lib().ffcz_solver_set_dft_stages(self._h, int(stages)))
 
     # -- reference API -------------------------------------------------------
     def _host(self, a) -> np.ndarray:

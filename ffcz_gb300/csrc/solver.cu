@@ -76,6 +76,14 @@ struct ffcz_solver {
   int loop_driver = FFCZ_LOOP_GRAPH;
   int pack_mode = FFCZ_PACK_CORRECT;
   int form = FFCZ_FORM_FUSED;  // FFCZ_FORM_PLAIN: the six-pass all-abs iteration
+  // tensor-core DFT stages (FFCZ_DFT_TENSOR; FP32 strided axes of length 256
+  // and 512): kernels, tile and plan of each strided axis (0 y, 1 x), used
+  // by its all-abs passes and the forward transforms
+  int dft = FFCZ_DFT_SIMT;
+  void *ktc[2][kStridedModes] = {};
+  SArgs stc[2]{};
+  Launch ltc[2]{};
+  AxisPlan ptc[2]{};
   // device arrays
   void *d_x = nullptr, *d_e = nullptr, *d_spec = nullptr;
   void *d_fedits = nullptr, *d_sedits = nullptr;
@@ -489,6 +497,26 @@ ClampArgs<T> clamp_args(const ffcz_solver *s) {
   return ca;
 }
 
+// One strided pass of axis 0 (y) or 1 (x) in `mode`: the tensor-core
+// kernel where one is selected for this axis and mode (all-abs), else the
+// plain (fused = false) or fused family's kernel, tile and plan.
+template <typename T>
+void strided_pass(ffcz_solver *s, cudaStream_t st, int axis, int mode, bool fused, const ClampArgs<T> &ca,
+                  c2<T> *spec) {
+  const long long H = (long long)s->H;
+  if (sizeof(T) == 4 && s->dft == FFCZ_DFT_TENSOR && s->ktc[axis][mode] && ca.mode == CLAMP_ABS) {
+    const Launch &ln = s->ltc[axis];
+    ((StridedFn<T>)s->ktc[axis][mode])<<<ln.grid, ln.threads, ln.smem, st>>>(spec, s->stc[axis], s->ptc[axis], ca,
+                                                                            tp<T>(s->d_fedits), H);
+    return;
+  }
+  void *k = (axis == 0 ? s->ky : s->kx)[mode];
+  const Launch &ln = fused ? (axis == 0 ? s->lyf : s->lxf) : (axis == 0 ? s->ly : s->lx);
+  const SArgs &sa = fused ? (axis == 0 ? s->syf : s->sxf) : (axis == 0 ? s->sy : s->sx);
+  const AxisPlan &pl = fused ? (axis == 0 ? s->pyf : s->pxf) : (axis == 0 ? s->py : s->px);
+  ((StridedFn<T>)k)<<<ln.grid, ln.threads, ln.smem, st>>>(spec, sa, pl, ca, tp<T>(s->d_fedits), H);
+}
+
 // One iteration: [prologue + R2C z] [y fwd] [fused fwd/clamp/inv] [y inv]
 // [C2R z + 1/N + violation] [check].
 template <typename T>
@@ -524,45 +552,35 @@ void launch_iteration(ffcz_solver *s, cudaStream_t st, int pro, const void *a, c
   if (plain && s->fused == 2) {
     // six passes: y forward, x forward + clamp, x inverse, y inverse
     if (s->has_y) {
-      ((StridedFn<T>)s->ky[MODE_FWD])<<<s->ly.grid, s->ly.threads, s->ly.smem, st>>>(spec, s->sy, s->py, delta,
-                                                                                     tp<T>(s->d_fedits), H);
+      strided_pass<T>(s, st, 0, MODE_FWD, false, delta, spec);
       mark();
     }
-    ((StridedFn<T>)s->kx[MODE_FC])<<<s->lx.grid, s->lx.threads, s->lx.smem, st>>>(spec, s->sx, s->px, delta,
-                                                                                   tp<T>(s->d_fedits), H);
+    strided_pass<T>(s, st, 1, MODE_FC, false, delta, spec);
     mark();
-    ((StridedFn<T>)s->kx[MODE_INV])<<<s->lx.grid, s->lx.threads, s->lx.smem, st>>>(spec, s->sx, s->px, delta,
-                                                                                    tp<T>(s->d_fedits), H);
+    strided_pass<T>(s, st, 1, MODE_INV, false, delta, spec);
     mark();
     if (s->has_y) {
-      ((StridedFn<T>)s->ky[MODE_INV])<<<s->ly.grid, s->ly.threads, s->ly.smem, st>>>(spec, s->sy, s->py, delta,
-                                                                                     tp<T>(s->d_fedits), H);
+      strided_pass<T>(s, st, 0, MODE_INV, false, delta, spec);
       mark();
     }
   } else if (plain && s->fused == 1) {
-    ((StridedFn<T>)s->ky[MODE_FC])<<<s->ly.grid, s->ly.threads, s->ly.smem, st>>>(spec, s->sy, s->py, delta,
-                                                                                   tp<T>(s->d_fedits), H);
+    strided_pass<T>(s, st, 0, MODE_FC, false, delta, spec);
     mark();
-    ((StridedFn<T>)s->ky[MODE_INV])<<<s->ly.grid, s->ly.threads, s->ly.smem, st>>>(spec, s->sy, s->py, delta,
-                                                                                    tp<T>(s->d_fedits), H);
+    strided_pass<T>(s, st, 0, MODE_INV, false, delta, spec);
     mark();
   } else if (s->fused == 2) {
     if (s->has_y) {
-      ((StridedFn<T>)s->ky[MODE_FWD])<<<s->ly.grid, s->ly.threads, s->ly.smem, st>>>(spec, s->sy, s->py, delta,
-                                                                                     tp<T>(s->d_fedits), H);
+      strided_pass<T>(s, st, 0, MODE_FWD, false, delta, spec);
       mark();
     }
-    ((StridedFn<T>)s->kx[fci])<<<s->lxf.grid, s->lxf.threads, s->lxf.smem, st>>>(spec, s->sxf, s->pxf, delta,
-                                                                                   tp<T>(s->d_fedits), H);
+    strided_pass<T>(s, st, 1, fci, true, delta, spec);
     mark();
     if (s->has_y) {
-      ((StridedFn<T>)s->ky[MODE_INV])<<<s->ly.grid, s->ly.threads, s->ly.smem, st>>>(spec, s->sy, s->py, delta,
-                                                                                     tp<T>(s->d_fedits), H);
+      strided_pass<T>(s, st, 0, MODE_INV, false, delta, spec);
       mark();
     }
   } else if (s->fused == 1) {
-    ((StridedFn<T>)s->ky[fci])<<<s->lyf.grid, s->lyf.threads, s->lyf.smem, st>>>(spec, s->syf, s->pyf, delta,
-                                                                                   tp<T>(s->d_fedits), H);
+    strided_pass<T>(s, st, 0, fci, true, delta, spec);
     mark();
   } else {
     const long long tot = s->rows * s->Hz;
@@ -912,12 +930,9 @@ int forward_spectrum(ffcz_solver *s, bool keep_as_orig = true, const void *src =
   const long long H = (long long)s->H;
   ((ZfwdFn<T>)s->kzf[PRO_PLAIN])<<<s->lz_f.grid, s->lz_f.threads, s->lz_f.smem, st>>>(
       (const T *)(src ? src : s->d_x), nullptr, tp<T>(s->d_sedits), (T)s->eps, spec, s->za, s->pz, post);
-  if (s->has_y)
-    ((StridedFn<T>)s->ky[MODE_FWD])<<<s->ly.grid, s->ly.threads, s->ly.smem, st>>>(spec, s->sy, s->py, none,
-                                                                                   tp<T>(s->d_fedits), H);
-  if (s->has_x)
-    ((StridedFn<T>)s->kx[MODE_FWD])<<<s->lx.grid, s->lx.threads, s->lx.smem, st>>>(spec, s->sx, s->px, none,
-                                                                                   tp<T>(s->d_fedits), H);
+  if (s->has_y) strided_pass<T>(s, st, 0, MODE_FWD, false, none, spec);
+  if (s->has_x) strided_pass<T>(s, st, 1, MODE_FWD, false, none, spec);
+  (void)H;
   if (keep_as_orig) {
     const size_t bytes = (size_t)s->rows * s->Hzp * 2 * s->es;
     if (!s->d_orig) FFCZ_CUDA(cudaMalloc(&s->d_orig, bytes));
@@ -966,29 +981,33 @@ __global__ void k_spec_absmax(const double2 *__restrict__ spec, long long rows, 
 template <typename T>
 __global__ void k_spec_absmax_t(const c2<T> *__restrict__ spec, long long rows, int Hz, int Hzp,
                                 unsigned long long *__restrict__ mx) {
-  double m = 0.0;
+  T mt = T(0);
   const long long total = rows * Hz;
   for (long long it = (long long)blockIdx.x * blockDim.x + threadIdx.x; it < total;
        it += (long long)gridDim.x * blockDim.x) {
     const long long r = it / Hz;
     const c2<T> v = spec[r * Hzp + (it - r * Hz)];
-    m = fmax(m, fmax(fabs((double)v.x), fabs((double)v.y)));
+    mt = fmax(mt, fmax(fabs(v.x), fabs(v.y)));
   }
+  double m = (double)mt;
   for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_down_sync(0xffffffffu, m, o));
   if ((threadIdx.x & 31) == 0) atomic_max_abs(mx, m);
 }
 
 // Clamps e to [-eps, eps] (the clamp deltas go to the spatial edits, and a
-// warp that clamped marks the accumulator written), and per block, in FP64,
-// the sums of the squares before and after the clamp and of the clamp's
-// |changes| (written to partial[3 block + 0..2]: the host adds them in
-// block order, so the sums are reproducible), and max |e| after it.
+// warp that clamped marks the accumulator written), and per block the sums
+// of the squares before and after the clamp and of the clamp's |changes|
+// (written to partial[3 block + 0..2]: the host adds them in block order, so
+// the sums are reproducible), and max |e| after it.  Each thread sums its
+// elements in T (FP64 arithmetic is slow on this GPU; the host widens the
+// sums by the rounding bound of that many terms), the warps and the block
+// in FP64.
 template <typename T>
 __global__ void __launch_bounds__(256) k_clamp_stats(T *__restrict__ e, T *__restrict__ sedits, T eps, long long n,
                                                      unsigned *sdirty, double *__restrict__ partial,
                                                      unsigned long long *__restrict__ mx) {
   __shared__ double ws[3][8];
-  double pre = 0.0, post = 0.0, chg = 0.0, m = 0.0;
+  T pre = T(0), post = T(0), chg = T(0), m = T(0);
   bool hit = false;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     const T v0 = e[i];
@@ -997,26 +1016,26 @@ __global__ void __launch_bounds__(256) k_clamp_stats(T *__restrict__ e, T *__res
       v = spatial_clamp(v, eps, sedits, i);
       e[i] = v;
       hit = true;
+      chg += fabs(v0 - v);
     }
-    const double d0 = (double)v0, d = (double)v;
-    pre = fma(d0, d0, pre);
-    post = fma(d, d, post);
-    chg += fabs(d0 - d);
-    m = fmax(m, fabs(d));
+    pre = fma(v0, v0, pre);
+    post = fma(v, v, post);
+    m = fmax(m, fabs(v));
   }
+  double dpre = (double)pre, dpost = (double)post, dchg = (double)chg, dm = (double)m;
   for (int o = 16; o > 0; o >>= 1) {
-    pre += __shfl_down_sync(0xffffffffu, pre, o);
-    post += __shfl_down_sync(0xffffffffu, post, o);
-    chg += __shfl_down_sync(0xffffffffu, chg, o);
-    m = fmax(m, __shfl_down_sync(0xffffffffu, m, o));
+    dpre += __shfl_down_sync(0xffffffffu, dpre, o);
+    dpost += __shfl_down_sync(0xffffffffu, dpost, o);
+    dchg += __shfl_down_sync(0xffffffffu, dchg, o);
+    dm = fmax(dm, __shfl_down_sync(0xffffffffu, dm, o));
   }
   const bool any = __any_sync(0xffffffffu, hit);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if (lane == 0) {
-    ws[0][warp] = pre;
-    ws[1][warp] = post;
-    ws[2][warp] = chg;
-    atomic_max_abs(mx, m);
+    ws[0][warp] = dpre;
+    ws[1][warp] = dpost;
+    ws[2][warp] = dchg;
+    atomic_max_abs(mx, dm);
     if (any) *sdirty = 1u;
   }
   __syncthreads();
@@ -1174,12 +1193,18 @@ int certify(ffcz_solver *s, bool clamp, T eps_t, bool use_recorded, double *smax
   const double beta = 16.0 * u * (double)L;
   const double N = (double)s->N;
   const double inf = std::numeric_limits<double>::infinity();
-  // the FP64 sums carry their own relative rounding of at most N u_64: 1.001
+  // each thread summed at most k terms in T (relative rounding <= (k+1) u
+  // for non-negative terms), the FP64 tree above it at most N u_64: widen
+  const double k = std::ceil(N / ((double)g * 256.0));
+  const double widen = (1.0 + (k + 2.0) * u) * 1.001;
+  pre *= widen;
+  post *= widen;
+  chg *= widen;
   if (use_recorded) {
     float fr = 0.0f;
     std::memcpy(&fr, &s->h_ctl->fmax_last, 4);
     *fmax = (double)fr;
-    *bound = std::nextafter(std::sqrt(N * pre * 1.001) * beta / (1.0 - beta) + chg * 1.001, inf);
+    *bound = std::nextafter(std::sqrt(N * pre) * beta / (1.0 - beta) + chg, inf);
     *how = 2;
     *ok = (*smax <= s->eps && std::nextafter(*fmax + *bound, inf) <= s->delta) ? 1 : 0;
     if (*ok) return FFCZ_OK;
@@ -1192,7 +1217,7 @@ int certify(ffcz_solver *s, bool clamp, T eps_t, bool use_recorded, double *smax
   FFCZ_CUDA(cudaMemcpyAsync(&bits, mx + 1, sizeof(bits), cudaMemcpyDeviceToHost, st));
   FFCZ_CUDA(cudaStreamSynchronize(st));
   std::memcpy(fmax, &bits, 8);
-  *bound = std::nextafter(beta * std::sqrt(N * post * 1.001), inf);
+  *bound = std::nextafter(beta * std::sqrt(N * post), inf);
   *how = 1;
   *ok = (*smax <= s->eps && std::nextafter(*fmax + *bound, inf) <= s->delta) ? 1 : 0;
   if (!*ok) *how = 0;
@@ -1425,6 +1450,53 @@ int ffcz_solver_set_form(ffcz_solver *s, int form) {
   if (form != s->form)
     for (LoopGraph &g : s->lg) g.reset();
   s->form = form;
+  return FFCZ_OK;
+}
+
+int ffcz_solver_set_dft_stages(ffcz_solver *s, int stages) {
+  FFCZ_TRY(check_solver(s));
+  if (stages != FFCZ_DFT_SIMT && stages != FFCZ_DFT_TENSOR) return fail(FFCZ_ERR_INVALID, "unknown DFT stages");
+  for (LoopGraph &g : s->lg) g.reset();
+  for (int a = 0; a < 2; ++a)
+    for (int m = 0; m < kStridedModes; ++m) s->ktc[a][m] = nullptr;
+  s->dft = FFCZ_DFT_SIMT;
+  if (stages == FFCZ_DFT_SIMT) return FFCZ_OK;
+  if (s->dtype != FFCZ_F32) return fail(FFCZ_ERR_UNSUPPORTED, "tensor-core DFT stages are FP32 only");
+  int axes = 0;
+  for (int a = 0; a < 2; ++a) {
+    const bool has = a == 0 ? s->has_y : s->has_x;
+    const int L = a == 0 ? (int)s->ny : (int)s->nx;
+    if (!has || (L != 256 && L != 512)) continue;
+    const int Q = a == 0 ? 1 : (int)s->ny;
+    const long long B = a == 0 ? (long long)s->nx : 1;
+    StaticGeom g;
+    for (int m : {MODE_FWD, MODE_INV, MODE_FC, MODE_FCI}) {
+      StridedFn<float> fn = nullptr;
+      if (!tc_strided(L, m, fn, g)) {
+        for (int b = 0; b < 2; ++b)
+          for (int mm = 0; mm < kStridedModes; ++mm) s->ktc[b][mm] = nullptr;
+        return fail(FFCZ_ERR_CUDA, "tensor-core pass set-up failed");
+      }
+      s->ktc[a][m] = (void *)fn;
+    }
+    SArgs &sa = s->stc[a];
+    sa.L = L;
+    sa.Q = Q;
+    sa.Hz = s->Hz;
+    sa.Hzp = s->Hzp;
+    sa.Wtot = (long long)Q * s->Hzp;
+    sa.TW = g.TW;
+    sa.log2TW = __builtin_ctz(g.TW);
+    sa.P = g.TW + 1;
+    sa.tpq = (int)ceil_div((size_t)s->Hz, (size_t)g.TW);
+    s->ltc[a].threads = g.threads;
+    s->ltc[a].smem = g.smem;
+    s->ltc[a].grid = (unsigned)(B * Q * (long long)sa.tpq);
+    s->ptc[a] = a == 0 ? s->py_s : s->px_s;  // the plain stage list's plan
+    ++axes;
+  }
+  if (!axes) return fail(FFCZ_ERR_UNSUPPORTED, "no strided axis of length 256 or 512");
+  s->dft = FFCZ_DFT_TENSOR;
   return FFCZ_OK;
 }
 

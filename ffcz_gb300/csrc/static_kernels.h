@@ -47,5 +47,9 @@ bool static_strided(int L, int mode, StridedFn<T> &fn, StaticGeom &g, int var = 
 // (MODE_FC): the plain stage-list family and tile of MODE_FWD, so it shares
 // that pass's geometry.  No float-float variant.
 template <typename T> bool static_strided_fc(int L, StridedFn<T> &fn, StaticGeom &g, int var = 0);
+// The FP32 passes whose radix-16 stages run on the tensor cores
+// (passes_tc.cuh), L = 256 or 512, modes MODE_FWD, MODE_INV, MODE_FC and
+// MODE_FCI, all on the plain stage list (static_plain_cap); false otherwise.
+bool tc_strided(int L, int mode, StridedFn<float> &fn, StaticGeom &g);
 
 }  // namespace ffcz

@@ -106,6 +106,9 @@ WORKLOADS = {
     "fp64_512": ((512, 512, 512), 11 / 3, 4, 5e-5, 2e-4, 0.0, True, np.float64, 500),
     # the FP64 variant at 256^3: a case small enough for full kernel profiles
     "fp64_256": ((256, 256, 256), 11 / 3, 4, 5e-5, 2e-4, 0.0, True, np.float64, 500),
+    # the precision field's spectrum kernels at a profiling size: the same
+    # 512-point x and y passes on a quarter of the z extent (2 GB resident)
+    "precision_slab": ((512, 512, 128), 3.0, 2, 1e-4, 1e-4, 0.0, False, np.float32, 100),
 }
 
 

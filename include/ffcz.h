@@ -102,6 +102,18 @@ int ffcz_solver_set_pack_mode(ffcz_solver *s, int mode);
 #define FFCZ_FORM_FUSED 0
 #define FFCZ_FORM_PLAIN 1
 int ffcz_solver_set_form(ffcz_solver *s, int form);
+/* Arithmetic of the radix-16 stages of the FP32 strided passes of length
+ * 256 and 512 (no counterpart in the reference, which calls cuFFT):
+ *   FFCZ_DFT_SIMT (default): register butterflies on the FP32 pipes;
+ *   FFCZ_DFT_TENSOR: each radix-16 stage as 16-point DFT matrix products on
+ *     the tensor cores (mma.sync m16n8k8, operands split into two TF32
+ *     terms, three products, FP32 accumulation: ~21-bit products), the tile
+ *     staged in shared memory; applies to the all-abs passes and forward
+ *     transforms of those axes (the other axes and modes keep SIMT).
+ * FFCZ_ERR_UNSUPPORTED for FP64 solvers or without such an axis. */
+#define FFCZ_DFT_SIMT 0
+#define FFCZ_DFT_TENSOR 1
+int ffcz_solver_set_dft_stages(ffcz_solver *s, int stages);
 
 /* initialize_all_abs(h_orig, eps, delta) -- impl:639-668.  x is a host
  * array of Nx*Ny*Nz elements of the solver's dtype; eps and delta are

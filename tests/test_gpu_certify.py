@@ -25,8 +25,14 @@ MARGIN = 4.0
 
 
 def bound(shape, e, u):
+    """16 u L sqrt(N sum e^2), the sum widened as the library widens its
+    per-thread partial sums (k terms each in the field's precision)."""
     L = sum(math.ceil(math.log2(n)) if n > 1 else 0 for n in shape) + 2
-    return 16.0 * u * L * math.sqrt(e.size * float(np.sum(e.astype(np.float64) ** 2)) * 1.001)
+    n = e.size
+    g = min(-(-n // 256), 152 * 16)
+    k = math.ceil(n / (g * 256.0))
+    widen = (1.0 + (k + 2.0) * u) * 1.001
+    return 16.0 * u * L * math.sqrt(n * float(np.sum(e.astype(np.float64) ** 2)) * widen)
 
 
 def inputs(shape, dtype):
@@ -66,7 +72,7 @@ def test_bound_covers_the_measured_rounding(cuda, shape, dtype):
             s.solve_all_abs(e, 0, 1e-7)
             c = s.certify_bounds()
             assert c["freq_max"] == max(np.abs(spec.real).max(), np.abs(spec.imag).max())
-            assert c["bound"] == pytest.approx(B, rel=1e-9)
+            assert c["bound"] == pytest.approx(B, rel=1e-5)  # the device sums in the field's precision
             assert c["spatial_max"] == float(np.abs(e).max())
     print(f"{shape} {np.dtype(dtype).name}: worst measured error / bound = {worst:.3g}")
 
