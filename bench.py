@@ -84,6 +84,8 @@ def parse():
                     help="leave out the strict FP64 bounds finish (the reference schedule's bounds only)")
     ap.add_argument("--no-plain", action="store_true", help="leave out the plain FP32 (six-pass) form")
     ap.add_argument("--no-stress", action="store_true", help="leave out the Delta = E sqrt(N/6) stress step")
+    ap.add_argument("--no-tensor", action="store_true",
+                    help="leave out the form with tensor-core DFT stages")
     ap.add_argument("--reference-budget-s", type=float, default=90.0,
                     help="--impl reference: time budget of its timed steps")
     ap.add_argument("--no-cufft-reference", action="store_true",
@@ -331,11 +333,13 @@ def run_ours(args):
     def zstd_jobs(res):
         return [pool.submit(F.zstd_compress, r.bitstream, args.zstd_level, zmode) for r in res if r is not None]
 
-    def make_solver(form, delta=None):
+    def make_solver(form, delta=None, tensor=False):
         s = F.ProjectionSolver(*fld.shape, dtype=dt)
         if dt == np.float64 and args.precision == "split":
             s.set_precision(F.FFCZ_PRECISION_SPLIT)
         s.set_form(form)
+        if tensor:
+            s.set_dft_stages(F.FFCZ_DFT_TENSOR)
         s.set_stream(torch.cuda.current_stream())
         s.set_loop_driver(F.FFCZ_LOOP_HOST if args.loop == "host" else F.FFCZ_LOOP_GRAPH)
         s.set_profiling(True)
@@ -461,6 +465,16 @@ def run_ours(args):
         plain["max_abs_diff_vs_chosen"] = float(np.abs(e_plain.astype(np.float64) - e_fin).max())
         ps.close()
 
+    tensor = None
+    if not args.no_tensor and dt == np.float32 and any(n in (256, 512) for n in fld.shape[:2] if n > 1):
+        ts, _ = make_solver(F.FFCZ_FORM_FUSED, tensor=True)
+        tensor = measure_form(ts)
+        e_tc = ts.get_results()
+        tensor["max_abs_diff_vs_chosen"] = float(np.abs(e_tc.astype(np.float64) - e_fin).max())
+        tensor["passes"] = {pass_names(fld.shape)[i]: round(statistics.mean(m for m, _ in v), 5)
+                            for i, v in tensor["pass_ms"].items()}
+        ts.close()
+
     stress = None if args.no_stress else measure_stress(F, torch, fld, dx, dxp, max_iter, strict, args)
 
     # dominant pass of the chosen form (first iteration's events inside the graph)
@@ -493,7 +507,7 @@ def run_ours(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32" if dt == np.float32 else "f64",
         "data": "synthetic", "config": config(args, fld, its, max_iter, strict),
         "e2e": {"value": rc["e2e"], "unit": "GB/s", "h2d_bytes_per_step": 2 * in_bytes, "d2h_bytes_per_step": rc["d2h"]},
-        "forms": form_report(rc, plain),
+        "forms": form_report(rc, plain, tensor),
         "gpu_only": {"value": rc["gpu_only"], "unit": "GB/s",
                      "what": "project + strict bounds + compaction + Huffman, device-resident inputs, no ZSTD"},
         "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -529,7 +543,7 @@ def run_ours(args):
     pool.shutdown()
 
 
-def form_report(rc, plain):
+def form_report(rc, plain, tensor=None):
     def one(r):
         return {"value": r["value"], "e2e": r["e2e"], "gpu_only": r["gpu_only"], "ms_per_step": r["ms_per_step"],
                 "passes_per_iteration": len(r["pass_ms"]), "iterations": r["its"], "clocks": r["clocks"]}
@@ -544,6 +558,12 @@ def form_report(rc, plain):
         out["ratio_value"] = rc["value"] / plain["value"]
         out["ratio_e2e"] = rc["e2e"] / plain["e2e"]
         out["ratio_gpu_only"] = rc["gpu_only"] / plain["gpu_only"]
+    if tensor is not None:
+        out["tensor_dft"] = dict(one(tensor), form="the chosen form with the radix-16 stages of the 256/512-point "
+                                                  "strided passes as tensor-core DFT matrix products (mma.sync, "
+                                                  "split-TF32 operands, FP32 accumulation)",
+                                 max_abs_diff_vs_chosen=tensor["max_abs_diff_vs_chosen"], passes_ms=tensor["passes"])
+        out["ratio_tensor_vs_chosen_value"] = tensor["value"] / rc["value"]
     return out
 
 

@@ -31,10 +31,13 @@ namespace ffcz {
 constexpr int kTcTW = 8;       // columns per tile (one MMA N dimension)
 constexpr int kTcThreads = 256;
 
-__host__ __device__ constexpr int tc_pitch(int L) { return L + L / 4 + 2; }
-// Shared-memory slot of (position, column): columns are L + L/4 + 2 apart,
-// and positions skew by 8 slots per L/16 block, so that the eight columns
-// and four rows an MMA fragment touches spread over all banks.
+// Column pitch: room for L positions plus the largest skew (8 * 15 slots),
+// and 2 mod 16 slots, so that consecutive columns start 4 banks apart.
+__host__ __device__ constexpr int tc_pitch(int L) { return L + 130; }
+// Shared-memory slot of (position, column): positions skew by 8 slots per
+// L/16 block, so that the eight columns and four rows an MMA fragment
+// touches spread over all banks.  Slots of a column stay below the next
+// column's first slot: L - 1 + 8 * 15 < tc_pitch(L).
 template <int L>
 __device__ __forceinline__ int tc_slot(int pos, int c) {
   return c * tc_pitch(L) + pos + 8 * (pos / (L / 16));
@@ -199,6 +202,7 @@ __global__ void __launch_bounds__(kTcThreads) ks_strided_tc(float2 *__restrict__
                                                             ClampArgs<float> ca, float *__restrict__ fedits,
                                                             long long H) {
   static_assert(L == 256 || L == 512, "tensor-core passes: L = 256 or 512");
+  static_assert((L - 1) + 8 * 15 < tc_pitch(L) && tc_pitch(L) % 16 == 2, "slot layout");
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float2 *b0 = reinterpret_cast<float2 *>(smem_raw);
   float2 *b1 = b0 + kTcTW * tc_pitch(L) + 16;
