@@ -1006,21 +1006,48 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_clamp_stats(T *__restrict__ e, T *__restrict__ sedits, T eps, long long n,
                                                      unsigned *sdirty, double *__restrict__ partial,
                                                      unsigned long long *__restrict__ mx) {
+  // 16-byte vectors, kU of them loaded before any is processed, so that
+  // each thread keeps several loads in flight (e is 16-byte aligned)
+  using V = std::conditional_t<sizeof(T) == 4, float4, double2>;
+  constexpr int kW = 16 / (int)sizeof(T), kU = 4;
   __shared__ double ws[3][8];
   T pre = T(0), post = T(0), chg = T(0), m = T(0);
   bool hit = false;
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    const T v0 = e[i];
-    T v = v0;
+  auto one = [&](T &v, long long i) {
+    const T v0 = v;
     if (v > eps || v < -eps) {
       v = spatial_clamp(v, eps, sedits, i);
-      e[i] = v;
       hit = true;
       chg += fabs(v0 - v);
     }
     pre = fma(v0, v0, pre);
     post = fma(v, v, post);
     m = fmax(m, fabs(v));
+    return v != v0;
+  };
+  V *ev = reinterpret_cast<V *>(e);
+  const long long nv = n / kW;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long b0 = (long long)blockIdx.x * blockDim.x + threadIdx.x; b0 < nv; b0 += stride * kU) {
+    V buf[kU];
+#pragma unroll
+    for (int u = 0; u < kU; ++u)
+      if (b0 + u * stride < nv) buf[u] = ev[b0 + u * stride];
+#pragma unroll
+    for (int u = 0; u < kU; ++u) {
+      const long long vi = b0 + u * stride;
+      if (vi >= nv) break;
+      T *vals = reinterpret_cast<T *>(&buf[u]);
+      bool changed = false;
+#pragma unroll
+      for (int w = 0; w < kW; ++w) changed |= one(vals[w], vi * kW + w);
+      if (changed) ev[vi] = buf[u];
+    }
+  }
+  // the last n mod kW elements
+  for (long long i = nv * kW + (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    T v = e[i];
+    if (one(v, i)) e[i] = v;
   }
   double dpre = (double)pre, dpost = (double)post, dchg = (double)chg, dm = (double)m;
   for (int o = 16; o > 0; o >>= 1) {
@@ -1195,7 +1222,7 @@ int certify(ffcz_solver *s, bool clamp, T eps_t, bool use_recorded, double *smax
   const double inf = std::numeric_limits<double>::infinity();
   // each thread summed at most k terms in T (relative rounding <= (k+1) u
   // for non-negative terms), the FP64 tree above it at most N u_64: widen
-  const double k = std::ceil(N / ((double)g * 256.0));
+  const double k = std::ceil(N / ((double)g * 256.0)) + 16.0;  // + one vector of the tail
   const double widen = (1.0 + (k + 2.0) * u) * 1.001;
   pre *= widen;
   post *= widen;
