@@ -427,6 +427,7 @@ def run_ours(args):
         rep["d2h"] = sum(len(r.bitstream) for r in out_e if r is not None) + 8 * 4
         rep["its"] = s.iterations
         rep["counts"] = s.active_counts()
+        rep["tiles"] = {k: {"variant": v[0], "tma_staged": v[1]} for k, v in s.tuning()["choice"].items()}
         return rep
 
     chosen, tune = make_solver(F.FFCZ_FORM_FUSED)
@@ -516,6 +517,7 @@ def run_ours(args):
         "passes": {names[i]: {"ms": round(m, 5), "GB/s": round(b / (m / 1e3) / 1e9, 1)} for i, (m, b) in avg.items()},
         "gpu_launches": rc["launches"],
         "autotune_ms": {k: [round(v[0], 4), round(v[1], 4)] for k, v in tune.items()},
+        "tiles": rc["tiles"],
         "iterations": its,
         "active_edits": {"freq": counts[0], "spatial": counts[1]},
         "bounds_fp64": bounds,

@@ -33,6 +33,7 @@ FFCZ_PRECISION_NATIVE, FFCZ_PRECISION_SPLIT = 0, 1
 FFCZ_ZSTD_SINGLE, FFCZ_ZSTD_CHUNKED, FFCZ_ZSTD_NONE = 0, 1, 2
 FFCZ_FORM_FUSED, FFCZ_FORM_PLAIN = 0, 1
 FFCZ_DFT_SIMT, FFCZ_DFT_TENSOR = 0, 1
+FFCZ_STAGING_REGISTERS, FFCZ_STAGING_TMA, FFCZ_STAGING_AUTO = 0, 1, 2
 FFCZ_ERR_INVALID, FFCZ_ERR_CUDA, FFCZ_ERR_UNSUPPORTED, FFCZ_ERR_NOT_INITIALIZED = -1, -2, -3, -4
 FFCZ_ERR_ZSTD, FFCZ_ERR_CAPACITY, FFCZ_ERR_CODE_TOO_LONG, FFCZ_ERR_EMPTY, FFCZ_ERR_IO = -5, -6, -7, -8, -9
 ERRORS = {-1: "INVALID", -2: "CUDA", -3: "UNSUPPORTED", -4: "NOT_INITIALIZED", -5: "ZSTD",
@@ -79,6 +80,8 @@ SIGNATURES = {
     "ffcz_solver_set_pack_mode": [_p, _i],
     "ffcz_solver_set_form": [_p, _i],
     "ffcz_solver_set_dft_stages": [_p, _i],
+    "ffcz_solver_set_staging": [_p, _i],
+    "ffcz_solver_get_tuning": [_p, _p, _p],
     "ffcz_init_all_abs": [_p, _p, _d, _d],
     "ffcz_init_all_abs_device": [_p, _p, _d, _d],
     "ffcz_solve_all_abs": [_p, _p, _i, _d],
@@ -257,6 +260,22 @@ class ProjectionSolver:
         strided passes of length 256/512 as tensor-core DFT matrix products)."""
         _check(lib().ffcz_solver_set_dft_stages(self._h, int(stages)))
 
+    def set_staging(self, staging: int) -> None:
+        """FFCZ_STAGING_REGISTERS, FFCZ_STAGING_TMA (persistent strided passes
+        fed by tensor-map copies issued ahead; identical results) or
+        FFCZ_STAGING_AUTO (the autotuner picks per axis)."""
+        _check(lib().ffcz_solver_set_staging(self._h, int(staging)))
+
+    def tuning(self) -> dict:
+        """Current tile choice per pass ({"z"|"y"|"x": (variant, staged)})
+        and the autotuner's last timings."""
+        ch = np.zeros(3, np.int32)
+        ms = np.zeros(10)
+        _check(lib().ffcz_solver_get_tuning(self._h, _np_ptr(ch), _np_ptr(ms)))
+        return {"choice": {k: (int(ch[i]) & 1, bool(int(ch[i]) & 2)) for i, k in enumerate("zyx")},
+                "ms": {"z": (ms[0], ms[1]), "y": (ms[2], ms[3]), "x": (ms[4], ms[5]),
+                       "y_tma": (ms[6], ms[7]), "x_tma": (ms[8], ms[9])}}
+
     # -- reference API -------------------------------------------------------
     def _host(self, a) -> np.ndarray:
         a = np.ascontiguousarray(a, dtype=self.dtype).reshape(-1)
@@ -313,11 +332,13 @@ class ProjectionSolver:
                                            float(delta_ptw), float(spatial_epsilon), idx.size))
 
     def autotune(self, reps: int = 5) -> dict:
-        """Keeps the faster of two tile widths per pass (results unchanged);
-        returns {pass: (default ms, alternative ms)} (0 = no alternative)."""
+        """Keeps the fastest of two tile widths per pass, and for the FP32
+        strided passes of register or TMA staging (results unchanged);
+        returns {pass: (default ms, alternative ms)} with the staged strided
+        passes as "y_tma" / "x_tma" (0 = not timed)."""
         ms = np.zeros(6)
         _check(lib().ffcz_solver_autotune(self._h, int(reps), _np_ptr(ms)))
-        return {"z": (ms[0], ms[1]), "y": (ms[2], ms[3]), "x": (ms[4], ms[5])}
+        return self.tuning()["ms"]
 
     def verify_bounds(self) -> tuple[float, float]:
         """(max |e|, max over the half spectrum of max(|Re|, |Im|) of e's R2C),

@@ -21,7 +21,7 @@ CSRC = PKG / "csrc"
 OUT = Path(os.environ.get("FFCZ_BUILD_DIR", str(PKG / "_build")))
 EXTRA = os.environ.get("FFCZ_NVCC_FLAGS", "").split()
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-LIB_SOURCES = ["solver.cu", "static_kernels.cu", "static_kernels_fc.cu", "static_kernels_tc.cu", "static_kernels_f64.cu", "static_kernels_f64s.cu", "huffman.cu", "decode.cu", "base.cu", "legacy_kernels.cu", "noalloc.cu", "fft_plan.cpp",
+LIB_SOURCES = ["solver.cu", "static_kernels.cu", "static_kernels_fc.cu", "static_kernels_tc.cu", "static_kernels_pipe.cu", "static_kernels_f64.cu", "static_kernels_f64s.cu", "huffman.cu", "decode.cu", "base.cu", "legacy_kernels.cu", "noalloc.cu", "fft_plan.cpp",
                "huffman_host.cpp", "capi_misc.cpp", "container.cpp"]
 
 

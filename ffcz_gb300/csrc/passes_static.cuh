@@ -244,20 +244,35 @@ __device__ __forceinline__ void rstage(c2<T> (&v)[E], int t, const c2<TS> *__res
 // the minimum (z forward at 250: 100 -> 91 us, z inverse 84 -> 66 us).
 //
 // Strided passes (lanes along columns): element (pos, c) at
-// pos*P + c + pos/B.  z passes (lanes along positions): row-major with pitch
-// RP and one pad slot every B positions.  FP64 tiles keep P = TW + 1 and
-// B = 16 for z.
-__host__ __device__ constexpr int sl_p(int L, int TW, int es) {
-  return es != 4 ? TW + 1
-       : mx_list(L) ? (((L == 500 || L == 900) && TW == 8) ? 12 : ((L == 1800 || L == 1000) && TW == 4) ? 6 : TW + 1)
-       : TW + 1;
+// pos*P + c + (pos/B)*TW, i.e. rows of P slots with one extra row of TW
+// slots after every B positions (B = 0: none).  The FP32 tiles take P = TW
+// and the B for which a bank model of every stage exchange of the length's
+// forward and inverse stage lists (64-bit accesses, a half-warp's distinct
+// words per bank) reaches or nears the minimum wavefront count; tiles of 16
+// columns are conflict-free dense.  Against the earlier P = TW + 1 layouts
+// the modelled wavefronts per warp and tile fall, e.g. for the fused
+// 512-point pass of 8 columns from 224 to the minimum 128 (the profile of
+// that kernel counted 227 with 42% bank conflicts), for the plain 512-point
+// passes of 8 columns from 512 to 288, for 1024 from 480 to 288, for 500
+// from 296 to 176 and for 1800 from 840 to 568.  z passes (lanes along
+// positions): row-major with pitch RP and one pad slot every B positions.
+// FP64 tiles keep P = TW + 1, B = 0 (strided) and B = 16 (z).
+// cap: the stage-list family (17: the plain 512-point passes' [16,16,2]).
+__host__ __device__ constexpr int sl_p(int L, int TW, int es, int cap) { return es != 4 ? TW + 1 : TW; }
+__host__ __device__ constexpr int sl_b(int L, int TW, int es, int cap) {
+  return (es != 4 || TW >= 16) ? 0
+       : L == 512 ? (cap == 17 ? 16 : 8)
+       : (L == 1024 || L == 2048 || L == 4096 || L == 400) ? 16
+       : L == 500 ? (TW == 8 ? 16 : 0)
+       : L == 1000 ? (TW == 4 ? 32 : 0)
+       : L == 1800 ? 32
+       : L == 768 ? 8
+       : L == 900 ? 2
+       : 0;
 }
-// (P = TW, B = 16/TW models better for the power-of-two tiles of 8 and fewer
-// columns but measured slower: 348 vs 284 us for the y pass at 512^3.)
-__host__ __device__ constexpr int sl_b(int L, int TW, int es) { return 0; }
 // elements of a strided tile
-__host__ __device__ constexpr int sl_size(int L, int TW, int es) {
-  return (L - 1) * sl_p(L, TW, es) + TW + (sl_b(L, TW, es) ? (L - 1) / sl_b(L, TW, es) : 0);
+__host__ __device__ constexpr int sl_size(int L, int TW, int es, int cap) {
+  return (L - 1) * sl_p(L, TW, es, cap) + TW + (sl_b(L, TW, es, cap) ? (L - 1) / sl_b(L, TW, es, cap) * TW : 0);
 }
 __host__ __device__ constexpr int zl_b(int M, int es) {
   return (es == 4 && mx_list(M))
@@ -272,9 +287,9 @@ __host__ __device__ constexpr int row_pitch(int M, int es) {
                 : M == 200 ? 218 : M == 400 ? 436 : M + M / 16 + 1)
              : M + M / 16 + 1;
 }
-template <int P, int B>
+template <int P, int B, int PAD>
 struct ColLayout {
-  static __device__ __forceinline__ int idx(int pos, int c) { return pos * P + c + (B ? pos / B : 0); }
+  static __device__ __forceinline__ int idx(int pos, int c) { return pos * P + c + (B ? (pos / B) * PAD : 0); }
 };
 template <int RP, int B>
 struct RowLayout {
@@ -350,6 +365,57 @@ __host__ __device__ constexpr int strided_minb(int es, int nt, int E) {
   return (es == 4 && nt == 256 && E == 16) ? FFCZ_MINB16 : (es == 4 && nt >= 384 && E <= 12) ? 2 : 1;
 }
 
+// Frequency projection of the modes MODE_FCI / MODE_FCIX / MODE_FC on the
+// forward result of a strided tile: thread t's values v of column c of the
+// tile (batch bb, row q, first column kz0), recording clamps in fedits,
+// hits in ca.fdirty and, for the all-abs box, the maximum |Re|, |Im| after
+// the clamp.  SPLIT (FP64 data in float-float registers): the box decided
+// in FP64.
+template <typename T, int MODE, int L, int CAP, bool SPLIT, typename V>
+__device__ __forceinline__ void tile_clamp(V (&v)[rp_elems(L, CAP)], int t, int c, long long bb, int q, int kz0,
+                                           bool live, const SArgs &s, const ClampArgs<T> &ca,
+                                           T *__restrict__ fedits, long long H) {
+  using C = std::conditional_t<SPLIT, ff, T>;
+  using VG = c2<T>;
+  constexpr int E = rp_elems(L, CAP);
+  constexpr bool ABS = MODE == MODE_FCI || MODE == MODE_FC;  // the all-abs box
+  bool hit = false;
+  T fm = T(0);  // max(|Re|, |Im|) after the all-abs clamp
+  // split FCI: |hi| below this is inside the box (0 when delta is too small
+  // for the margin to mean anything: every coefficient decides in FP64)
+  const float dlo = SPLIT ? (float)((double)ca.delta * (1.0 - 0x1p-20)) : 0.0f;
+  if (live) {
+#pragma unroll
+    for (int i = 0; i < E; ++i) {
+      const int l = last_pos<L, -1, CAP>(t, i);
+      const long long k = ((bb * L + l) * (long long)s.Q + q) * s.Hz + kz0 + c;
+      if constexpr (SPLIT) {  // the box in FP64; unclamped values keep their split form
+        // hi is within 2^-23 of the value: well inside the box, nothing to
+        // decide in FP64 (the pointwise box always decides in FP64)
+        if (ABS && fabsf(v[i].x.hi) < dlo && fabsf(v[i].y.hi) < dlo) continue;
+        const VG g = cvt<T>(v[i]);
+        VG h;
+        if (ABS) {
+          h = freq_clamp<T>(g, ca.delta, fedits, k, H, hit);
+        } else {
+          const long long pad = (bb * L + l) * s.Wtot + (long long)q * s.Hzp + kz0 + c;
+          h = freq_project<T>(g, ca, fedits, k, pad, H, hit);
+        }
+        if (h.x != g.x) v[i].x = C((double)h.x);
+        if (h.y != g.y) v[i].y = C((double)h.y);
+      } else if (ABS) {
+        v[i] = freq_clamp<T>(v[i], ca.delta, fedits, k, H, hit);
+        fm = fmax(fm, fmax(fabs((T)v[i].x), fabs((T)v[i].y)));
+      } else {
+        const long long pad = (bb * L + l) * s.Wtot + (long long)q * s.Hzp + kz0 + c;
+        v[i] = freq_project<T>(v[i], ca, fedits, k, pad, H, hit);
+      }
+    }
+  }
+  mark_dirty(ca.fdirty, hit);
+  if constexpr (ABS && !SPLIT) record_fmax(ca.fmax, fm);
+}
+
 // ---------------------------------------------------------------------------
 // Strided C2C pass.  Block = TC threads per column x TW columns (c fastest
 // across lanes, so each row access is TW contiguous complex values).
@@ -363,7 +429,7 @@ __global__ void __launch_bounds__((L / rp_elems(L, CAP)) << LGTW,
   using V = c2<C>;
   using VG = c2<T>;
   constexpr int E = rp_elems(L, CAP), TW = 1 << LGTW;
-  using LY = ColLayout<sl_p(L, TW, sizeof(T)), sl_b(L, TW, sizeof(T))>;
+  using LY = ColLayout<sl_p(L, TW, sizeof(T), CAP), sl_b(L, TW, sizeof(T), CAP), TW>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   V *buf = reinterpret_cast<V *>(smem_raw);
   const int c = threadIdx.x & (TW - 1);
@@ -384,42 +450,7 @@ __global__ void __launch_bounds__((L / rp_elems(L, CAP)) << LGTW,
     v[i] = live ? cvt<C>(src[(long long)first_pos<L, D0, CAP>(t, i) * s.Wtot]) : mkc<C>(C(0), C(0));
   RRun<C, D0, L, LY, 0, CAP, C>::run(v, buf, t, c, p);  // split: p.tw is the float-float table
   if (MODE == MODE_FCI || MODE == MODE_FCIX || MODE == MODE_FC) {
-    constexpr bool ABS = MODE == MODE_FCI || MODE == MODE_FC;  // the all-abs box
-    bool hit = false;
-    T fm = T(0);  // max(|Re|, |Im|) after the all-abs clamp
-    // split FCI: |hi| below this is inside the box (0 when delta is too small
-    // for the margin to mean anything: every coefficient decides in FP64)
-    const float dlo = SPLIT ? (float)((double)ca.delta * (1.0 - 0x1p-20)) : 0.0f;
-    if (live) {
-#pragma unroll
-      for (int i = 0; i < E; ++i) {
-        const int l = last_pos<L, -1, CAP>(t, i);
-        const long long k = ((bb * L + l) * (long long)s.Q + q) * s.Hz + kz0 + c;
-        if constexpr (SPLIT) {  // the box in FP64; unclamped values keep their split form
-          // hi is within 2^-23 of the value: well inside the box, nothing to
-          // decide in FP64 (the pointwise box always decides in FP64)
-          if (ABS && fabsf(v[i].x.hi) < dlo && fabsf(v[i].y.hi) < dlo) continue;
-          const VG g = cvt<T>(v[i]);
-          VG h;
-          if (ABS) {
-            h = freq_clamp<T>(g, ca.delta, fedits, k, H, hit);
-          } else {
-            const long long pad = (bb * L + l) * s.Wtot + (long long)q * s.Hzp + kz0 + c;
-            h = freq_project<T>(g, ca, fedits, k, pad, H, hit);
-          }
-          if (h.x != g.x) v[i].x = C((double)h.x);
-          if (h.y != g.y) v[i].y = C((double)h.y);
-        } else if (ABS) {
-          v[i] = freq_clamp<T>(v[i], ca.delta, fedits, k, H, hit);
-          if constexpr (!SPLIT) fm = fmax(fm, fmax(fabs((T)v[i].x), fabs((T)v[i].y)));
-        } else {
-          const long long pad = (bb * L + l) * s.Wtot + (long long)q * s.Hzp + kz0 + c;
-          v[i] = freq_project<T>(v[i], ca, fedits, k, pad, H, hit);
-        }
-      }
-    }
-    mark_dirty(ca.fdirty, hit);
-    if constexpr (ABS && !SPLIT) record_fmax(ca.fmax, fm);
+    tile_clamp<T, MODE, L, CAP, SPLIT>(v, t, c, bb, q, kz0, live, s, ca, fedits, H);
     // The inverse's first stage reads the positions the forward's last
     // stage wrote, so the same registers continue.  A barrier separates the
     // forward's last shared reads from the inverse's first shared writes.

@@ -10,6 +10,7 @@
 #include <memory>
 #include <vector>
 
+#include <cudaTypedefs.h>
 #include <nvtx3/nvToolsExt.h>
 
 #include "extract.cuh"
@@ -84,6 +85,16 @@ struct ffcz_solver {
   SArgs stc[2]{};
   Launch ltc[2]{};
   AxisPlan ptc[2]{};
+  // TMA-staged strided passes (FP32 compile-time axes, passes_pipe.cuh):
+  // requested staging (FFCZ_STAGING_*), whether each strided axis (0 y, 1 x)
+  // runs them, their kernel, persistent grid and tile count per mode, and
+  // the tensor map of each stage-list family (0 plain, 1 fused) of an axis
+  int staging = FFCZ_STAGING_AUTO;
+  int pipe_on[2] = {0, 0};
+  void *kp[2][kStridedModes] = {};
+  Launch lp[2][kStridedModes]{};
+  long long pt[2][kStridedModes] = {};
+  CUtensorMap tmap[2][2];
   // device arrays
   void *d_x = nullptr, *d_e = nullptr, *d_spec = nullptr;
   void *d_fedits = nullptr, *d_sedits = nullptr;
@@ -126,7 +137,7 @@ struct ffcz_solver {
   int z_ept = 0, y_ept = 0, x_ept = 0;  // values per thread of the runtime-planned tiles
   int zvar = 0, yvar = 0, xvar = 0;     // tile variant of each compile-time pass
   int split = 0;                        // FP64: float-float pass kernels where they exist
-  double tune_ms[6] = {};               // autotuner: (default, alternative) ms of z, y, x
+  double tune_ms[10] = {};  // autotuner: (default, alternative) ms of z, y, x; staged (default, alternative) of y, x
   int kernel_gen = 0;                   // bumped when the autotuner swaps kernels
   // parameters
   double eps = 0, delta = 0;
@@ -313,6 +324,85 @@ bool apply_static_strided(ffcz_solver *s, int axis, int var) {
   }
   (axis == 0 ? s->static_y : s->static_x) = 1;
   (axis == 0 ? s->yvar : s->xvar) = var;
+  s->pipe_on[axis] = 0;  // staged kernels belong to a tile variant: set up again
+  return true;
+}
+
+// cuTensorMapEncodeTiled from the driver, looked up once through the
+// runtime (the library does not link libcuda); null where unavailable.
+static PFN_cuTensorMapEncodeTiled_v12000 tmap_encoder() {
+  static const PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      p = nullptr;
+    return (PFN_cuTensorMapEncodeTiled_v12000)p;
+  }();
+  return fn;
+}
+
+// Staged kernels of strided axis `axis` (0 y, 1 x) for its current tile
+// variant: each mode's kernel (the tile of the register kernel it replaces),
+// a tensor map per stage-list family over the padded spectrum d_spec, and a
+// persistent grid of the resident blocks (at most one per tile).  False,
+// with nothing changed, where the axis or a mode has no staged kernel.
+bool setup_pipe(ffcz_solver *s, int axis) {
+  if (s->dtype != FFCZ_F32 || s->split || !s->d_spec) return false;
+  if (!(axis == 0 ? (s->has_y && s->static_y) : (s->has_x && s->static_x))) return false;
+  const PFN_cuTensorMapEncodeTiled_v12000 enc = tmap_encoder();
+  if (!enc) return false;
+  const int L = axis == 0 ? (int)s->ny : (int)s->nx;
+  const int Q = axis == 0 ? 1 : (int)s->ny;
+  const long long B = axis == 0 ? (long long)s->nx : 1;
+  const int var = axis == 0 ? s->yvar : s->xvar;
+  void **k = axis == 0 ? s->ky : s->kx;
+  int sms = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device) != cudaSuccess || sms < 1) return false;
+  void *kp[kStridedModes] = {};
+  Launch lp[kStridedModes]{};
+  long long pt[kStridedModes] = {};
+  CUtensorMap tm[2];
+  for (int fam = 0; fam < 2; ++fam) {
+    const SArgs &sa = fam ? (axis == 0 ? s->syf : s->sxf) : (axis == 0 ? s->sy : s->sx);
+    const Launch &ln = fam ? (axis == 0 ? s->lyf : s->lxf) : (axis == 0 ? s->ly : s->lx);
+    const int modes[3] = {fam ? MODE_FCI : MODE_FWD, fam ? MODE_FCIX : MODE_INV, fam ? -1 : MODE_FC};
+    for (int m : modes) {
+      if (m < 0 || (m == MODE_FC && !k[MODE_FC])) continue;  // no plain-form clamp pass here
+      PipeFn fn = nullptr;
+      StaticGeom g;
+      int nbuf = 0, nb = 0;
+      if (!pipe_strided(L, m, fn, g, var, nbuf) || g.TW != sa.TW || g.threads != ln.threads) return false;
+      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, (const void *)fn, g.threads, g.smem) != cudaSuccess ||
+          nb < 1)
+        return false;
+      kp[m] = (void *)fn;
+      pt[m] = B * Q * (long long)sa.tpq;
+      lp[m].threads = g.threads;
+      lp[m].smem = g.smem;
+      lp[m].grid = (unsigned)std::min<long long>(pt[m], (long long)nb * sms);
+    }
+    // (kz: Hz, q: Q, position: L, batch: B), 8-byte elements; columns past
+    // Hz read as zeros
+    const cuuint64_t dims[4] = {(cuuint64_t)s->Hz, (cuuint64_t)Q, (cuuint64_t)L, (cuuint64_t)B};
+    const cuuint64_t strides[3] = {(cuuint64_t)s->Hzp * 8, (cuuint64_t)sa.Wtot * 8, (cuuint64_t)L * sa.Wtot * 8};
+    const int bp = pipe_box_positions(L, sa.TW);
+    if (bp <= 0) return false;
+    const cuuint32_t box[4] = {(cuuint32_t)sa.TW, 1, (cuuint32_t)bp, 1};
+    const cuuint32_t estr[4] = {1, 1, 1, 1};
+    if (enc(&tm[fam], CU_TENSOR_MAP_DATA_TYPE_INT64, 4, s->d_spec, dims, strides, box, estr,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+      return false;
+  }
+  for (int m = 0; m < kStridedModes; ++m) {
+    s->kp[axis][m] = kp[m];
+    s->lp[axis][m] = lp[m];
+    s->pt[axis][m] = pt[m];
+  }
+  s->tmap[axis][0] = tm[0];
+  s->tmap[axis][1] = tm[1];
   return true;
 }
 
@@ -497,6 +587,28 @@ ClampArgs<T> clamp_args(const ffcz_solver *s) {
   return ca;
 }
 
+// One strided pass of axis 0 (y) or 1 (x) in `mode` with the register
+// kernel of the plain (fused = false) or fused family, or its TMA-staged
+// variant where the axis runs those (they are set up for d_spec only).
+template <typename T>
+void strided_kernel(ffcz_solver *s, cudaStream_t st, int axis, int mode, bool fused, const ClampArgs<T> &ca,
+                    c2<T> *spec) {
+  const long long H = (long long)s->H;
+  const SArgs &sa = fused ? (axis == 0 ? s->syf : s->sxf) : (axis == 0 ? s->sy : s->sx);
+  const AxisPlan &pl = fused ? (axis == 0 ? s->pyf : s->pxf) : (axis == 0 ? s->py : s->px);
+  if constexpr (sizeof(T) == 4) {
+    if (s->pipe_on[axis] && s->kp[axis][mode] && (void *)spec == s->d_spec) {
+      const Launch &lp = s->lp[axis][mode];
+      ((PipeFn)s->kp[axis][mode])<<<lp.grid, lp.threads, lp.smem, st>>>(
+          s->tmap[axis][fused ? 1 : 0], spec, sa, pl, ca, tp<T>(s->d_fedits), H, s->pt[axis][mode], &s->d_ctl->err);
+      return;
+    }
+  }
+  void *k = (axis == 0 ? s->ky : s->kx)[mode];
+  const Launch &ln = fused ? (axis == 0 ? s->lyf : s->lxf) : (axis == 0 ? s->ly : s->lx);
+  ((StridedFn<T>)k)<<<ln.grid, ln.threads, ln.smem, st>>>(spec, sa, pl, ca, tp<T>(s->d_fedits), H);
+}
+
 // One strided pass of axis 0 (y) or 1 (x) in `mode`: the tensor-core
 // kernel where one is selected for this axis and mode (all-abs), else the
 // plain (fused = false) or fused family's kernel, tile and plan.
@@ -510,11 +622,7 @@ void strided_pass(ffcz_solver *s, cudaStream_t st, int axis, int mode, bool fuse
                                                                             tp<T>(s->d_fedits), H);
     return;
   }
-  void *k = (axis == 0 ? s->ky : s->kx)[mode];
-  const Launch &ln = fused ? (axis == 0 ? s->lyf : s->lxf) : (axis == 0 ? s->ly : s->lx);
-  const SArgs &sa = fused ? (axis == 0 ? s->syf : s->sxf) : (axis == 0 ? s->sy : s->sx);
-  const AxisPlan &pl = fused ? (axis == 0 ? s->pyf : s->pxf) : (axis == 0 ? s->py : s->px);
-  ((StridedFn<T>)k)<<<ln.grid, ln.threads, ln.smem, st>>>(spec, sa, pl, ca, tp<T>(s->d_fedits), H);
+  strided_kernel<T>(s, st, axis, mode, fused, ca, spec);
 }
 
 // One iteration: [prologue + R2C z] [y fwd] [fused fwd/clamp/inv] [y inv]
@@ -720,6 +828,7 @@ int project(ffcz_solver *s, int pro, const void *a, const void *b, int max_iter,
   FFCZ_CUDA(cudaMemcpyAsync(s->h_ctl, s->d_ctl, sizeof(LoopCtl), cudaMemcpyDeviceToHost, s->stream));
   FFCZ_CUDA(cudaStreamSynchronize(s->stream));
   s->launches = 1 + (long long)s->h_ctl->iterations * s->kernels_per_iter + 1;
+  if (s->h_ctl->err) return fail(FFCZ_ERR_CUDA, "a TMA-staged pass gave up waiting for its tile copies");
   return FFCZ_OK;
 }
 
@@ -1107,7 +1216,7 @@ int autotune(ffcz_solver *s, int reps, double *ms6) {
     cudaEventElapsedTime(&ms, e0, e1);
     return (double)ms / reps;
   };
-  double t[6] = {0, 0, 0, 0, 0, 0};
+  double t[10] = {};
   auto zrun = [&]() {
     ((ZfwdFn<T>)s->kzf[PRO_PLAIN])<<<s->lz_f.grid, s->lz_f.threads, s->lz_f.smem, st>>>(
         (const T *)s->d_x, nullptr, tp<T>(s->d_sedits), (T)s->eps, spec, s->za, s->pz, post);
@@ -1132,17 +1241,33 @@ int autotune(ffcz_solver *s, int reps, double *ms6) {
     const AxisPlan &plf = axis == 0 ? s->pyf : s->pxf;
     auto run = [&]() {
       if (fused_here) {
-        ((StridedFn<T>)k[MODE_FCI])<<<lnf.grid, lnf.threads, lnf.smem, st>>>(spec, saf, plf, ca, tp<T>(s->d_fedits),
-                                                                             H);
+        strided_kernel<T>(s, st, axis, MODE_FCI, true, ca, spec);
       } else {
-        ((StridedFn<T>)k[MODE_FWD])<<<ln.grid, ln.threads, ln.smem, st>>>(spec, sa, pl, ca, tp<T>(s->d_fedits), H);
-        ((StridedFn<T>)k[MODE_INV])<<<ln.grid, ln.threads, ln.smem, st>>>(spec, sa, pl, ca, tp<T>(s->d_fedits), H);
+        strided_kernel<T>(s, st, axis, MODE_FWD, false, ca, spec);
+        strided_kernel<T>(s, st, axis, MODE_INV, false, ca, spec);
       }
     };
-    double *tt = t + 2 + 2 * axis;
-    for (int var = 0; var < 2; ++var)
-      if (apply_static_strided<T>(s, axis, var)) tt[var] = timed(run);
-    apply_static_strided<T>(s, axis, (tt[1] > 0 && tt[1] < tt[0]) ? 1 : 0);
+    // candidates: register kernels of tile variants 0 / 1 (tt), their
+    // TMA-staged versions (tq), as the staging setting allows
+    double *tt = t + 2 + 2 * axis, *tq = t + 6 + 2 * axis;
+    const bool reg = s->staging != FFCZ_STAGING_TMA;
+    const bool stg = sizeof(T) == 4 && s->staging != FFCZ_STAGING_REGISTERS;
+    for (int var = 0; var < 2; ++var) {
+      if (!apply_static_strided<T>(s, axis, var)) continue;
+      if (reg) tt[var] = timed(run);
+      if (stg && setup_pipe(s, axis)) {
+        s->pipe_on[axis] = 1;
+        tq[var] = timed(run);
+        s->pipe_on[axis] = 0;
+      }
+    }
+    int best = -1;
+    for (int c = 0; c < 4; ++c) {
+      const double v = c < 2 ? tt[c] : tq[c - 2];
+      if (v > 0 && (best < 0 || v < (best < 2 ? tt[best] : tq[best - 2]))) best = c;
+    }
+    apply_static_strided<T>(s, axis, best > 0 ? (best & 1) : 0);
+    if (best >= 2 && setup_pipe(s, axis)) s->pipe_on[axis] = 1;
   }
   FFCZ_CUDA(cudaGetLastError());
   for (double v : t)
@@ -1155,7 +1280,7 @@ int autotune(ffcz_solver *s, int reps, double *ms6) {
   // the cached loop graphs hold the previous kernels
   for (LoopGraph &g : s->lg) g.reset();
   ++s->kernel_gen;
-  for (int i = 0; i < 6; ++i) s->tune_ms[i] = t[i];
+  for (int i = 0; i < 10; ++i) s->tune_ms[i] = t[i];
   if (ms6)
     for (int i = 0; i < 6; ++i) ms6[i] = t[i];
   return FFCZ_OK;
@@ -1524,6 +1649,36 @@ int ffcz_solver_set_dft_stages(ffcz_solver *s, int stages) {
   }
   if (!axes) return fail(FFCZ_ERR_UNSUPPORTED, "no strided axis of length 256 or 512");
   s->dft = FFCZ_DFT_TENSOR;
+  return FFCZ_OK;
+}
+
+int ffcz_solver_set_staging(ffcz_solver *s, int staging) {
+  FFCZ_TRY(check_solver(s));
+  if (staging != FFCZ_STAGING_REGISTERS && staging != FFCZ_STAGING_TMA && staging != FFCZ_STAGING_AUTO)
+    return fail(FFCZ_ERR_INVALID, "unknown staging");
+  FFCZ_CUDA(cudaStreamSynchronize(s->stream));
+  for (LoopGraph &g : s->lg) g.reset();  // the cached loops hold the previous kernels
+  ++s->kernel_gen;
+  s->staging = staging;
+  int on = 0;
+  for (int a = 0; a < 2; ++a) {
+    s->pipe_on[a] = 0;
+    if (staging == FFCZ_STAGING_TMA && setup_pipe(s, a)) on += (s->pipe_on[a] = 1);
+  }
+  if (staging == FFCZ_STAGING_TMA && !on)
+    return fail(FFCZ_ERR_UNSUPPORTED, "no strided axis with a TMA-staged kernel (FP32 compile-time lengths)");
+  return FFCZ_OK;
+}
+
+int ffcz_solver_get_tuning(ffcz_solver *s, int *choice, double *ms10) {
+  FFCZ_TRY(check_solver(s));
+  if (choice) {
+    choice[0] = s->zvar;
+    choice[1] = s->yvar | (s->pipe_on[0] ? 2 : 0);
+    choice[2] = s->xvar | (s->pipe_on[1] ? 2 : 0);
+  }
+  if (ms10)
+    for (int i = 0; i < 10; ++i) ms10[i] = s->tune_ms[i];
   return FFCZ_OK;
 }
 

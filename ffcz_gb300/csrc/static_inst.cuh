@@ -89,7 +89,7 @@ bool strided_for_family(int mode, StridedFn<T> &fn, StaticGeom &g) {
   }
   g.TW = C::TW;
   g.threads = C::NT;
-  g.smem = (size_t)sl_size(L, C::TW, sizeof(T)) * sizeof(c2<T>);
+  g.smem = (size_t)sl_size(L, C::TW, sizeof(T), CAP) * sizeof(c2<T>);
   return set_smem(fn, g.smem) == FFCZ_OK;
 }
 template <typename T, int L, int VAR>
@@ -100,7 +100,7 @@ bool strided_fc_for(StridedFn<T> &fn, StaticGeom &g) {
   fn = ks_strided<T, MODE_FC, L, C::LGTW, CAP, false>;
   g.TW = C::TW;
   g.threads = C::NT;
-  g.smem = (size_t)sl_size(L, C::TW, sizeof(T)) * sizeof(c2<T>);
+  g.smem = (size_t)sl_size(L, C::TW, sizeof(T), CAP) * sizeof(c2<T>);
   return set_smem(fn, g.smem) == FFCZ_OK;
 }
 template <typename T, int L, int VAR, bool SPLIT = false>

@@ -2,6 +2,8 @@
 // (passes_static.cuh) and construction of their twiddle tables.
 #pragma once
 
+#include <cuda.h>
+
 #include <complex>
 #include <vector>
 
@@ -51,5 +53,17 @@ template <typename T> bool static_strided_fc(int L, StridedFn<T> &fn, StaticGeom
 // (passes_tc.cuh), L = 256 or 512, modes MODE_FWD, MODE_INV, MODE_FC and
 // MODE_FCI, all on the plain stage list (static_plain_cap); false otherwise.
 bool tc_strided(int L, int mode, StridedFn<float> &fn, StaticGeom &g);
+
+// TMA-staged persistent variant of an FP32 strided pass (passes_pipe.cuh):
+// the tile geometry of the register kernel of the same mode and variant,
+// tiles read through a rank-4 tensor map over the padded spectrum
+// (kz: Hz, q: Q, position: L, batch: B; 8-byte elements), nbuf tile slots
+// per block; grid = resident blocks, at most one per tile.  False where
+// no such kernel exists.
+using PipeFn = void (*)(const CUtensorMap, c2<float> *, SArgs, AxisPlan, ClampArgs<float>, float *, long long,
+                        long long, int *);
+bool pipe_strided(int L, int mode, PipeFn &fn, StaticGeom &g, int var, int &nbuf);
+// Positions per box of that tensor map for length L and tile width TW.
+int pipe_box_positions(int L, int TW);
 
 }  // namespace ffcz

@@ -115,6 +115,30 @@ int ffcz_solver_set_form(ffcz_solver *s, int form);
 #define FFCZ_DFT_TENSOR 1
 int ffcz_solver_set_dft_stages(ffcz_solver *s, int stages);
 
+/* How the FP32 strided (y, x) passes of compile-time lengths get their tiles
+ * (no counterpart in the reference):
+ *   FFCZ_STAGING_REGISTERS: each block loads its tile straight into
+ *     registers (one tile per block, nothing in flight while it computes);
+ *   FFCZ_STAGING_TMA: persistent blocks whose next tiles arrive in shared
+ *     memory by tensor-map (TMA) copies issued ahead while the current tile
+ *     is transformed; same arithmetic in the same order, identical results;
+ *   FFCZ_STAGING_AUTO (default): registers until ffcz_solver_autotune,
+ *     which times both per axis and keeps the faster.
+ * FFCZ_ERR_UNSUPPORTED for TMA when no strided axis has a staged kernel
+ * (FP64 solvers, lengths without compile-time kernels).  A staged pass that
+ * waits about two seconds for a tile without it arriving gives up, and the
+ * solve returns FFCZ_ERR_CUDA. */
+#define FFCZ_STAGING_REGISTERS 0
+#define FFCZ_STAGING_TMA 1
+#define FFCZ_STAGING_AUTO 2
+int ffcz_solver_set_staging(ffcz_solver *s, int staging);
+/* Tile choices of the solver: choice[3] (may be NULL) receives, per pass
+ * (z, y, x), the tile variant (bit 0) and whether the pass runs TMA-staged
+ * (bit 1); ms10 (may be NULL) the autotuner's last timings: (default,
+ * alternative) ms of z, y and x with register staging, then (default,
+ * alternative) ms of y and x TMA-staged; 0 where not timed. */
+int ffcz_solver_get_tuning(ffcz_solver *s, int *choice, double *ms10);
+
 /* initialize_all_abs(h_orig, eps, delta) -- impl:639-668.  x is a host
  * array of Nx*Ny*Nz elements of the solver's dtype; eps and delta are
  * converted to the solver's dtype. */
