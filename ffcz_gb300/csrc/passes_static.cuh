@@ -287,14 +287,20 @@ __host__ __device__ constexpr int row_pitch(int M, int es) {
                 : M == 200 ? 218 : M == 400 ? 436 : M + M / 16 + 1)
              : M + M / 16 + 1;
 }
+// (Positions are never negative: unsigned division by the compile-time B
+// is a plain shift or multiply-high, without the signed rounding fix-up.)
 template <int P, int B, int PAD>
 struct ColLayout {
-  static __device__ __forceinline__ int idx(int pos, int c) { return pos * P + c + (B ? (pos / B) * PAD : 0); }
+  static __device__ __forceinline__ int idx(int pos, int c) {
+    return pos * P + c + (B ? (int)((unsigned)pos / (unsigned)B) * PAD : 0);
+  }
 };
 template <int RP, int B>
 struct RowLayout {
   static_assert(B == 0 || RP > 0, "pitch");
-  static __device__ __forceinline__ int idx(int pos, int c) { return c * RP + pos + (B ? pos / B : 0); }
+  static __device__ __forceinline__ int idx(int pos, int c) {
+    return c * RP + pos + (B ? (int)((unsigned)pos / (unsigned)B) : 0);
+  }
 };
 
 template <int L, int E, int R>
@@ -303,8 +309,8 @@ __device__ __forceinline__ int in_pos(int t, int m, int r) {
 }
 template <int L, int E, int R, int NS>
 __device__ __forceinline__ int out_pos(int t, int m, int r) {
-  const int j = t + m * (L / E);
-  return (j / NS) * NS * R + j % NS + r * NS;
+  const unsigned j = (unsigned)(t + m * (L / E));
+  return (int)((j / NS) * NS * R + j % NS + r * NS);
 }
 
 // Runs stages S..end of direction DIR; v holds stage S's inputs.  Between
@@ -384,7 +390,24 @@ __device__ __forceinline__ void tile_clamp(V (&v)[rp_elems(L, CAP)], int t, int 
   // split FCI: |hi| below this is inside the box (0 when delta is too small
   // for the margin to mean anything: every coefficient decides in FP64)
   const float dlo = SPLIT ? (float)((double)ca.delta * (1.0 - 0x1p-20)) : 0.0f;
-  if (live) {
+  bool any = live;
+  if constexpr (ABS && !SPLIT) {
+    // Branch-free look first: a thread none of whose coefficients leaves the
+    // box (|Re|, |Im| <= delta; NaN compares false, as in the clamp) has
+    // nothing to clamp and its maximum is that of its values; the others
+    // run the per-coefficient clamp below.
+    any = false;
+    if (live) {
+#pragma unroll
+      for (int i = 0; i < E; ++i) {
+        const T ax = fabs((T)v[i].x), ay = fabs((T)v[i].y);
+        any |= (ax > ca.delta) | (ay > ca.delta);
+        fm = fmax(fm, fmax(ax, ay));
+      }
+    }
+    if (any) fm = T(0);
+  }
+  if (any) {
 #pragma unroll
     for (int i = 0; i < E; ++i) {
       const int l = last_pos<L, -1, CAP>(t, i);
