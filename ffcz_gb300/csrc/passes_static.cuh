@@ -291,26 +291,46 @@ __host__ __device__ constexpr int row_pitch(int M, int es) {
 // is a plain shift or multiply-high, without the signed rounding fix-up.)
 template <int P, int B, int PAD>
 struct ColLayout {
-  static __device__ __forceinline__ int idx(int pos, int c) {
+  static __host__ __device__ __forceinline__ constexpr int idx(int pos, int c) {
     return pos * P + c + (B ? (int)((unsigned)pos / (unsigned)B) * PAD : 0);
   }
 };
 template <int RP, int B>
 struct RowLayout {
   static_assert(B == 0 || RP > 0, "pitch");
-  static __device__ __forceinline__ int idx(int pos, int c) {
+  static __host__ __device__ __forceinline__ constexpr int idx(int pos, int c) {
     return c * RP + pos + (B ? (int)((unsigned)pos / (unsigned)B) : 0);
   }
 };
 
 template <int L, int E, int R>
-__device__ __forceinline__ int in_pos(int t, int m, int r) {
+__host__ __device__ __forceinline__ constexpr int in_pos(int t, int m, int r) {
   return t + m * (L / E) + r * (L / R);
 }
 template <int L, int E, int R, int NS>
-__device__ __forceinline__ int out_pos(int t, int m, int r) {
+__host__ __device__ __forceinline__ constexpr int out_pos(int t, int m, int r) {
   const unsigned j = (unsigned)(t + m * (L / E));
   return (int)((j / NS) * NS * R + j % NS + r * NS);
+}
+
+// Shared-memory offset of slot (m, r) of a thread's exchange accesses from
+// its slot (0, 0): the writes of a stage of radix R and span NS (OUT), or
+// the reads of a stage of radix R.  Layouts add the column (row) linearly,
+// so the offset does not depend on it.
+template <typename LY, int L, int E, int R, int NS, bool OUT>
+__host__ __device__ constexpr int xoff(int t, int m, int r) {
+  return OUT ? LY::idx(out_pos<L, E, R, NS>(t, m, r), 0) - LY::idx(out_pos<L, E, R, NS>(t, 0, 0), 0)
+             : LY::idx(in_pos<L, E, R>(t, m, r), 0) - LY::idx(in_pos<L, E, R>(t, 0, 0), 0);
+}
+// True when those offsets are the same for every thread of a column (row):
+// the accesses then address one base register with compile-time offsets.
+template <typename LY, int L, int E, int R, int NS, bool OUT>
+__host__ __device__ constexpr bool xaffine() {
+  for (int t = 1; t < L / E; ++t)
+    for (int m = 0; m < E / R; ++m)
+      for (int r = 0; r < R; ++r)
+        if (xoff<LY, L, E, R, NS, OUT>(t, m, r) != xoff<LY, L, E, R, NS, OUT>(0, m, r)) return false;
+  return true;
 }
 
 // Runs stages S..end of direction DIR; v holds stage S's inputs.  Between
@@ -327,15 +347,31 @@ struct RRun {
       rstage<T, DIR, R, LG, L, E, tw_paired(CAP, R), TS>(v, t, tw);
       if constexpr (S + 1 < rp_nst(L, CAP)) {
         constexpr int R2 = rp_rad(L, DIR, S + 1, CAP);
+        if constexpr (xaffine<LY, L, E, R, LG, true>()) {
+          c2<T> *w = buf + LY::idx(out_pos<L, E, R, LG>(t, 0, 0), c);
 #pragma unroll
-        for (int m = 0; m < E / R; ++m)
+          for (int m = 0; m < E / R; ++m)
 #pragma unroll
-          for (int r = 0; r < R; ++r) buf[LY::idx(out_pos<L, E, R, LG>(t, m, r), c)] = v[m * R + r];
+            for (int r = 0; r < R; ++r) w[xoff<LY, L, E, R, LG, true>(0, m, r)] = v[m * R + r];
+        } else {
+#pragma unroll
+          for (int m = 0; m < E / R; ++m)
+#pragma unroll
+            for (int r = 0; r < R; ++r) buf[LY::idx(out_pos<L, E, R, LG>(t, m, r), c)] = v[m * R + r];
+        }
         __syncthreads();
+        if constexpr (xaffine<LY, L, E, R2, 1, false>()) {
+          const c2<T> *rd = buf + LY::idx(in_pos<L, E, R2>(t, 0, 0), c);
 #pragma unroll
-        for (int m = 0; m < E / R2; ++m)
+          for (int m = 0; m < E / R2; ++m)
 #pragma unroll
-          for (int r = 0; r < R2; ++r) v[m * R2 + r] = buf[LY::idx(in_pos<L, E, R2>(t, m, r), c)];
+            for (int r = 0; r < R2; ++r) v[m * R2 + r] = rd[xoff<LY, L, E, R2, 1, false>(0, m, r)];
+        } else {
+#pragma unroll
+          for (int m = 0; m < E / R2; ++m)
+#pragma unroll
+            for (int r = 0; r < R2; ++r) v[m * R2 + r] = buf[LY::idx(in_pos<L, E, R2>(t, m, r), c)];
+        }
         __syncthreads();
         RRun<T, DIR, L, LY, S + 1, CAP, TS>::run(v, buf, t, c, p);
       }
