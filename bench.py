@@ -91,6 +91,8 @@ def parse():
     ap.add_argument("--no-cufft-reference", action="store_true",
                     help="leave out the timing of the reference's own cuFFT build")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default tile of every pass")
+    ap.add_argument("--staging", default="auto", choices=["auto", "tma", "registers"],
+                    help="tiles of the FP32 strided passes: chosen by the autotuner, TMA-staged, or register-staged")
     ap.add_argument("--zstd-threads", type=int, default=0,
                     help="host threads of the ZSTD pool (default: every host core; 16 vs 14 threads "
                          "on a 16-core host: 2.42 vs 2.12-2.23 GB/s at 256^3)")
@@ -341,7 +343,11 @@ def run_ours(args):
         if tensor:
             s.set_dft_stages(F.FFCZ_DFT_TENSOR)
         s.set_stream(torch.cuda.current_stream())
+        if args.staging != "auto" and dt == np.float32:
+            s.set_staging(F.FFCZ_STAGING_TMA if args.staging == "tma" else F.FFCZ_STAGING_REGISTERS)
         s.set_loop_driver(F.FFCZ_LOOP_HOST if args.loop == "host" else F.FFCZ_LOOP_GRAPH)
+        if strict:  # the strict finish changes the edits: compact once, after it
+            s.set_extraction(F.FFCZ_EXTRACT_ON_DEMAND)
         s.set_profiling(True)
         s.initialize_all_abs_device(dx, fld.eps, fld.delta if delta is None else delta)
         tune = {} if args.no_autotune else s.autotune(5)
@@ -578,6 +584,8 @@ def measure_stress(F, torch, fld, dx, dxp, max_iter, strict, args, c=1.0):
     delta = synth.stress_delta(fld, c)
     with F.ProjectionSolver(*fld.shape, dtype=fld.x.dtype) as m:
         m.set_stream(torch.cuda.current_stream())
+        if strict:
+            m.set_extraction(F.FFCZ_EXTRACT_ON_DEMAND)
         m.initialize_all_abs_device(dx, fld.eps, delta)
         ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         ms = []

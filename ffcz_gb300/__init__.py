@@ -34,6 +34,7 @@ FFCZ_ZSTD_SINGLE, FFCZ_ZSTD_CHUNKED, FFCZ_ZSTD_NONE = 0, 1, 2
 FFCZ_FORM_FUSED, FFCZ_FORM_PLAIN = 0, 1
 FFCZ_DFT_SIMT, FFCZ_DFT_TENSOR = 0, 1
 FFCZ_STAGING_REGISTERS, FFCZ_STAGING_TMA, FFCZ_STAGING_AUTO = 0, 1, 2
+FFCZ_EXTRACT_EAGER, FFCZ_EXTRACT_ON_DEMAND = 0, 1
 FFCZ_ERR_INVALID, FFCZ_ERR_CUDA, FFCZ_ERR_UNSUPPORTED, FFCZ_ERR_NOT_INITIALIZED = -1, -2, -3, -4
 FFCZ_ERR_ZSTD, FFCZ_ERR_CAPACITY, FFCZ_ERR_CODE_TOO_LONG, FFCZ_ERR_EMPTY, FFCZ_ERR_IO = -5, -6, -7, -8, -9
 ERRORS = {-1: "INVALID", -2: "CUDA", -3: "UNSUPPORTED", -4: "NOT_INITIALIZED", -5: "ZSTD",
@@ -81,6 +82,7 @@ SIGNATURES = {
     "ffcz_solver_set_form": [_p, _i],
     "ffcz_solver_set_dft_stages": [_p, _i],
     "ffcz_solver_set_staging": [_p, _i],
+    "ffcz_solver_set_extraction": [_p, _i],
     "ffcz_solver_get_tuning": [_p, _p, _p],
     "ffcz_init_all_abs": [_p, _p, _d, _d],
     "ffcz_init_all_abs_device": [_p, _p, _d, _d],
@@ -265,6 +267,12 @@ class ProjectionSolver:
         fed by tensor-map copies issued ahead; identical results) or
         FFCZ_STAGING_AUTO (the autotuner picks per axis)."""
         _check(lib().ffcz_solver_set_staging(self._h, int(staging)))
+
+    def set_extraction(self, mode: int) -> None:
+        """FFCZ_EXTRACT_EAGER (compact at the end of every solve, as the
+        reference) or FFCZ_EXTRACT_ON_DEMAND (compact when the results are
+        first read or the edit arrays about to change; same results)."""
+        _check(lib().ffcz_solver_set_extraction(self._h, int(mode)))
 
     def tuning(self) -> dict:
         """Current tile choice per pass ({"z"|"y"|"x": (variant, staged)})

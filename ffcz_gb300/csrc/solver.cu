@@ -90,6 +90,10 @@ struct ffcz_solver {
   // runs them, their kernel, persistent grid and tile count per mode, and
   // the tensor map of each stage-list family (0 plain, 1 fused) of an axis
   int staging = FFCZ_STAGING_AUTO;
+  // FFCZ_EXTRACT_ON_DEMAND: a solve leaves its compaction pending; the first
+  // call that needs (or would overwrite) the compacted results runs it
+  int extract_mode = FFCZ_EXTRACT_EAGER;
+  bool extract_pending = false;
   int pipe_on[2] = {0, 0};
   void *kp[2][kStridedModes] = {};
   Launch lp[2][kStridedModes]{};
@@ -910,6 +914,7 @@ int finish_extract(ffcz_solver *s) {
     if (s->h_ctl->count[1] == 0) FFCZ_CUDA(cudaMemsetAsync(s->d_spack, 0, s->spack_bytes, s->stream));
   }
   s->extracted = true;
+  s->extract_pending = false;
   return FFCZ_OK;
 }
 
@@ -1481,6 +1486,8 @@ static int clear_accumulators(ffcz_solver *s, cudaStream_t st) {
 
 extern "C" {
 
+static int ensure_extracted(ffcz_solver *s);
+
 int ffcz_solver_create(size_t nx, size_t ny, size_t nz, int dtype, ffcz_solver **out) {
   if (!out) return fail(FFCZ_ERR_INVALID, "out is NULL");
   *out = nullptr;
@@ -1670,6 +1677,14 @@ int ffcz_solver_set_staging(ffcz_solver *s, int staging) {
   return FFCZ_OK;
 }
 
+int ffcz_solver_set_extraction(ffcz_solver *s, int mode) {
+  FFCZ_TRY(check_solver(s));
+  if (mode != FFCZ_EXTRACT_EAGER && mode != FFCZ_EXTRACT_ON_DEMAND) return fail(FFCZ_ERR_INVALID, "unknown mode");
+  FFCZ_TRY(ensure_extracted(s));
+  s->extract_mode = mode;
+  return FFCZ_OK;
+}
+
 int ffcz_solver_get_tuning(ffcz_solver *s, int *choice, double *ms10) {
   FFCZ_TRY(check_solver(s));
   if (choice) {
@@ -1735,7 +1750,19 @@ static int solve_mode(ffcz_solver *s, int mode, int pro, const void *a, const vo
   s->ptw_partial = mode == FFCZ_MODE_PARTIAL_PTW;
   s->ptw_dc = s->ptw_partial ? s->partial_dc : 1;
   FFCZ_TRY(DISPATCH(s, project, s, pro, a, b, max_iter, tol));
+  if (extract_after && s->extract_mode == FFCZ_EXTRACT_ON_DEMAND) {
+    s->extract_pending = true;
+    return FFCZ_OK;
+  }
   return extract_after ? DISPATCH(s, extract, s) : FFCZ_OK;
+}
+
+// Runs a compaction the last solve left pending (FFCZ_EXTRACT_ON_DEMAND),
+// before its results are read or the edit arrays change: every call sees
+// what the eager mode would have given it.
+static int ensure_extracted(ffcz_solver *s) {
+  if (!s->extract_pending || s->extracted) return FFCZ_OK;
+  return DISPATCH(s, extract, s);
 }
 
 static int solve_host(ffcz_solver *s, int mode, const void *h_err, int max_iter, double tol) {
@@ -1846,6 +1873,7 @@ int ffcz_extract(ffcz_solver *s) {
 
 int ffcz_reset_edit_accumulators(ffcz_solver *s) {
   FFCZ_TRY(check_solver(s));
+  FFCZ_TRY(ensure_extracted(s));
   FFCZ_TRY(clear_accumulators(s, s->stream));
   FFCZ_CUDA(cudaStreamSynchronize(s->stream));
   return FFCZ_OK;
@@ -1853,6 +1881,7 @@ int ffcz_reset_edit_accumulators(ffcz_solver *s) {
 
 int ffcz_set_edit_accumulators(ffcz_solver *s, const void *h_freq_edits, const void *h_spatial_edits) {
   FFCZ_TRY(check_solver(s));
+  FFCZ_TRY(ensure_extracted(s));
   static const unsigned one = 1u;
   if (h_freq_edits) {
     FFCZ_CUDA(cudaMemcpyAsync(s->d_fedits, h_freq_edits, 2 * s->H * s->es, cudaMemcpyHostToDevice, s->stream));
@@ -1889,6 +1918,7 @@ int ffcz_get_convergence(ffcz_solver *s, double *metric) {
 
 int ffcz_get_active_counts(ffcz_solver *s, size_t *n_freq, size_t *n_spatial) {
   FFCZ_TRY(check_solver(s));
+  FFCZ_TRY(ensure_extracted(s));
   if (n_freq) *n_freq = s->extracted ? (size_t)s->h_ctl->count[0] : 0;
   if (n_spatial) *n_spatial = s->extracted ? (size_t)s->h_ctl->count[1] : 0;
   return FFCZ_OK;
@@ -1896,6 +1926,7 @@ int ffcz_get_active_counts(ffcz_solver *s, size_t *n_freq, size_t *n_spatial) {
 
 int ffcz_get_minmax(ffcz_solver *s, double *fmin, double *fmax, double *smin, double *smax) {
   FFCZ_TRY(check_solver(s));
+  FFCZ_TRY(ensure_extracted(s));
   if (fmin) *fmin = s->h_ctl->mn[0];
   if (fmax) *fmax = s->h_ctl->mx[0];
   if (smin) *smin = s->h_ctl->mn[1];
@@ -1928,26 +1959,32 @@ static int get_stream(ffcz_solver *s, const void *src, size_t count, size_t esz,
 
 int ffcz_get_freq_quant(ffcz_solver *s, uint16_t *dst, size_t cap, size_t *len) {
   FFCZ_TRY(check_solver(s));
+  FFCZ_TRY(ensure_extracted(s));
   return get_stream(s, s->d_fquant, s->extracted ? s->h_ctl->count[0] : 0, 2, dst, cap, len);
 }
 int ffcz_get_spatial_quant(ffcz_solver *s, uint16_t *dst, size_t cap, size_t *len) {
   FFCZ_TRY(check_solver(s));
+  FFCZ_TRY(ensure_extracted(s));
   return get_stream(s, s->d_squant, s->extracted ? s->h_ctl->count[1] : 0, 2, dst, cap, len);
 }
 int ffcz_get_freq_compact(ffcz_solver *s, void *dst, size_t cap, size_t *len) {
   FFCZ_TRY(check_solver(s));
+  FFCZ_TRY(ensure_extracted(s));
   return get_stream(s, s->d_fcompact, s->extracted ? s->h_ctl->count[0] : 0, s->es, dst, cap, len);
 }
 int ffcz_get_spatial_compact(ffcz_solver *s, void *dst, size_t cap, size_t *len) {
   FFCZ_TRY(check_solver(s));
+  FFCZ_TRY(ensure_extracted(s));
   return get_stream(s, s->d_scompact, s->extracted ? s->h_ctl->count[1] : 0, s->es, dst, cap, len);
 }
 int ffcz_get_freq_flags_pack(ffcz_solver *s, uint8_t *dst, size_t cap, size_t *len) {
   FFCZ_TRY(check_solver(s));
+  FFCZ_TRY(ensure_extracted(s));
   return get_stream(s, s->d_fpack, (2 * s->H + 7) / 8, 1, dst, cap, len);
 }
 int ffcz_get_spatial_flags_pack(ffcz_solver *s, uint8_t *dst, size_t cap, size_t *len) {
   FFCZ_TRY(check_solver(s));
+  FFCZ_TRY(ensure_extracted(s));
   return get_stream(s, s->d_spack, (s->N + 7) / 8, 1, dst, cap, len);
 }
 
@@ -1980,6 +2017,7 @@ int ffcz_get_spatial_flags(ffcz_solver *s, uint8_t *dst, size_t cap, size_t *len
 
 int ffcz_get_device_array(ffcz_solver *s, int which, void **dptr, size_t *bytes) {
   FFCZ_TRY(check_solver(s));
+  FFCZ_TRY(ensure_extracted(s));
   if (!dptr) return fail(FFCZ_ERR_INVALID, "NULL argument");
   const size_t es = s->es, N = s->N, H2 = 2 * s->H;
   const size_t cf = s->extracted ? s->h_ctl->count[0] : 0, cs = s->extracted ? s->h_ctl->count[1] : 0;
@@ -2027,6 +2065,7 @@ int ffcz_solver_set_precision(ffcz_solver *s, int precision) {
 
 int ffcz_solver_autotune(ffcz_solver *s, int reps, double *ms6) {
   FFCZ_TRY(check_solver(s));
+  FFCZ_TRY(ensure_extracted(s));
   if (reps < 1) return fail(FFCZ_ERR_INVALID, "reps must be positive");
   Range r("ffcz:autotune");
   return DISPATCH(s, autotune, s, reps, ms6);
@@ -2148,6 +2187,7 @@ int ffcz_reconstruct_device(ffcz_solver *s, const void *d_decomp, const uint16_t
                             const uint16_t *d_spatial_quant, size_t n_spatial, const uint8_t *d_spatial_pack,
                             double spatial_min, double spatial_max, void *d_out) {
   FFCZ_TRY(check_solver(s));
+  FFCZ_TRY(ensure_extracted(s));
   FFCZ_TRY(check_dev_ptr(d_decomp, "decompressed data"));
   FFCZ_TRY(check_dev_ptr(d_out, "output"));
   if (n_freq > 2 * s->H || n_spatial > s->N) return fail(FFCZ_ERR_INVALID, "more edits than elements");
@@ -2160,6 +2200,7 @@ int ffcz_reconstruct_device(ffcz_solver *s, const void *d_decomp, const uint16_t
 int ffcz_solver_decode(ffcz_solver *s, const void *d_decomp, ffcz_huff_result *const *in4, double freq_min,
                        double freq_max, double spatial_min, double spatial_max, void *d_out) {
   FFCZ_TRY(check_solver(s));
+  FFCZ_TRY(ensure_extracted(s));
   Range r("ffcz:decode");
   if (!in4) return fail(FFCZ_ERR_INVALID, "in4 is NULL");
   const size_t nf = in4[0] ? in4[0]->num_elements : 0, ns = in4[2] ? in4[2]->num_elements : 0;
@@ -2204,6 +2245,7 @@ int ffcz_solver_container_header(ffcz_solver *s, ffcz_container_header *h) {
 
 int ffcz_solver_encode(ffcz_solver *s, int zstd_level, int zstd_mode, ffcz_huff_result **out4) {
   FFCZ_TRY(check_solver(s));
+  FFCZ_TRY(ensure_extracted(s));
   Range r("ffcz:encode");
   if (!out4) return fail(FFCZ_ERR_INVALID, "out4 is NULL");
   for (int i = 0; i < 4; ++i) out4[i] = nullptr;

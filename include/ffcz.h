@@ -128,6 +128,20 @@ int ffcz_solver_set_dft_stages(ffcz_solver *s, int stages);
  * (FP64 solvers, lengths without compile-time kernels).  A staged pass that
  * waits about two seconds for a tile without it arriving gives up, and the
  * solve returns FFCZ_ERR_CUDA. */
+/* When a solve compacts its edit accumulators (no counterpart in the
+ * reference, whose solve_all_abs always extracts at its end, impl:850-852):
+ *   FFCZ_EXTRACT_EAGER (default): at the end of every solve, as the reference;
+ *   FFCZ_EXTRACT_ON_DEMAND: the solve leaves the compaction pending and the
+ *     first call that reads its results (counts, min/max, streams, packs,
+ *     device arrays, encode) or changes the edit arrays (reset, set,
+ *     decode, autotune) runs it first.  Every call returns what it returns
+ *     in the eager mode; a solve followed by ffcz_strict_finish then
+ *     compacts once instead of twice.  A pending compaction runs before
+ *     the mode changes. */
+#define FFCZ_EXTRACT_EAGER 0
+#define FFCZ_EXTRACT_ON_DEMAND 1
+int ffcz_solver_set_extraction(ffcz_solver *s, int mode);
+
 #define FFCZ_STAGING_REGISTERS 0
 #define FFCZ_STAGING_TMA 1
 #define FFCZ_STAGING_AUTO 2
