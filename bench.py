@@ -67,7 +67,9 @@ PEAKS = ROOT / "MEASURED_PEAKS.json"
 # `ncu --set full` capture of the same workload (cold-cache replays, writes
 # still dirty in L2 at kernel exit not counted).
 TRAFFIC = {"plain256": {"zfwd_r2c": 169.0e6, "y_fwd": 89.3e6, "x_fwd_clamp_inv": 91.5e6, "y_inv": 89.3e6,
-                        "zinv_c2r_viol": 98.2e6}}
+                        "zinv_c2r_viol": 98.2e6},
+           "precision512": {"zfwd_r2c": 1591.2e6, "y_fwd": 1054.4e6, "x_fwd_clamp_inv": 1067.7e6, "y_inv": 1053.6e6,
+                            "zinv_c2r_viol": 1057.9e6}}
 
 
 def parse():
