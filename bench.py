@@ -341,7 +341,11 @@ def run_ours(args):
         s = F.ProjectionSolver(*fld.shape, dtype=dt)
         if dt == np.float64 and args.precision == "split":
             s.set_precision(F.FFCZ_PRECISION_SPLIT)
-        s.set_form(form)
+        try:
+            s.set_form(form)
+        except F.FFCzError:
+            s.close()
+            raise
         if tensor:
             s.set_dft_stages(F.FFCZ_DFT_TENSOR)
         s.set_stream(torch.cuda.current_stream())
@@ -468,11 +472,15 @@ def run_ours(args):
 
     plain = None
     if not args.no_plain:
-        ps, _ = make_solver(F.FFCZ_FORM_PLAIN)
-        plain = measure_form(ps)
-        e_plain = ps.get_results()
-        plain["max_abs_diff_vs_chosen"] = float(np.abs(e_plain.astype(np.float64) - e_fin).max())
-        ps.close()
+        try:
+            ps, _ = make_solver(F.FFCZ_FORM_PLAIN)
+        except F.FFCzError as ex:  # e.g. float-float FP64 passes have no forward-with-clamp kernel
+            plain = {"unavailable": str(ex)}
+        else:
+            plain = measure_form(ps)
+            e_plain = ps.get_results()
+            plain["max_abs_diff_vs_chosen"] = float(np.abs(e_plain.astype(np.float64) - e_fin).max())
+            ps.close()
 
     tensor = None
     if not args.no_tensor and dt == np.float32 and any(n in (256, 512) for n in fld.shape[:2] if n > 1):
@@ -561,7 +569,9 @@ def form_report(rc, plain, tensor=None):
     out = {"chosen": dict(one(rc), form="fused: five HBM passes per 3D iteration (x forward + clamp + x inverse "
                                         "in one pass), graph-captured loop, strict FP64 bounds by certificate "
                                         "or FP64 transform")}
-    if plain is not None:
+    if plain is not None and "unavailable" in plain:
+        out["plain_fp32"] = plain
+    elif plain is not None:
         out["plain_fp32"] = dict(one(plain), form="plain FP32: six HBM passes per 3D iteration (x forward + "
                                                   "clamp and x inverse separate), same kernels otherwise",
                                  max_abs_diff_vs_chosen=plain["max_abs_diff_vs_chosen"])
