@@ -73,15 +73,18 @@ __global__ void __launch_bounds__((L / rp_elems(L, CAP)) << LGTW, MINB)
   const int tid = threadIdx.x;
   const int c = tid & (TW - 1);
   const int t = tid >> LGTW;
-  const long long per_b = (long long)s.Q * s.tpq;
-  // tile -> (batch, row, first column): the order of ks_strided's blocks
-  auto coords = [&](long long tile, long long &bb, int &q, int &kz0) {
-    bb = tile / per_b;
-    const int rem = (int)(tile - bb * per_b);
-    q = rem / s.tpq;
-    kz0 = (rem - q * s.tpq) * TW;
+  // tile -> (batch, row, first column): the order of ks_strided's blocks,
+  // in 32-bit arithmetic (a pass has fewer than 2^31 tiles)
+  const unsigned per_b = (unsigned)s.Q * (unsigned)s.tpq;
+  const unsigned nt32 = (unsigned)ntiles;
+  auto coords = [&](unsigned tile, long long &bb, int &q, int &kz0) {
+    const unsigned b = tile / per_b;
+    const unsigned rem = tile - b * per_b;
+    bb = b;
+    q = (int)(rem / (unsigned)s.tpq);
+    kz0 = ((int)rem - q * s.tpq) * TW;
   };
-  auto issue = [&](long long tile, int slot) {
+  auto issue = [&](unsigned tile, int slot) {
     long long bb;
     int q, kz0;
     coords(tile, bb, q, kz0);
@@ -98,18 +101,18 @@ __global__ void __launch_bounds__((L / rp_elems(L, CAP)) << LGTW, MINB)
     fence_mbar_init();
 #pragma unroll
     for (int b = 0; b < NBUF; ++b) {
-      const long long tile = blockIdx.x + (long long)b * gridDim.x;
-      if (tile < ntiles) issue(tile, b);
+      const unsigned tile = blockIdx.x + (unsigned)b * gridDim.x;
+      if (tile < nt32) issue(tile, b);
     }
   }
   __syncthreads();
   constexpr int D0 = (MODE == MODE_INV) ? +1 : -1;
   constexpr int DL = (MODE == MODE_FWD || MODE == MODE_FC) ? -1 : +1;
-  for (long long i = 0;; ++i) {
-    const long long tile = blockIdx.x + i * gridDim.x;
-    if (tile >= ntiles) break;
+  for (unsigned i = 0;; ++i) {
+    const unsigned tile = blockIdx.x + i * gridDim.x;
+    if (tile >= nt32) break;
     const int slot = (int)(i % NBUF);
-    const unsigned parity = (unsigned)((i / NBUF) & 1);
+    const unsigned parity = (i / NBUF) & 1u;
     V *buf = reinterpret_cast<V *>(base + slot * SLOT);
     long long bb;
     int q, kz0;
@@ -128,9 +131,8 @@ __global__ void __launch_bounds__((L / rp_elems(L, CAP)) << LGTW, MINB)
         // let the copies still in flight land (again with a limit) before
         // the block's shared memory is released
         for (int k = 0; k < NBUF; ++k) {
-          const long long ii = i + k;
-          if (blockIdx.x + ii * gridDim.x < ntiles)
-            mbar_wait_bounded(smem_u32(bar + (int)(ii % NBUF)), (unsigned)((ii / NBUF) & 1));
+          const unsigned ii = i + k;
+          if (blockIdx.x + ii * gridDim.x < nt32) mbar_wait_bounded(smem_u32(bar + (int)(ii % NBUF)), (ii / NBUF) & 1u);
         }
       }
       return;
@@ -148,8 +150,8 @@ __global__ void __launch_bounds__((L / rp_elems(L, CAP)) << LGTW, MINB)
     fence_proxy_async_smem();
     __syncthreads();
     if (tid == 0) {
-      const long long nt = tile + (long long)NBUF * gridDim.x;
-      if (nt < ntiles) issue(nt, slot);
+      const unsigned nt = tile + (unsigned)NBUF * gridDim.x;
+      if (nt < nt32) issue(nt, slot);
     }
     V *dst = spec + bb * (long long)L * s.Wtot + (long long)q * s.Hzp + kz0 + c;
     if (live) {

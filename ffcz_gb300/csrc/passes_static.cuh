@@ -572,12 +572,15 @@ __global__ void __launch_bounds__((L / rp_elems(L, CAP)) << LGTW,
   V *buf = reinterpret_cast<V *>(smem_raw);
   const int c = threadIdx.x & (TW - 1);
   const int t = threadIdx.x >> LGTW;
-  const long long tile = blockIdx.x;
-  const long long per_b = (long long)s.Q * s.tpq;
-  const long long bb = tile / per_b;
-  const int rem = (int)(tile - bb * per_b);
-  const int q = rem / s.tpq;
-  const int kb = rem - q * s.tpq;
+  // tile -> (batch, row, first column) in 32-bit arithmetic (a pass has
+  // fewer than 2^31 tiles; a 64-bit division costs dozens of instructions)
+  const unsigned tile = blockIdx.x;
+  const unsigned per_b = (unsigned)s.Q * (unsigned)s.tpq;
+  const unsigned bbu = tile / per_b;
+  const unsigned rem = tile - bbu * per_b;
+  const int q = (int)(rem / (unsigned)s.tpq);
+  const int kb = (int)rem - q * s.tpq;
+  const long long bb = bbu;
   const int kz0 = kb * TW;
   const bool live = c < s.Hz - kz0;
   const VG *src = spec + bb * (long long)L * s.Wtot + (long long)q * s.Hzp + kz0 + c;
