@@ -95,6 +95,7 @@ SIGNATURES = {
     "ffcz_set_edit_accumulators": [_p, _p, _p],
     "ffcz_huff_histogram_device": [_p, _sz, _i, _p, _p],
     "ffcz_huff_tree": [_p, _sz, _p, _p, _p, _p],
+    "ffcz_huff_codebook": [_p, _sz, _p, _p, _p, _sz, _SP],
     "ffcz_solver_synchronize": [_p],
     "ffcz_get_iterations": [_p, C.POINTER(C.c_int)],
     "ffcz_get_convergence": [_p, C.POINTER(C.c_double)],

@@ -469,6 +469,22 @@ int ffcz_huff_tree(const uint32_t *freqs, size_t n, int32_t *left, int32_t *righ
   return FFCZ_OK;
 }
 
+int ffcz_huff_codebook(const uint32_t *hist, size_t nbins, uint32_t *symbols, uint32_t *codes, int32_t *lengths,
+                       size_t cap, size_t *n) {
+  if (!n || (nbins && !hist)) return fail(FFCZ_ERR_INVALID, "NULL argument");
+  Codebook cb;
+  build_codebook(hist, nbins, cb);
+  *n = cb.sym.size();
+  if (cb.sym.size() > cap) return fail(FFCZ_ERR_CAPACITY, "more symbols than the arrays hold");
+  if (!cb.sym.empty() && (!symbols || !codes || !lengths)) return fail(FFCZ_ERR_INVALID, "NULL argument");
+  for (size_t i = 0; i < cb.sym.size(); ++i) {
+    symbols[i] = cb.sym[i];
+    codes[i] = cb.code[i];
+    lengths[i] = cb.len[i];
+  }
+  return FFCZ_OK;
+}
+
 size_t ffcz_zstd_bound(size_t n) { return zstd_bound(n); }
 
 int ffcz_zstd_compress(const uint8_t *src, size_t n, int level, int mode, uint8_t *dst, size_t cap,

@@ -38,22 +38,28 @@ void build_codebook(const uint32_t *hist, size_t nbins, Codebook &cb) {
   std::vector<int> left, right;
   std::vector<uint64_t> wt;
   build_tree(cb.freq.data(), n, left, right, wt);
-  const int root = 2 * n - 2;
-  // Iterative depth-first walk from the root.
-  struct Item { int node; uint32_t code; int len; };
-  std::vector<Item> stack;
-  stack.push_back({root, 0u, 0});
-  while (!stack.empty()) {
-    const Item it = stack.back();
-    stack.pop_back();
-    if (left[it.node] < 0 && right[it.node] < 0) {
-      cb.code[it.node] = it.code;
-      cb.len[it.node] = it.len ? it.len : 1;
-      cb.max_len = std::max(cb.max_len, cb.len[it.node]);
-      continue;
-    }
-    if (right[it.node] >= 0) stack.push_back({right[it.node], (it.code << 1) | 1u, it.len + 1});
-    if (left[it.node] >= 0) stack.push_back({left[it.node], it.code << 1, it.len + 1});
+  // Codes from the root down, as the reference's recursive walk gives them
+  // (0 to the left child, 1 to the right, MSB-first in a uint32 that keeps
+  // its low 32 bits): every child has a smaller index than its parent
+  // (internal nodes are created in increasing order from smaller ones), so
+  // one sweep from the root (2n-2) downwards reaches each node after its
+  // parent.
+  const int nodes = 2 * n - 1;
+  std::vector<uint32_t> code(nodes);
+  std::vector<int32_t> len(nodes);
+  code[nodes - 1] = 0u;
+  len[nodes - 1] = 0;
+  for (int k = nodes - 1; k >= n; --k) {
+    const int a = left[k], b = right[k];
+    code[a] = code[k] << 1;
+    len[a] = len[k] + 1;
+    code[b] = (code[k] << 1) | 1u;
+    len[b] = len[k] + 1;
+  }
+  for (int i = 0; i < n; ++i) {
+    cb.code[i] = code[i];
+    cb.len[i] = len[i];
+    cb.max_len = std::max(cb.max_len, len[i]);
   }
 }
 
@@ -71,31 +77,30 @@ void build_tree(const uint32_t *freq, int n, std::vector<int> &left, std::vector
     if (n == 1) wt[0] = freq[0];
     return;
   }
-  // (freq, index) packed so that it sorts as the pair; LSD radix sort in
-  // 16-bit digits over the bits in use
-  std::vector<uint64_t> key(n), tmp(n);
-  uint64_t all = 0;
+  // Leaves in (freq, index) order: they start in index order, so a stable
+  // LSD counting sort on freq alone (16-bit digits, only the digits in use,
+  // count arrays sized to the largest digit) orders ties by index.
+  uint32_t maxf = 0;
   for (int i = 0; i < n; ++i) {
     wt[i] = freq[i];
-    key[i] = ((uint64_t)freq[i] << 32) | (uint32_t)i;
-    all |= key[i];
+    maxf = std::max(maxf, freq[i]);
   }
-  std::vector<uint32_t> count(1u << 16);
-  for (int shift = 0; shift < 64 && (all >> shift); shift += 16) {
-    if (((all >> shift) & 0xffffu) == 0) continue;  // every digit zero: nothing moves
-    std::fill(count.begin(), count.end(), 0u);
-    for (int i = 0; i < n; ++i) ++count[(key[i] >> shift) & 0xffffu];
+  std::vector<int> leaves(n), tmp(n);
+  for (int i = 0; i < n; ++i) leaves[i] = i;
+  std::vector<uint32_t> count;
+  for (int shift = 0; shift < 32 && (maxf >> shift); shift += 16) {
+    const uint32_t top = std::min<uint32_t>(maxf >> shift, 0xffffu);
+    count.assign((size_t)top + 1, 0u);
+    for (int i = 0; i < n; ++i) ++count[(freq[leaves[i]] >> shift) & 0xffffu];
     uint32_t run = 0;
     for (uint32_t &c : count) {
       const uint32_t t = c;
       c = run;
       run += t;
     }
-    for (int i = 0; i < n; ++i) tmp[count[(key[i] >> shift) & 0xffffu]++] = key[i];
-    key.swap(tmp);
+    for (int i = 0; i < n; ++i) tmp[count[(freq[leaves[i]] >> shift) & 0xffffu]++] = leaves[i];
+    leaves.swap(tmp);
   }
-  std::vector<int> leaves(n);
-  for (int i = 0; i < n; ++i) leaves[i] = (int)(key[i] & 0xffffffffu);
   int qa = 0, qb = n;  // heads: sorted leaves, internal nodes
   int next = n;
   auto take = [&]() {

@@ -429,6 +429,15 @@ int ffcz_huff_histogram_device(const void *d_data, size_t n, int symbol_bytes, v
  * child; -1 for no child.  *root = 2n-2 (0 for one leaf, -1 for none). */
 int ffcz_huff_tree(const uint32_t *freqs, size_t n, int32_t *left, int32_t *right, uint64_t *weights,
                    int32_t *root);
+/* The code table the encoder builds from a dense histogram (nbins counts,
+ * host memory, no GPU): cudaFrequencyCount's ascending (symbol, count)
+ * pairs, buildHuffmanTree and generateCodesRecursive
+ * (HuffmanZSTDCoder.cuh:48-178): symbols with a non-zero count in
+ * ascending order, their codes (MSB-first, the low 32 bits) and lengths
+ * (one symbol: code 0, length 1).  *n receives the number of symbols;
+ * FFCZ_ERR_CAPACITY when it exceeds cap. */
+int ffcz_huff_codebook(const uint32_t *hist, size_t nbins, uint32_t *symbols, uint32_t *codes, int32_t *lengths,
+                       size_t cap, size_t *n);
 /* CompressionResult fields (:240-246). */
 int ffcz_huff_result_sizes(const ffcz_huff_result *r, size_t *compressed_bytes,
                            size_t *bitstream_bytes, size_t *num_elements,
