@@ -552,6 +552,142 @@ __global__ void __launch_bounds__(EX_THREADS) k_ex_place(const T *__restrict__ s
   }
 }
 
+// ---------------------------------------------------------------------------
+// Listed accumulators.  An edit accumulator whose dirty flag reads 0 but
+// whose index list (slist[0] = count, slist[4..] = indices, at most
+// EX_LIST_MAX) is non-empty holds zeros everywhere except at the listed
+// indices (a list may repeat an index).  k_ex_part treats it as untouched
+// (zero flag words and records, nothing read); this one block then folds
+// the listed values into the results the full compaction gives for the
+// array: the active values in ascending index order with their uint16
+// codes, their flag bits, the count and the whole-array min and max (the
+// zeros of the unlisted entries included).
+constexpr int EX_LIST_MAX = 4096;
+constexpr int EX_LIST_THREADS = 1024;
+
+template <typename T>
+__global__ void __launch_bounds__(EX_LIST_THREADS) k_ex_listed(const T *__restrict__ a, long long n, T thr,
+                                                                const unsigned *__restrict__ dirty,
+                                                                const unsigned *__restrict__ slist,
+                                                                T *__restrict__ compact, uint16_t *__restrict__ quant,
+                                                                unsigned *__restrict__ pack_words, int write_pack,
+                                                                T *__restrict__ mnmx, LoopCtl *__restrict__ ctl,
+                                                                int which) {
+  constexpr int PER = EX_LIST_MAX / EX_LIST_THREADS;
+  __shared__ unsigned key[EX_LIST_MAX];
+  __shared__ unsigned wsum[EX_LIST_THREADS / 32];
+  __shared__ unsigned long long wmn[EX_LIST_THREADS / 32], wmx[EX_LIST_THREADS / 32];
+  if (*dirty != 0u) return;  // written throughout: the full compaction stands
+  const unsigned cnt = slist[0];
+  if (cnt == 0u) return;     // untouched
+  if (cnt > (unsigned)EX_LIST_MAX) {  // (an overflowing recorder marks the array written throughout)
+    if (threadIdx.x == 0) ctl->err = 2;
+    return;
+  }
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  int P = 1;
+  while (P < (int)cnt) P <<= 1;
+  for (int i = tid; i < P; i += EX_LIST_THREADS) key[i] = i < (int)cnt ? slist[4 + i] : 0xffffffffu;
+  __syncthreads();
+  // bitonic sort, ascending
+  for (int k = 2; k <= P; k <<= 1)
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int i = tid; i < P; i += EX_LIST_THREADS) {
+        const int l = i ^ j;
+        if (l > i) {
+          const unsigned x = key[i], y = key[l];
+          if (((i & k) == 0) == (x > y)) {
+            key[i] = y;
+            key[l] = x;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  // thread t owns sorted slots [t*PER, t*PER + PER)
+  T v[PER];
+  unsigned act = 0, uniq = 0;
+  T mn = dev_inf<T>(), mx = -dev_inf<T>();
+#pragma unroll
+  for (int q = 0; q < PER; ++q) {
+    const int i = tid * PER + q;
+    v[q] = T(0);
+    if (i < (int)cnt && (i == 0 || key[i] != key[i - 1])) {
+      v[q] = a[key[i]];
+      ++uniq;
+      mn = fmin(mn, v[q]);
+      mx = fmax(mx, v[q]);
+      if (fabs(v[q]) > thr) act |= 1u << q;
+    }
+  }
+  // block sums of the unique and active counts, min and max as keys
+  unsigned na = __popc(act), xs = na;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned y = __shfl_up_sync(0xffffffffu, xs, o);
+    if (lane >= o) xs += y;
+  }
+  unsigned long long kmn = uniq ? ord_key<T>(mn) : ~0ull, kmx = uniq ? ord_key<T>(mx) : 0ull;
+  unsigned u = uniq;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    u += __shfl_xor_sync(0xffffffffu, u, o);
+    const unsigned long long p = __shfl_xor_sync(0xffffffffu, kmn, o), q = __shfl_xor_sync(0xffffffffu, kmx, o);
+    kmn = p < kmn ? p : kmn;
+    kmx = q > kmx ? q : kmx;
+  }
+  __shared__ unsigned wu[EX_LIST_THREADS / 32];
+  if (lane == 31) wsum[warp] = xs;
+  if (lane == 0) {
+    wu[warp] = u;
+    wmn[warp] = kmn;
+    wmx[warp] = kmx;
+  }
+  __syncthreads();
+  unsigned off = xs - na, total = 0, utot = 0;
+  for (int w = 0; w < EX_LIST_THREADS / 32; ++w) {
+    off += w < warp ? wsum[w] : 0u;
+    total += wsum[w];
+    utot += wu[w];
+    kmn = wmn[w] < kmn ? wmn[w] : kmn;
+    kmx = wmx[w] > kmx ? wmx[w] : kmx;
+  }
+  T gmn = key_val<T>(kmn), gmx = key_val<T>(kmx);
+  if ((long long)utot < n) {  // the unlisted entries are zeros
+    gmn = fmin(gmn, T(0));
+    gmx = fmax(gmx, T(0));
+  }
+  // the full compaction's keys of the same values
+  gmn = key_val<T>(ord_key<T>(gmn));
+  gmx = key_val<T>(ord_key<T>(gmx));
+#pragma unroll
+  for (int q = 0; q < PER; ++q)
+    if (act & (1u << q)) {
+      const unsigned idx = key[tid * PER + q];
+      compact[off] = v[q];
+      quant[off] = quantize16<T>(v[q], gmn, gmx);
+      ++off;
+      if (write_pack) atomicOr(pack_words + (idx >> 5), 1u << (idx & 31u));
+    }
+  if (tid == 0) {
+    mnmx[0] = gmn;
+    mnmx[1] = gmx;
+    ctl->count[which] = total;
+    ctl->mn[which] = (double)gmn;
+    ctl->mx[which] = (double)gmx;
+  }
+}
+
+// Records element i of an accumulator that a clamp just wrote: while the
+// accumulator's dirty flag reads 0 the index joins its list; a full list
+// marks the accumulator written throughout instead.
+__device__ __forceinline__ void ex_list_record(unsigned *dirty, unsigned *slist, long long i) {
+  if (*(volatile unsigned *)dirty != 0u) return;
+  const unsigned k = atomicAdd(slist, 1u);
+  if (k < (unsigned)EX_LIST_MAX) slist[4 + k] = (unsigned)i;
+  else atomicExch(dirty, 1u);
+}
+
 // Flag pack of projection_algorithm.cu:382-405 as launched by
 // projection_algorithm_impl.cuh:429-449 (nbytes = ceil(n/8)): byte b <
 // ceil(nbytes/8) holds the flags of elements [8b, 8b+8) ∩ [0, nbytes);

@@ -114,6 +114,10 @@ struct ffcz_solver {
   // d_sdirty: the same for the spatial accumulator, set by the loop control
   // (k_check before a clamping prologue, k_final_clamp) and the decoder.
   unsigned *d_fdirty = nullptr, *d_sdirty = nullptr;
+  // index list of the spatial accumulator while only the strict finish's
+  // clamp has written it since its last clear ([0] = count, [4..] =
+  // indices; see k_ex_listed)
+  unsigned *d_slist = nullptr;
   void *d_mnmx = nullptr;
   size_t nblk_max = 0;
   unsigned long long *d_up_blk = nullptr;  // decoder: set flags per chunk (lazy)
@@ -880,6 +884,11 @@ int extract_one(ffcz_solver *s, cudaStream_t st, const T *a, size_t n, int which
     k_pack_reference<T><<<g, 256, 0, st>>>(a, (long long)n, thr, pack, (long long)pack_alloc);
     s->launches += 1;
   }
+  if (which == 1) {  // the spatial accumulator may be listed (strict finish's clamp only)
+    k_ex_listed<T><<<1, EX_LIST_THREADS, 0, st>>>(a, (long long)n, thr, s->d_sdirty, s->d_slist, compact, quant,
+                                                  (unsigned *)pack, correct, mnmx, s->d_ctl, which);
+    s->launches += 1;
+  }
   FFCZ_CUDA(cudaGetLastError());
   return FFCZ_OK;
 }
@@ -930,7 +939,7 @@ void free_all(ffcz_solver *s) {
   for (LoopGraph &g : s->lg) g.reset();
   void *bufs[] = {s->d_x, s->d_e, s->d_spec, s->d_fedits, s->d_sedits, s->d_fcompact, s->d_scompact,
                   s->d_fquant, s->d_squant, s->d_fpack, s->d_spack, s->d_tw, s->d_ctl, s->d_ex_rec, s->d_fdirty, s->d_sdirty,
-                  s->d_mnmx, s->d_tw_ff};
+                  s->d_slist, s->d_mnmx, s->d_tw_ff};
   for (void *p : bufs)
     if (p) cudaFree(p);
   if (s->d_up_blk) cudaFree(s->d_up_blk);
@@ -1118,7 +1127,7 @@ __global__ void k_spec_absmax_t(const c2<T> *__restrict__ spec, long long rows, 
 // in FP64.
 template <typename T>
 __global__ void __launch_bounds__(256) k_clamp_stats(T *__restrict__ e, T *__restrict__ sedits, T eps, long long n,
-                                                     unsigned *sdirty, double *__restrict__ partial,
+                                                     unsigned *sdirty, unsigned *slist, double *__restrict__ partial,
                                                      unsigned long long *__restrict__ mx) {
   // 16-byte vectors, kU of them loaded before any is processed, so that
   // each thread keeps several loads in flight (e is 16-byte aligned)
@@ -1133,6 +1142,7 @@ __global__ void __launch_bounds__(256) k_clamp_stats(T *__restrict__ e, T *__res
       v = spatial_clamp(v, eps, sedits, i);
       hit = true;
       chg += fabs(v0 - v);
+      if (slist) ex_list_record(sdirty, slist, i);
     }
     pre = fma(v0, v0, pre);
     post = fma(v, v, post);
@@ -1177,7 +1187,7 @@ __global__ void __launch_bounds__(256) k_clamp_stats(T *__restrict__ e, T *__res
     ws[1][warp] = dpost;
     ws[2][warp] = dchg;
     atomic_max_abs(mx, dm);
-    if (any) *sdirty = 1u;
+    if (any && !slist) *sdirty = 1u;
   }
   __syncthreads();
   if (threadIdx.x < 3) {
@@ -1281,6 +1291,7 @@ int autotune(ffcz_solver *s, int reps, double *ms6) {
   FFCZ_CUDA(cudaMemsetAsync(s->d_fdirty, 0, sizeof(unsigned), st));
   FFCZ_CUDA(cudaMemsetAsync(s->d_sedits, 0, s->N * s->es, st));
   FFCZ_CUDA(cudaMemsetAsync(s->d_sdirty, 0, sizeof(unsigned), st));
+  FFCZ_CUDA(cudaMemsetAsync(s->d_slist, 0, sizeof(unsigned), st));
   FFCZ_CUDA(cudaStreamSynchronize(st));
   // the cached loop graphs hold the previous kernels
   for (LoopGraph &g : s->lg) g.reset();
@@ -1326,8 +1337,8 @@ int certify(ffcz_solver *s, bool clamp, T eps_t, bool use_recorded, double *smax
   unsigned long long *mx = (unsigned long long *)(partial + 3 * 152 * 16);
   FFCZ_CUDA(cudaMemsetAsync(mx, 0, 2 * sizeof(unsigned long long), st));
   const T lim = clamp ? eps_t : std::numeric_limits<T>::infinity();
-  k_clamp_stats<T><<<g, 256, 0, st>>>(tp<T>(s->d_e), tp<T>(s->d_sedits), lim, (long long)s->N, s->d_sdirty, partial,
-                                      mx);
+  k_clamp_stats<T><<<g, 256, 0, st>>>(tp<T>(s->d_e), tp<T>(s->d_sedits), lim, (long long)s->N, s->d_sdirty,
+                                      s->d_slist, partial, mx);
   FFCZ_CUDA(cudaGetLastError());
   std::vector<double> h(3 * g + 1);
   FFCZ_CUDA(cudaMemcpyAsync(h.data(), partial, 3 * g * sizeof(double), cudaMemcpyDeviceToHost, st));
@@ -1459,8 +1470,20 @@ static __global__ void k_to_ff(const double2 *__restrict__ src, ffc *__restrict_
 // Zeroes `bytes` bytes at p (16-byte aligned) when *dirty != 0: an
 // accumulator whose flag reads 0 is all zeros already (the flag is cleared
 // with the array and set by every path that writes it).
-static __global__ void k_zero_if_dirty(void *__restrict__ p, size_t bytes, const unsigned *__restrict__ dirty) {
-  if (*dirty == 0u) return;
+// A listed accumulator (flag 0, slist non-empty) has only its listed
+// entries zeroed.
+static __global__ void k_zero_if_dirty(void *__restrict__ p, size_t bytes, const unsigned *__restrict__ dirty,
+                                       const unsigned *__restrict__ slist, int elem_bytes) {
+  if (*dirty == 0u) {
+    if (!slist) return;
+    const unsigned cnt = min(slist[0], (unsigned)EX_LIST_MAX);
+    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x) {
+      const size_t k = slist[4 + i];
+      if (elem_bytes == 4) reinterpret_cast<unsigned *>(p)[k] = 0u;
+      else reinterpret_cast<unsigned long long *>(p)[k] = 0ull;
+    }
+    return;
+  }
   uint4 *q = reinterpret_cast<uint4 *>(p);
   const size_t n4 = bytes / 16;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n4; i += (size_t)gridDim.x * blockDim.x)
@@ -1474,11 +1497,12 @@ static int clear_accumulators(ffcz_solver *s, cudaStream_t st) {
   const size_t fb = 2 * s->H * s->es, sb = s->N * s->es;
   const unsigned gf = (unsigned)std::min<size_t>(std::max<size_t>(ceil_div(fb / 16, (size_t)256), 1), 152 * 8);
   const unsigned gs = (unsigned)std::min<size_t>(std::max<size_t>(ceil_div(sb / 16, (size_t)256), 1), 152 * 8);
-  k_zero_if_dirty<<<gf, 256, 0, st>>>(s->d_fedits, fb, s->d_fdirty);
-  k_zero_if_dirty<<<gs, 256, 0, st>>>(s->d_sedits, sb, s->d_sdirty);
+  k_zero_if_dirty<<<gf, 256, 0, st>>>(s->d_fedits, fb, s->d_fdirty, nullptr, (int)s->es);
+  k_zero_if_dirty<<<gs, 256, 0, st>>>(s->d_sedits, sb, s->d_sdirty, s->d_slist, (int)s->es);
   FFCZ_CUDA(cudaGetLastError());
   FFCZ_CUDA(cudaMemsetAsync(s->d_fdirty, 0, sizeof(unsigned), st));
   FFCZ_CUDA(cudaMemsetAsync(s->d_sdirty, 0, sizeof(unsigned), st));
+  FFCZ_CUDA(cudaMemsetAsync(s->d_slist, 0, sizeof(unsigned), st));
   return FFCZ_OK;
 }
 
@@ -1544,6 +1568,7 @@ int ffcz_solver_create(size_t nx, size_t ny, size_t nz, int dtype, ffcz_solver *
   if (rc == FFCZ_OK) rc = alloc((void **)&s->d_ex_rec, nrec * sizeof(unsigned long long));
   if (rc == FFCZ_OK) rc = alloc((void **)&s->d_fdirty, sizeof(unsigned));
   if (rc == FFCZ_OK) rc = alloc((void **)&s->d_sdirty, sizeof(unsigned));
+  if (rc == FFCZ_OK) rc = alloc((void **)&s->d_slist, (EX_LIST_MAX + 4) * sizeof(unsigned));
   if (rc == FFCZ_OK) rc = alloc(&s->d_mnmx, 4 * es);
   if (rc == FFCZ_OK) {
     cudaError_t e = cudaMallocHost(&s->h_ctl, sizeof(LoopCtl));
@@ -1562,6 +1587,7 @@ int ffcz_solver_create(size_t nx, size_t ny, size_t nz, int dtype, ffcz_solver *
     if (e == cudaSuccess) e = cudaMemset(s->d_fdirty, 0, sizeof(unsigned));
     if (e == cudaSuccess) e = cudaMemset(s->d_sedits, 0, N * es);
     if (e == cudaSuccess) e = cudaMemset(s->d_sdirty, 0, sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaMemset(s->d_slist, 0, sizeof(unsigned));
     if (e == cudaSuccess) e = xp_init(s.get());
     if (e != cudaSuccess) rc = cuda_fail(e, "cudaMemset", __FILE__, __LINE__);
   }
