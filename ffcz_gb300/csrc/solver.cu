@@ -1254,11 +1254,14 @@ int autotune(ffcz_solver *s, int reps, double *ms6) {
     const Launch &lnf = axis == 0 ? s->lyf : s->lxf;
     const SArgs &saf = axis == 0 ? s->syf : s->sxf;
     const AxisPlan &plf = axis == 0 ? s->pyf : s->pxf;
+    // the passes this axis runs in the solver's form (the plain form's x
+    // axis: forward with clamp, then inverse, where the tile has that kernel)
+    const bool plain_form = s->form == FFCZ_FORM_PLAIN && s->cmode == CLAMP_ABS;
     auto run = [&]() {
-      if (fused_here) {
+      if (fused_here && !(plain_form && k[MODE_FC])) {
         strided_kernel<T>(s, st, axis, MODE_FCI, true, ca, spec);
       } else {
-        strided_kernel<T>(s, st, axis, MODE_FWD, false, ca, spec);
+        strided_kernel<T>(s, st, axis, fused_here ? MODE_FC : MODE_FWD, false, ca, spec);
         strided_kernel<T>(s, st, axis, MODE_INV, false, ca, spec);
       }
     };

@@ -109,6 +109,9 @@ WORKLOADS = {
     # the precision field's spectrum kernels at a profiling size: the same
     # 512-point x and y passes on a quarter of the z extent (2 GB resident)
     "precision_slab": ((512, 512, 128), 3.0, 2, 1e-4, 1e-4, 0.0, False, np.float32, 100),
+    # and its 512-point z passes (rows of 257 complex values) on a quarter of
+    # the x and y extents (a 142 MB spectrum, larger than L2)
+    "precision_rows": ((256, 256, 512), 3.0, 2, 1e-4, 1e-4, 0.0, False, np.float32, 100),
 }
 
 
