@@ -502,6 +502,15 @@ __device__ __forceinline__ void tile_clamp(V (&v)[rp_elems(L, CAP)], int t, int 
   constexpr bool ABS = MODE == MODE_FCI || MODE == MODE_FC;  // the all-abs box
   bool hit = false;
   T fm = T(0);  // max(|Re|, |Im|) after the all-abs clamp
+  // SPLIT: the same as an upper bound of the float-float values,
+  // |hi| + |lo| rounded up
+  float fms = 0.0f;
+  auto ffmag = [](const V &w) {
+    if constexpr (SPLIT)
+      return fmaxf(__fadd_ru(fabsf(w.x.hi), fabsf(w.x.lo)), __fadd_ru(fabsf(w.y.hi), fabsf(w.y.lo)));
+    else
+      return 0.0f;
+  };
   // split FCI: |hi| below this is inside the box (0 when delta is too small
   // for the margin to mean anything: every coefficient decides in FP64)
   const float dlo = SPLIT ? (float)((double)ca.delta * (1.0 - 0x1p-20)) : 0.0f;
@@ -530,7 +539,10 @@ __device__ __forceinline__ void tile_clamp(V (&v)[rp_elems(L, CAP)], int t, int 
       if constexpr (SPLIT) {  // the box in FP64; unclamped values keep their split form
         // hi is within 2^-23 of the value: well inside the box, nothing to
         // decide in FP64 (the pointwise box always decides in FP64)
-        if (ABS && fabsf(v[i].x.hi) < dlo && fabsf(v[i].y.hi) < dlo) continue;
+        if (ABS && fabsf(v[i].x.hi) < dlo && fabsf(v[i].y.hi) < dlo) {
+          fms = fmaxf(fms, ffmag(v[i]));
+          continue;
+        }
         const VG g = cvt<T>(v[i]);
         VG h;
         if (ABS) {
@@ -541,6 +553,7 @@ __device__ __forceinline__ void tile_clamp(V (&v)[rp_elems(L, CAP)], int t, int 
         }
         if (h.x != g.x) v[i].x = C((double)h.x);
         if (h.y != g.y) v[i].y = C((double)h.y);
+        if (ABS) fms = fmaxf(fms, ffmag(v[i]));
       } else if (ABS) {
         v[i] = freq_clamp<T>(v[i], ca.delta, fedits, k, H, hit);
         fm = fmax(fm, fmax(fabs((T)v[i].x), fabs((T)v[i].y)));
@@ -552,6 +565,7 @@ __device__ __forceinline__ void tile_clamp(V (&v)[rp_elems(L, CAP)], int t, int 
   }
   mark_dirty(ca.fdirty, hit);
   if constexpr (ABS && !SPLIT) record_fmax(ca.fmax, fm);
+  if constexpr (ABS && SPLIT) record_fmax(ca.fmax, fms);
 }
 
 // ---------------------------------------------------------------------------

@@ -1418,8 +1418,9 @@ int strict_finish(ffcz_solver *s, int max_iter, double tol, int max_rounds, int 
   double cs = 0.0, cf = 0.0, cb = 0.0;
   int cok = 0, how = 0;
   // the clamp pass's recorded maximum describes e only after a loop that
-  // converged on a frequency projection (no final spatial clamp since)
-  const bool recorded = !s->split && s->h_ctl->converged && s->h_ctl->iterations >= 1;
+  // converged on a frequency projection (no final spatial clamp since);
+  // the float-float passes record an upper bound of their values too
+  const bool recorded = s->h_ctl->converged && s->h_ctl->iterations >= 1;
   FFCZ_TRY(certify<T>(s, true, Et, recorded, &cs, &cf, &cb, &cok, &how));
   s->extracted = false;
   s->cert_ok = cok;

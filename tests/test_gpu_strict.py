@@ -94,3 +94,28 @@ def test_strict_needs_an_all_abs_solve(cuda):
         with pytest.raises(F.FFCzError) as ei:
             s.strict_finish()
         assert ei.value.code == -1  # the pointwise box is not the all-abs box
+
+
+@pytest.mark.parametrize("c", [1e3, 1.0])
+def test_split_precision_strict_finish(cuda, c):
+    """FP64 fields on the float-float passes: the fused pass records an upper
+    bound of the clamped spectrum's |Re|, |Im| (|hi| + |lo| rounded up), so
+    after a loop that converged well inside the frequency box the strict
+    finish certifies both bounds from it without an FP64 transform (c = 1e3:
+    no coefficient reaches the box); with clamps at the bound (c = 1) it
+    decides otherwise.  Either way both
+    bounds hold under the oracle's numpy FP64 check."""
+    shape = (8, 128, 256)
+    fld, e0, delta = setup(shape, np.float64, 23, c)
+    with F.ProjectionSolver(*shape, dtype=np.float64) as s:
+        s.set_precision(F.FFCZ_PRECISION_SPLIT)
+        s.initialize_all_abs(fld.x, fld.eps, delta)
+        s.solve_all_abs(e0, 100, 1e-7)
+        st = s.strict_finish(100, 1e-7, 4)
+        e = s.get_results()
+    chk = O.check_bounds(np.zeros(1), e, fld.eps, delta)
+    assert st["met"] and chk["spatial_max"] <= fld.eps and chk["freq_max"] <= delta, (st, chk)
+    if c > 10:
+        assert st["certified_by"] == "recorded clamp maximum", st
+        # the recorded maximum plus the rounding bound covers the final spectrum
+        assert st["cert_freq_max"] + st["cert_bound"] >= chk["freq_max"]
