@@ -2444,6 +2444,7 @@ int ffcz_batch_set_stream(ffcz_batch *b, void *stream) {
 int ffcz_batch_reset_edit_accumulators(ffcz_batch *b) {
   if (!b) return fail(FFCZ_ERR_INVALID, "batch is NULL");
   for (ffcz_solver *s : b->f) FFCZ_CUDA(cudaStreamSynchronize(s->stream));
+  for (ffcz_solver *s : b->f) FFCZ_TRY(ensure_extracted(s));  // a pending compaction reads the arrays first
   for (ffcz_solver *s : b->f) FFCZ_TRY(clear_accumulators(s, b->stream));
   FFCZ_CUDA(cudaStreamSynchronize(b->stream));
   return FFCZ_OK;
@@ -2506,7 +2507,8 @@ int ffcz_batch_solve_pair_device(ffcz_batch *b, const void *const *d_orig, const
     s->pro_last = PRO_DIFF;
     s->npass = 0;  // pass times are recorded by single-field solves only
     s->launches = 1 + (long long)s->h_ctl->iterations * s->kernels_per_iter + 1 +
-                  (s->pack_mode == FFCZ_PACK_CORRECT ? 6 : 8);
+                  (s->pack_mode == FFCZ_PACK_CORRECT ? 7 : 9);  // compaction: 3 per accumulator, the listed
+                                                                // fold-in, 2 reference-mode packs
     FFCZ_TRY(finish_extract(s));
   }
   return FFCZ_OK;
