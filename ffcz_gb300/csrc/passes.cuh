@@ -253,27 +253,73 @@ __global__ void __launch_bounds__(sizeof(T) == 4 ? 512 : 256) k_zfwd(const T *__
 }
 
 // ---------------------------------------------------------------------------
-// Block-wide max of a non-negative value, folded into ctl->viol_bits.
+// Statistics of the e that a z-inverse pass writes, for the strict finish
+// after a loop that converged (its last pass wrote the final e): per block
+// its sum of squares and its max |e| (zpart[2 block + 0, 1]; no atomics on
+// one address).  The sum runs in T over at most ZS_TERMS values per thread,
+// then over the warp's five-level tree (or in FP64 past ZS_TERMS values),
+// then in FP64.
+constexpr int ZS_TERMS = 64;
+
+// One output value of a z-inverse pass: |v| into the running max and its
+// square into the running sum (one max with an |.| operand and one FMA).
 template <typename T>
-__device__ __forceinline__ void block_max_to_ctl(T v, LoopCtl *ctl) {
-  __shared__ T red[32];
+__device__ __forceinline__ void zs_note(T v, T &amax, T &ssq) {
+  amax = fmax(amax, fabs(v));
+  ssq = fma(v, v, ssq);
+}
+
+// Block-wide reductions of a z-inverse pass: the violation max(|e|-eps, 0)
+// to ctl->viol_bits (atomicMax of the bits, only by blocks that have one;
+// the violation of the largest |e| is the largest violation, rounding being
+// monotonic), the block's sum of squares and max |e| to zpart.  The sum
+// runs in Q (T: the warps' five-level trees in T, then FP64 over the warps
+// in a fixed order, so that FP32 data keeps the FP64 pipe to a few
+// operations per block).  HAS_V: the caller also passes a violation of its
+// own (vmax), folded in with the one of amax.
+template <typename T, bool HAS_V = false, typename Q>
+__device__ __forceinline__ void block_stats_to_ctl(T amax, Q qt, T eps, LoopCtl *ctl, double *zpart,
+                                                   T vmax = T(0)) {
+  __shared__ T ra[32], rv[HAS_V ? 32 : 1];
+  __shared__ double rq[32];
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
-    const T u = __shfl_xor_sync(0xffffffffu, v, o);
-    v = u > v ? u : v;
+    const T w = __shfl_xor_sync(0xffffffffu, amax, o);
+    amax = w > amax ? w : amax;
+    qt += __shfl_xor_sync(0xffffffffu, qt, o);
+    if constexpr (HAS_V) {
+      const T u = __shfl_xor_sync(0xffffffffu, vmax, o);
+      vmax = u > vmax ? u : vmax;
+    }
   }
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  if (lane == 0) red[warp] = v;
+  if (lane == 0) {
+    ra[warp] = amax;
+    rq[warp] = (double)qt;
+    if constexpr (HAS_V) rv[warp] = vmax;
+  }
   __syncthreads();
   if (warp == 0) {
     const int nw = (blockDim.x + 31) >> 5;
-    v = lane < nw ? red[lane] : T(0);
+    amax = lane < nw ? ra[lane] : T(0);
+    double q = lane < nw ? rq[lane] : 0.0;
+    if constexpr (HAS_V) vmax = lane < nw ? rv[lane] : T(0);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-      const T u = __shfl_xor_sync(0xffffffffu, v, o);
-      v = u > v ? u : v;
+      const T w = __shfl_xor_sync(0xffffffffu, amax, o);
+      amax = w > amax ? w : amax;
+      q += __shfl_xor_sync(0xffffffffu, q, o);
+      if constexpr (HAS_V) {
+        const T u = __shfl_xor_sync(0xffffffffu, vmax, o);
+        vmax = u > vmax ? u : vmax;
+      }
     }
-    if (lane == 0 && v > T(0)) atomicMax(&ctl->viol_bits, to_bits<T>(v));
+    if (lane == 0) {
+      if (amax > eps) vmax = max(vmax, amax - eps);
+      if (vmax > T(0)) atomicMax(&ctl->viol_bits, to_bits<T>(vmax));
+      zpart[2 * blockIdx.x] = q;
+      zpart[2 * blockIdx.x + 1] = (double)amax;
+    }
   }
 }
 
@@ -287,8 +333,8 @@ __device__ __forceinline__ void block_max_to_ctl(T v, LoopCtl *ctl) {
 // real part.
 template <typename T, int EPT>
 __global__ void __launch_bounds__(sizeof(T) == 4 ? 512 : 256) k_zinv(const c2<T> *__restrict__ spec, T *__restrict__ e,
-                                              T eps, T factor, LoopCtl *ctl, ZArgs z, AxisPlan p,
-                                              const c2<T> *__restrict__ post) {
+                                              T eps, T factor, LoopCtl *ctl, double *zpart, ZArgs z,
+                                              AxisPlan p, const c2<T> *__restrict__ post) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   c2<T> *buf = reinterpret_cast<c2<T> *>(smem_raw);
   const int tid = threadIdx.x, nthr = blockDim.x;
@@ -338,7 +384,9 @@ __global__ void __launch_bounds__(sizeof(T) == 4 ? 512 : 256) k_zinv(const c2<T>
     }
     __syncthreads();
     fft_tile<T, +1, EPT>(buf, p, P, z.log2TW, tid, nthr);
-    T vmax = T(0);
+    T amax = T(0), ssq = T(0);
+    double dsq = 0.0;
+    int terms = 0;
     const int tot2 = M * z.TW;
     for (int it = tid; it < tot2; it += nthr) {
       const int c = it / M;
@@ -348,12 +396,17 @@ __global__ void __launch_bounds__(sizeof(T) == 4 ? 512 : 256) k_zinv(const c2<T>
       c2<T> o;
       o.x = v.x * factor;
       o.y = v.y * factor;
-      *reinterpret_cast<c2<T> *>(e + (row0 + c) * (long long)z.Nz + 2 * n) = o;
-      const T a0 = fabs(o.x), a1 = fabs(o.y);
-      if (a0 > eps) vmax = max(vmax, a0 - eps);
-      if (a1 > eps) vmax = max(vmax, a1 - eps);
+      const long long i = (row0 + c) * (long long)z.Nz + 2 * n;
+      *reinterpret_cast<c2<T> *>(e + i) = o;
+      zs_note<T>(o.x, amax, ssq);
+      zs_note<T>(o.y, amax, ssq);
+      if ((terms += 2) == ZS_TERMS) {
+        dsq += (double)ssq;
+        ssq = T(0);
+        terms = 0;
+      }
     }
-    block_max_to_ctl<T>(vmax, ctl);
+    block_stats_to_ctl<T>(amax, dsq + (double)ssq, eps, ctl, zpart);
   } else {
     const int L = z.Nz;
     // Hermitian extension: rows Hz..L-1 from conj of rows L-Hz+1..1.
@@ -367,17 +420,24 @@ __global__ void __launch_bounds__(sizeof(T) == 4 ? 512 : 256) k_zinv(const c2<T>
     for (int c = tid; c < z.TW; c += nthr) buf[c].y = T(0);
     __syncthreads();
     fft_tile<T, +1, EPT>(buf, p, P, z.log2TW, tid, nthr);
-    T vmax = T(0);
+    T amax = T(0), ssq = T(0);
+    double dsq = 0.0;
+    int terms = 0;
     for (int it = tid; it < L * z.TW; it += nthr) {
       const int c = it / L;
       const int n = it - c * L;
       if (c >= nrows) continue;
       const T o = buf[n * P + c].x * factor;
-      e[(row0 + c) * (long long)z.Nz + n] = o;
-      const T a0 = fabs(o);
-      if (a0 > eps) vmax = max(vmax, a0 - eps);
+      const long long i = (row0 + c) * (long long)z.Nz + n;
+      e[i] = o;
+      zs_note<T>(o, amax, ssq);
+      if (++terms == ZS_TERMS) {
+        dsq += (double)ssq;
+        ssq = T(0);
+        terms = 0;
+      }
     }
-    block_max_to_ctl<T>(vmax, ctl);
+    block_stats_to_ctl<T>(amax, dsq + (double)ssq, eps, ctl, zpart);
   }
 }
 

@@ -699,12 +699,13 @@ __global__ void __launch_bounds__((M / rp_elems(M, 8)) << LGTW) ks_zfwd(const T 
 // registers (imaginary parts of X[0] and X[M] ignored).
 template <typename T, int M, int LGTW, bool SPLIT = false>
 __global__ void __launch_bounds__((M / rp_elems(M, 8)) << LGTW) ks_zinv(const c2<T> *__restrict__ spec, T *__restrict__ e,
-                                                          T eps, T factor, LoopCtl *ctl, ZArgs z, AxisPlan p,
-                                                          const c2<T> *__restrict__ post) {
+                                                          T eps, T factor, LoopCtl *ctl, double *zpart,
+                                                          ZArgs z, AxisPlan p, const c2<T> *__restrict__ post) {
   using C = std::conditional_t<SPLIT, ff, T>;  // float-float for split FP64
   using V = c2<C>;
   using VG = c2<T>;
   constexpr int E = rp_elems(M, 8), TC = M / E;
+  static_assert(2 * E <= ZS_TERMS, "a thread sums at most ZS_TERMS squares in T");
   using LY = RowLayout<row_pitch(M, sizeof(T)), zl_b(M, sizeof(T))>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   V *buf = reinterpret_cast<V *>(smem_raw);
@@ -739,8 +740,11 @@ __global__ void __launch_bounds__((M / rp_elems(M, 8)) << LGTW) ks_zinv(const c2
     for (int i = 0; i < E; ++i) v[i] = mkc<C>(C(0), C(0));
   }
   RRun<C, +1, M, LY, 0, 8, C>::run(v, buf, t, c, p);
-  T vmax = T(0);
+  T amax = T(0), ssq = T(0);
   if constexpr (SPLIT) {
+    // no statistics (they would need FP64 arithmetic on every value): a sum
+    // that is not a number tells the strict finish to make its own pass
+    T vmax = T(0);
     if (live) {
       // float-float normalisation; the violation in FP64 only where an FP32
       // look at hi cannot rule it out (|o| <= |hi|(1 + 2^-23) < eps below elo)
@@ -764,6 +768,7 @@ __global__ void __launch_bounds__((M / rp_elems(M, 8)) << LGTW) ks_zinv(const c2
         }
       }
     }
+    block_stats_to_ctl<T, true>(T(0), __longlong_as_double(0x7ff8000000000000ll), eps, ctl, zpart, vmax);
   } else if (live) {
     T *out = e + row * (long long)(2 * M);
 #pragma unroll
@@ -773,12 +778,11 @@ __global__ void __launch_bounds__((M / rp_elems(M, 8)) << LGTW) ks_zinv(const c2
       o.x = u.x * factor;
       o.y = u.y * factor;
       *reinterpret_cast<VG *>(out + 2 * last_pos<M, +1, 8>(t, i)) = o;
-      const T a0 = fabs(o.x), a1 = fabs(o.y);
-      if (a0 > eps) vmax = max(vmax, a0 - eps);
-      if (a1 > eps) vmax = max(vmax, a1 - eps);
+      zs_note<T>(o.x, amax, ssq);
+      zs_note<T>(o.y, amax, ssq);
     }
   }
-  block_max_to_ctl<T>(vmax, ctl);
+  if constexpr (!SPLIT) block_stats_to_ctl<T>(amax, ssq, eps, ctl, zpart);
 }
 
 }  // namespace ffcz

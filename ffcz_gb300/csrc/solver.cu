@@ -118,6 +118,15 @@ struct ffcz_solver {
   // clamp has written it since its last clear ([0] = count, [4..] =
   // indices; see k_ex_listed)
   unsigned *d_slist = nullptr;
+  // statistics of the e written by the last z-inverse pass: per block its
+  // sum of squares and max |e| (zpart), valid for the strict finish while
+  // zstat_ok (a loop ran and nothing changed e since) over zstat_nblk
+  // blocks; zhot: the strict finish's list of blocks to clamp (two counts,
+  // then block indices)
+  double *d_zpart = nullptr;
+  unsigned *d_zhot = nullptr;
+  bool zstat_ok = false;
+  unsigned zstat_nblk = 0;
   void *d_mnmx = nullptr;
   size_t nblk_max = 0;
   unsigned long long *d_up_blk = nullptr;  // decoder: set flags per chunk (lazy)
@@ -207,6 +216,14 @@ int pick_tile(int rows_smem, int L, size_t es2, int twmax, Launch &ln, int &TW, 
 }
 
 template <typename T> constexpr int ept_of() { return sizeof(T) == 4 ? 8 : 4; }
+
+// The strict finish's spatial limit: the largest T <= eps.
+template <typename T>
+T strict_lim(double eps) {
+  T t = (T)eps;
+  if ((double)t > eps) t = std::nextafter(t, T(0));
+  return t;
+}
 
 template <typename T, int E>
 int set_smem_attrs_e() {
@@ -705,8 +722,8 @@ void launch_iteration(ffcz_solver *s, cudaStream_t st, int pro, const void *a, c
     mark();
   }
   const T factor = T(1) / static_cast<T>(s->N);
-  ((ZinvFn<T>)s->kzi)<<<s->lz_i.grid, s->lz_i.threads, s->lz_i.smem, st>>>(spec, tp<T>(s->d_e), eps, factor,
-                                                                          s->d_ctl, s->za, s->pz, post);
+  ((ZinvFn<T>)s->kzi)<<<s->lz_i.grid, s->lz_i.threads, s->lz_i.smem, st>>>(
+      spec, tp<T>(s->d_e), eps, factor, s->d_ctl, s->d_zpart, s->za, s->pz, post);
   mark();
   if (record) s->npass = ne - 1;
   k_check<T><<<1, 1, 0, st>>>(s->d_ctl, tol, max_iter, h, use_graph, s->d_sdirty);
@@ -819,6 +836,7 @@ int project(ffcz_solver *s, int pro, const void *a, const void *b, int max_iter,
   const T tol = (T)tol_d;
   s->pro_last = pro;
   s->extracted = false;
+  s->zstat_ok = false;
   if (max_iter <= 0) {
     k_init_ctl<<<1, 1, 0, s->stream>>>(s->d_ctl);
     const unsigned g = (unsigned)std::min<size_t>(ceil_div(s->N, 256), 152 * 16);
@@ -837,6 +855,8 @@ int project(ffcz_solver *s, int pro, const void *a, const void *b, int max_iter,
   FFCZ_CUDA(cudaStreamSynchronize(s->stream));
   s->launches = 1 + (long long)s->h_ctl->iterations * s->kernels_per_iter + 1;
   if (s->h_ctl->err) return fail(FFCZ_ERR_CUDA, "a TMA-staged pass gave up waiting for its tile copies");
+  s->zstat_ok = true;  // the last z inverse's statistics describe e (unless a final clamp followed)
+  s->zstat_nblk = s->lz_i.grid;
   return FFCZ_OK;
 }
 
@@ -939,7 +959,7 @@ void free_all(ffcz_solver *s) {
   for (LoopGraph &g : s->lg) g.reset();
   void *bufs[] = {s->d_x, s->d_e, s->d_spec, s->d_fedits, s->d_sedits, s->d_fcompact, s->d_scompact,
                   s->d_fquant, s->d_squant, s->d_fpack, s->d_spack, s->d_tw, s->d_ctl, s->d_ex_rec, s->d_fdirty, s->d_sdirty,
-                  s->d_slist, s->d_mnmx, s->d_tw_ff};
+                  s->d_slist, s->d_mnmx, s->d_tw_ff, s->d_zpart, s->d_zhot};
   for (void *p : bufs)
     if (p) cudaFree(p);
   if (s->d_up_blk) cudaFree(s->d_up_blk);
@@ -1025,8 +1045,9 @@ int reconstruct(ffcz_solver *s, const void *d_decomp, const uint16_t *fq, size_t
   }
   const c2<T> *post = post_table<T>(s);
   const T factor = T(1) / static_cast<T>(s->N);
+  s->zstat_ok = false;  // e is rewritten below
   ((ZinvFn<T>)s->kzi)<<<s->lz_i.grid, s->lz_i.threads, s->lz_i.smem, st>>>(spec, tp<T>(s->d_e), (T)s->eps, factor,
-                                                                          s->d_ctl, s->za, s->pz, post);
+                                                                          s->d_ctl, s->d_zpart, s->za, s->pz, post);
   FFCZ_CUDA(cudaMemsetAsync(s->d_sedits, 0, s->N * s->es, st));
   if (ns) FFCZ_TRY(unpack_edits<T>(s, sq, ns, spack, s->N, smin, smax, s->d_spack, s->spack_bytes, tp<T>(s->d_sedits),
                                    nullptr));
@@ -1197,6 +1218,73 @@ __global__ void __launch_bounds__(256) k_clamp_stats(T *__restrict__ e, T *__res
   }
 }
 
+// The strict clamp after a converged loop, from its last z inverse's
+// per-block statistics instead of a pass over e.  Step 1, over the z
+// inverse's blocks in kZsScan contiguous ranges (one per block of this
+// kernel): each range's sum of squares and max |e| to out[2 g + 0, 1] (the
+// host adds the sums in range order), the blocks whose maximum exceeds lim
+// appended to hot[3..] (hot[0] counts them; hot[0..2] start at zero), and
+// hot[2] set when a sum is not a number (e holds a NaN: nothing is
+// clamped and the caller makes a full pass).
+constexpr int kZsScan = 64;
+__global__ void __launch_bounds__(512) k_zstat_scan(const double *__restrict__ zpart, unsigned nblk, double lim,
+                                                    unsigned *__restrict__ hot, double *__restrict__ out) {
+  __shared__ double ws[16], wm[16];
+  const unsigned per = (nblk + gridDim.x - 1) / gridDim.x;
+  const unsigned b0 = blockIdx.x * per, b1 = min(b0 + per, nblk);
+  double q = 0.0, m = 0.0;
+  for (unsigned b = b0 + threadIdx.x; b < b1; b += blockDim.x) {
+    const double bm = zpart[2 * (size_t)b + 1];
+    q += zpart[2 * (size_t)b];
+    m = fmax(m, bm);
+    if (bm > lim) hot[3 + atomicAdd(&hot[0], 1u)] = b;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    q += __shfl_down_sync(0xffffffffu, q, o);
+    m = fmax(m, __shfl_down_sync(0xffffffffu, m, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    ws[threadIdx.x >> 5] = q;
+    wm[threadIdx.x >> 5] = m;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+      t += ws[w];
+      m = fmax(m, wm[w]);
+    }
+    out[2 * blockIdx.x] = t;
+    out[2 * blockIdx.x + 1] = m;
+    if (!(t >= 0.0)) atomicOr(&hot[2], 1u);
+  }
+}
+
+// Step 2: clamps the values above lim in the listed blocks' rows (span
+// values from block b * span; the edits go to the spatial accumulator,
+// listed as k_clamp_stats lists them) and counts them in hot[1]; nothing
+// when hot[2] is set.
+template <typename T>
+__global__ void __launch_bounds__(256) k_zstat_clamp(T *__restrict__ e, T *__restrict__ sedits, T lim,
+                                                     long long span, long long n, unsigned *sdirty, unsigned *slist,
+                                                     unsigned *__restrict__ hot) {
+  const unsigned nh = hot[2] ? 0u : hot[0];
+  unsigned c = 0;
+  for (unsigned h = blockIdx.x; h < nh; h += gridDim.x) {
+    const long long lo = (long long)hot[3 + h] * span, hi = min(lo + span, n);
+    for (long long i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+      const T v0 = e[i];
+      const T v = spatial_clamp(v0, lim, sedits, i);
+      if (v != v0) {
+        e[i] = v;
+        ex_list_record(sdirty, slist, i);
+        ++c;
+      }
+    }
+  }
+  if (c) atomicAdd(&hot[1], c);
+}
+
 // Times the default and the alternative tile of each compile-time pass on
 // the solver's own buffers (z forward + z inverse; y forward + y inverse;
 // the fused pass, with no clamp firing) and keeps the faster.  Every
@@ -1205,6 +1293,7 @@ __global__ void __launch_bounds__(256) k_clamp_stats(T *__restrict__ e, T *__res
 template <typename T>
 int autotune(ffcz_solver *s, int reps, double *ms6) {
   cudaStream_t st = s->stream;
+  s->zstat_ok = false;  // the timed passes overwrite e
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   FFCZ_CUDA(cudaEventCreate(&e0));
   FFCZ_CUDA(cudaEventCreate(&e1));
@@ -1235,8 +1324,8 @@ int autotune(ffcz_solver *s, int reps, double *ms6) {
   auto zrun = [&]() {
     ((ZfwdFn<T>)s->kzf[PRO_PLAIN])<<<s->lz_f.grid, s->lz_f.threads, s->lz_f.smem, st>>>(
         (const T *)s->d_x, nullptr, tp<T>(s->d_sedits), (T)s->eps, spec, s->za, s->pz, post);
-    ((ZinvFn<T>)s->kzi)<<<s->lz_i.grid, s->lz_i.threads, s->lz_i.smem, st>>>(spec, tp<T>(s->d_e), (T)s->eps,
-                                                                            T(1), s->d_ctl, s->za, s->pz, post);
+    ((ZinvFn<T>)s->kzi)<<<s->lz_i.grid, s->lz_i.threads, s->lz_i.smem, st>>>(
+        spec, tp<T>(s->d_e), (T)s->eps, T(1), s->d_ctl, s->d_zpart, s->za, s->pz, post);
   };
   if (s->static_z) {
     for (int var = 0; var < 2; ++var)
@@ -1340,20 +1429,57 @@ int certify(ffcz_solver *s, bool clamp, T eps_t, bool use_recorded, double *smax
   unsigned long long *mx = (unsigned long long *)(partial + 3 * 152 * 16);
   FFCZ_CUDA(cudaMemsetAsync(mx, 0, 2 * sizeof(unsigned long long), st));
   const T lim = clamp ? eps_t : std::numeric_limits<T>::infinity();
-  k_clamp_stats<T><<<g, 256, 0, st>>>(tp<T>(s->d_e), tp<T>(s->d_sedits), lim, (long long)s->N, s->d_sdirty,
-                                      s->d_slist, partial, mx);
-  FFCZ_CUDA(cudaGetLastError());
-  std::vector<double> h(3 * g + 1);
-  FFCZ_CUDA(cudaMemcpyAsync(h.data(), partial, 3 * g * sizeof(double), cudaMemcpyDeviceToHost, st));
-  FFCZ_CUDA(cudaMemcpyAsync(h.data() + 3 * g, mx, sizeof(double), cudaMemcpyDeviceToHost, st));
-  FFCZ_CUDA(cudaStreamSynchronize(st));
+  const double inf = std::numeric_limits<double>::infinity();
   double pre = 0.0, post = 0.0, chg = 0.0;
-  for (unsigned i = 0; i < g; ++i) {
-    pre += h[3 * i];
-    post += h[3 * i + 1];
-    chg += h[3 * i + 2];
+  // terms each thread summed in T before its sum went to FP64
+  double k = std::ceil((double)s->N / ((double)g * 256.0)) + 16.0;  // + one vector of the tail
+  bool stats = false;
+  if (clamp && use_recorded && s->zstat_ok && !s->zsplit) {
+    // the loop's last z inverse wrote e and its per-block statistics: clamp
+    // only the rows of the blocks whose maximum exceeds lim
+    s->zstat_ok = false;
+    FFCZ_CUDA(cudaMemsetAsync(s->d_zhot, 0, 3 * sizeof(unsigned), st));
+    k_zstat_scan<<<kZsScan, 512, 0, st>>>(s->d_zpart, s->zstat_nblk, (double)lim, s->d_zhot, partial);
+    const unsigned gc = (unsigned)std::min<size_t>(s->zstat_nblk, 152 * 8);
+    k_zstat_clamp<T><<<gc, 256, 0, st>>>(tp<T>(s->d_e), tp<T>(s->d_sedits), lim, (long long)s->za.TW * s->nz,
+                                         (long long)s->N, s->d_sdirty, s->d_slist, s->d_zhot);
+    FFCZ_CUDA(cudaGetLastError());
+    double h[2 * kZsScan];
+    unsigned hc[3];
+    FFCZ_CUDA(cudaMemcpyAsync(h, partial, sizeof(h), cudaMemcpyDeviceToHost, st));
+    FFCZ_CUDA(cudaMemcpyAsync(hc, s->d_zhot, sizeof(hc), cudaMemcpyDeviceToHost, st));
+    FFCZ_CUDA(cudaStreamSynchronize(st));
+    double q = 0.0, amax = 0.0;
+    for (int i = 0; i < kZsScan; ++i) {
+      q += h[2 * i];
+      amax = std::fmax(amax, h[2 * i + 1]);
+    }
+    if (!hc[2] && q >= 0.0) {
+      stats = true;
+      pre = post = q;  // the clamp only shrinks values: pre bounds post
+      const double cnt = (double)hc[1];
+      *smax = cnt > 0.0 ? (double)lim : amax;
+      // every clamped value moved by at most amax - lim
+      chg = cnt > 0.0 ? std::nextafter(cnt * std::nextafter(amax - (double)lim, inf), inf) : 0.0;
+      k = (double)ZS_TERMS + 8.0;  // a thread's terms and the warp's tree, in T
+    }
   }
-  std::memcpy(smax, &h[3 * g], 8);
+  if (!stats) {
+    k_clamp_stats<T><<<g, 256, 0, st>>>(tp<T>(s->d_e), tp<T>(s->d_sedits), lim, (long long)s->N, s->d_sdirty,
+                                        s->d_slist, partial, mx);
+    FFCZ_CUDA(cudaGetLastError());
+    std::vector<double> h(3 * g + 1);
+    FFCZ_CUDA(cudaMemcpyAsync(h.data(), partial, 3 * g * sizeof(double), cudaMemcpyDeviceToHost, st));
+    FFCZ_CUDA(cudaMemcpyAsync(h.data() + 3 * g, mx, sizeof(double), cudaMemcpyDeviceToHost, st));
+    FFCZ_CUDA(cudaStreamSynchronize(st));
+    for (unsigned i = 0; i < g; ++i) {
+      pre += h[3 * i];
+      post += h[3 * i + 1];
+      chg += h[3 * i + 2];
+    }
+    std::memcpy(smax, &h[3 * g], 8);
+  }
+  if (clamp) s->zstat_ok = false;
   auto clog2 = [](size_t n) {
     int l = 0;
     while (((size_t)1 << l) < n) ++l;
@@ -1363,10 +1489,8 @@ int certify(ffcz_solver *s, bool clamp, T eps_t, bool use_recorded, double *smax
   const double u = sizeof(T) == 4 ? 0x1p-24 : (s->split ? 0x1p-44 : 0x1p-53);
   const double beta = 16.0 * u * (double)L;
   const double N = (double)s->N;
-  const double inf = std::numeric_limits<double>::infinity();
   // each thread summed at most k terms in T (relative rounding <= (k+1) u
   // for non-negative terms), the FP64 tree above it at most N u_64: widen
-  const double k = std::ceil(N / ((double)g * 256.0)) + 16.0;  // + one vector of the tail
   const double widen = (1.0 + (k + 2.0) * u) * 1.001;
   pre *= widen;
   post *= widen;
@@ -1406,8 +1530,7 @@ int strict_finish(ffcz_solver *s, int max_iter, double tol, int max_rounds, int 
   if (max_rounds < 0 || max_iter < 1) return fail(FFCZ_ERR_INVALID, "max_rounds < 0 or max_iter < 1");
   Range rg("ffcz:strict_finish");
   const double E = s->eps, D = s->delta;
-  T Et = (T)E;
-  if ((double)Et > E) Et = std::nextafter(Et, T(0));
+  const T Et = strict_lim<T>(E);
   const bool was_extracted = s->extracted;
   cudaStream_t st = s->stream;
   const unsigned g = (unsigned)std::min<size_t>(ceil_div(s->N, 256), 152 * 16);
@@ -1437,6 +1560,7 @@ int strict_finish(ffcz_solver *s, int max_iter, double tol, int max_rounds, int 
                                         s->d_sdirty);
     FFCZ_CUDA(cudaGetLastError());
     s->extracted = false;
+    s->zstat_ok = false;
     if ((rc = ffcz_verify_bounds(s, &sm, &fm)) != FFCZ_OK) break;
     if ((sm <= E && fm <= D) || r == max_rounds) break;
     dt -= 2.0 * (fm - D);  // twice the worst overshoot of the last check
@@ -1573,6 +1697,9 @@ int ffcz_solver_create(size_t nx, size_t ny, size_t nz, int dtype, ffcz_solver *
   if (rc == FFCZ_OK) rc = alloc((void **)&s->d_fdirty, sizeof(unsigned));
   if (rc == FFCZ_OK) rc = alloc((void **)&s->d_sdirty, sizeof(unsigned));
   if (rc == FFCZ_OK) rc = alloc((void **)&s->d_slist, (EX_LIST_MAX + 4) * sizeof(unsigned));
+  // a sum and a maximum per z-inverse block, at most one block per row
+  if (rc == FFCZ_OK) rc = alloc((void **)&s->d_zpart, 2 * (size_t)s->rows * sizeof(double));
+  if (rc == FFCZ_OK) rc = alloc((void **)&s->d_zhot, (3 + (size_t)s->rows) * sizeof(unsigned));
   if (rc == FFCZ_OK) rc = alloc(&s->d_mnmx, 4 * es);
   if (rc == FFCZ_OK) {
     cudaError_t e = cudaMallocHost(&s->h_ctl, sizeof(LoopCtl));
@@ -2506,6 +2633,8 @@ int ffcz_batch_solve_pair_device(ffcz_batch *b, const void *const *d_orig, const
     ffcz_solver *s = b->f[i];
     s->pro_last = PRO_DIFF;
     s->npass = 0;  // pass times are recorded by single-field solves only
+    s->zstat_ok = true;  // as after project(): the last z inverse wrote e
+    s->zstat_nblk = s->lz_i.grid;
     s->launches = 1 + (long long)s->h_ctl->iterations * s->kernels_per_iter + 1 +
                   (s->pack_mode == FFCZ_PACK_CORRECT ? 7 : 9);  // compaction: 3 per accumulator, the listed
                                                                 // fold-in, 2 reference-mode packs

@@ -14,7 +14,7 @@ namespace ffcz {
 template <typename T>
 using ZfwdFn = void (*)(const T *, const T *, T *, T, c2<T> *, ZArgs, AxisPlan, const c2<T> *);
 template <typename T>
-using ZinvFn = void (*)(const c2<T> *, T *, T, T, LoopCtl *, ZArgs, AxisPlan, const c2<T> *);
+using ZinvFn = void (*)(const c2<T> *, T *, T, T, LoopCtl *, double *, ZArgs, AxisPlan, const c2<T> *);
 template <typename T>
 using StridedFn = void (*)(c2<T> *, SArgs, AxisPlan, ClampArgs<T>, T *, long long);
 
