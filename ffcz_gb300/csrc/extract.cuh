@@ -378,12 +378,23 @@ __device__ __forceinline__ unsigned ex_chunk(const T *__restrict__ a, long long 
   return run;
 }
 
+// State of an accumulator's compaction outputs (xst[0]): 1 while its records
+// and flag words hold the results of the untouched (all-zero) array, apart
+// from the flag words listed in xst[2 .. 2 + xst[1]) that the last listed fold
+// set bits in.  While the accumulator is untouched (dirty flag 0) a
+// compaction then needs no pass: no active value, min = max = 0.
+__device__ __forceinline__ bool ex_known_clean(const unsigned *dirty, const unsigned *xst) {
+  return xst && dirty && *dirty == 0u && xst[0] != 0u;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(EX_THREADS, 3) k_ex_part(const T *__restrict__ a, long long n, long long nchunk, T thr,
                                                            const unsigned *__restrict__ dirty,
+                                                           const unsigned *__restrict__ xst,
                                                            T *__restrict__ scratch, ExRec rec,
                                                            unsigned *__restrict__ pack_words, int write_pack) {
   constexpr int CH = xp_chunk<T>(), SPAN = 32 * xp_vec<T>();
+  if (ex_known_clean(dirty, xst)) return;
   __shared__ unsigned scnt[XP_WPG];
   __shared__ unsigned long long smn[XP_WPG], smx[XP_WPG];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -444,9 +455,21 @@ __global__ void __launch_bounds__(EX_THREADS, 3) k_ex_part(const T *__restrict__
 constexpr int XS_THREADS = 1024;
 template <typename T>
 __global__ void __launch_bounds__(XS_THREADS) k_ex_scan_rec(long long ngroup, ExRec rec, T *__restrict__ mnmx,
-                                                            LoopCtl *__restrict__ ctl, int which) {
+                                                            LoopCtl *__restrict__ ctl, int which,
+                                                            const unsigned *__restrict__ dirty,
+                                                            unsigned *__restrict__ xst) {
   constexpr int NW = XS_THREADS / 32;
   __shared__ unsigned long long wa[NW], wb[NW], wc[NW];
+  if (ex_known_clean(dirty, xst)) {  // no active value, min = max = 0
+    if (threadIdx.x == 0) {
+      mnmx[0] = T(0);
+      mnmx[1] = T(0);
+      ctl->count[which] = 0ull;
+      ctl->mn[which] = 0.0;
+      ctl->mx[which] = 0.0;
+    }
+    return;
+  }
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const long long K = (ngroup + XP_PAD - 1) / XP_PAD * (XP_PAD / XS_THREADS);
   const long long r0 = threadIdx.x * K;
@@ -511,14 +534,23 @@ __global__ void __launch_bounds__(XS_THREADS) k_ex_scan_rec(long long ngroup, Ex
     ctl->count[which] = tot;
     ctl->mn[which] = (double)gmn;
     ctl->mx[which] = (double)gmx;
+    // k_ex_part rewrote the records and the flag words: they hold the
+    // untouched array's results exactly when it was untouched
+    if (xst) {
+      xst[0] = (dirty && *dirty == 0u) ? 1u : 0u;
+      xst[1] = 0u;
+    }
   }
 }
 
 template <typename T>
 __global__ void __launch_bounds__(EX_THREADS) k_ex_place(const T *__restrict__ scratch, long long nchunk, ExRec rec,
                                                          T *__restrict__ compact, uint16_t *__restrict__ quant,
-                                                         const T *__restrict__ mnmx) {
+                                                         const T *__restrict__ mnmx,
+                                                         const unsigned *__restrict__ dirty,
+                                                         const unsigned *__restrict__ xst) {
   constexpr int CH = xp_chunk<T>();
+  if (ex_known_clean(dirty, xst)) return;  // nothing to place
   const int lane = threadIdx.x & 31;
   const long long wpb = EX_THREADS / 32;
   const T mn = mnmx[0], mx = mnmx[1];
@@ -572,12 +604,22 @@ __global__ void __launch_bounds__(EX_LIST_THREADS) k_ex_listed(const T *__restri
                                                                 T *__restrict__ compact, uint16_t *__restrict__ quant,
                                                                 unsigned *__restrict__ pack_words, int write_pack,
                                                                 T *__restrict__ mnmx, LoopCtl *__restrict__ ctl,
-                                                                int which) {
+                                                                int which, unsigned *__restrict__ xst) {
   constexpr int PER = EX_LIST_MAX / EX_LIST_THREADS;
   __shared__ unsigned key[EX_LIST_MAX];
   __shared__ unsigned wsum[EX_LIST_THREADS / 32];
   __shared__ unsigned long long wmn[EX_LIST_THREADS / 32], wmx[EX_LIST_THREADS / 32];
   if (*dirty != 0u) return;  // written throughout: the full compaction stands
+  {
+    // the flag words the last fold set bits in go back to zero (the other
+    // words are zero: k_ex_part wrote them, or left them from a compaction
+    // of the untouched array)
+    const unsigned nw = min(xst[1], (unsigned)EX_LIST_MAX);
+    for (unsigned i = threadIdx.x; i < nw; i += EX_LIST_THREADS) pack_words[xst[2 + i]] = 0u;
+    __syncthreads();
+    if (threadIdx.x == 0) xst[1] = 0u;
+    __syncthreads();
+  }
   const unsigned cnt = slist[0];
   if (cnt == 0u) return;     // untouched
   if (cnt > (unsigned)EX_LIST_MAX) {  // (an overflowing recorder marks the array written throughout)
@@ -667,7 +709,10 @@ __global__ void __launch_bounds__(EX_LIST_THREADS) k_ex_listed(const T *__restri
       compact[off] = v[q];
       quant[off] = quantize16<T>(v[q], gmn, gmx);
       ++off;
-      if (write_pack) atomicOr(pack_words + (idx >> 5), 1u << (idx & 31u));
+      if (write_pack) {
+        atomicOr(pack_words + (idx >> 5), 1u << (idx & 31u));
+        xst[2 + atomicAdd(&xst[1], 1u)] = idx >> 5;
+      }
     }
   if (tid == 0) {
     mnmx[0] = gmn;

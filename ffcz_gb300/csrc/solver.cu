@@ -118,6 +118,10 @@ struct ffcz_solver {
   // clamp has written it since its last clear ([0] = count, [4..] =
   // indices; see k_ex_listed)
   unsigned *d_slist = nullptr;
+  // per accumulator: whether its compaction outputs hold the untouched
+  // array's results, and the flag words its last listed fold wrote
+  // (ex_known_clean); 2 + EX_LIST_MAX words each
+  unsigned *d_xs = nullptr;
   // statistics of the e written by the last z-inverse pass: per block its
   // sum of squares and max |e| (zpart), valid for the strict finish while
   // zstat_ok (a loop ran and nothing changed e since) over zstat_nblk
@@ -892,12 +896,13 @@ int extract_one(ffcz_solver *s, cudaStream_t st, const T *a, size_t n, int which
   // the spectrum buffer (>= n values of T) is idle once the loop has ended
   T *scratch = (T *)s->d_spec;
   const int correct = s->pack_mode == FFCZ_PACK_CORRECT;
-  k_ex_part<T><<<(unsigned)ngroup, EX_THREADS, 0, st>>>(a, (long long)n, (long long)nchunk, thr,
-                                                        which == 0 ? s->d_fdirty : s->d_sdirty, scratch, rec,
-                                                        (unsigned *)pack, correct);
-  k_ex_scan_rec<T><<<1, XS_THREADS, 0, st>>>((long long)ngroup, rec, mnmx, s->d_ctl, which);
+  const unsigned *dirty = which == 0 ? s->d_fdirty : s->d_sdirty;
+  unsigned *xs = s->d_xs + (size_t)which * (2 + EX_LIST_MAX);
+  k_ex_part<T><<<(unsigned)ngroup, EX_THREADS, 0, st>>>(a, (long long)n, (long long)nchunk, thr, dirty, xs, scratch,
+                                                        rec, (unsigned *)pack, correct);
+  k_ex_scan_rec<T><<<1, XS_THREADS, 0, st>>>((long long)ngroup, rec, mnmx, s->d_ctl, which, dirty, xs);
   const unsigned gp = (unsigned)std::min<size_t>(ceil_div(nchunk, (size_t)(EX_THREADS / 32)), 152 * 8);
-  k_ex_place<T><<<gp, EX_THREADS, 0, st>>>(scratch, (long long)nchunk, rec, compact, quant, mnmx);
+  k_ex_place<T><<<gp, EX_THREADS, 0, st>>>(scratch, (long long)nchunk, rec, compact, quant, mnmx, dirty, xs);
   s->launches += 3;
   if (!correct) {
     const unsigned g = (unsigned)std::min<size_t>(ceil_div(pack_alloc, 256), 152 * 16);
@@ -906,7 +911,7 @@ int extract_one(ffcz_solver *s, cudaStream_t st, const T *a, size_t n, int which
   }
   if (which == 1) {  // the spatial accumulator may be listed (strict finish's clamp only)
     k_ex_listed<T><<<1, EX_LIST_THREADS, 0, st>>>(a, (long long)n, thr, s->d_sdirty, s->d_slist, compact, quant,
-                                                  (unsigned *)pack, correct, mnmx, s->d_ctl, which);
+                                                  (unsigned *)pack, correct, mnmx, s->d_ctl, which, xs);
     s->launches += 1;
   }
   FFCZ_CUDA(cudaGetLastError());
@@ -959,7 +964,7 @@ void free_all(ffcz_solver *s) {
   for (LoopGraph &g : s->lg) g.reset();
   void *bufs[] = {s->d_x, s->d_e, s->d_spec, s->d_fedits, s->d_sedits, s->d_fcompact, s->d_scompact,
                   s->d_fquant, s->d_squant, s->d_fpack, s->d_spack, s->d_tw, s->d_ctl, s->d_ex_rec, s->d_fdirty, s->d_sdirty,
-                  s->d_slist, s->d_mnmx, s->d_tw_ff, s->d_zpart, s->d_zhot};
+                  s->d_slist, s->d_mnmx, s->d_tw_ff, s->d_zpart, s->d_zhot, s->d_xs};
   for (void *p : bufs)
     if (p) cudaFree(p);
   if (s->d_up_blk) cudaFree(s->d_up_blk);
@@ -998,6 +1003,14 @@ int copy_out(const void *src, size_t bytes, void *dst, size_t cap_bytes, cudaStr
 // Flag pack + codes of one edit array -> dequantised values (spectrum or
 // dense), on the solver's stream.  The pack is copied into the solver's
 // zero-padded pack buffer (whole 32-bit words) unless it already is it.
+// The compaction outputs (records, flag words) are about to be written by
+// something other than a compaction: the next compaction of an untouched
+// accumulator makes its pass again.
+static int forget_clean_outputs(ffcz_solver *s) {
+  FFCZ_CUDA(cudaMemsetAsync(s->d_xs, 0, 2 * (2 + EX_LIST_MAX) * sizeof(unsigned), s->stream));
+  return FFCZ_OK;
+}
+
 template <typename T>
 int unpack_edits(ffcz_solver *s, const uint16_t *quant, size_t count, const uint8_t *pack, size_t n, double mn,
                  double mx, uint8_t *pack_buf, size_t pack_alloc, T *dense, c2<T> *spec) {
@@ -1028,6 +1041,7 @@ int reconstruct(ffcz_solver *s, const void *d_decomp, const uint16_t *fq, size_t
                 double fmin, double fmax, const uint16_t *sq, size_t ns, const uint8_t *spack, double smin,
                 double smax, void *d_out) {
   cudaStream_t st = s->stream;
+  FFCZ_TRY(forget_clean_outputs(s));  // the flag words receive the decoded streams
   const long long H = (long long)s->H;
   c2<T> *spec = (c2<T> *)s->d_spec;
   FFCZ_CUDA(cudaMemsetAsync(s->d_spec, 0, (size_t)s->rows * s->Hzp * 2 * s->es, st));
@@ -1697,6 +1711,7 @@ int ffcz_solver_create(size_t nx, size_t ny, size_t nz, int dtype, ffcz_solver *
   if (rc == FFCZ_OK) rc = alloc((void **)&s->d_fdirty, sizeof(unsigned));
   if (rc == FFCZ_OK) rc = alloc((void **)&s->d_sdirty, sizeof(unsigned));
   if (rc == FFCZ_OK) rc = alloc((void **)&s->d_slist, (EX_LIST_MAX + 4) * sizeof(unsigned));
+  if (rc == FFCZ_OK) rc = alloc((void **)&s->d_xs, 2 * (2 + EX_LIST_MAX) * sizeof(unsigned));
   // a sum and a maximum per z-inverse block, at most one block per row
   if (rc == FFCZ_OK) rc = alloc((void **)&s->d_zpart, 2 * (size_t)s->rows * sizeof(double));
   if (rc == FFCZ_OK) rc = alloc((void **)&s->d_zhot, (3 + (size_t)s->rows) * sizeof(unsigned));
@@ -1719,6 +1734,7 @@ int ffcz_solver_create(size_t nx, size_t ny, size_t nz, int dtype, ffcz_solver *
     if (e == cudaSuccess) e = cudaMemset(s->d_sedits, 0, N * es);
     if (e == cudaSuccess) e = cudaMemset(s->d_sdirty, 0, sizeof(unsigned));
     if (e == cudaSuccess) e = cudaMemset(s->d_slist, 0, sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaMemset(s->d_xs, 0, 2 * (2 + EX_LIST_MAX) * sizeof(unsigned));
     if (e == cudaSuccess) e = xp_init(s.get());
     if (e != cudaSuccess) rc = cuda_fail(e, "cudaMemset", __FILE__, __LINE__);
   }
@@ -1754,6 +1770,7 @@ int ffcz_solver_set_loop_driver(ffcz_solver *s, int driver) {
 int ffcz_solver_set_pack_mode(ffcz_solver *s, int mode) {
   FFCZ_TRY(check_solver(s));
   if (mode != FFCZ_PACK_CORRECT && mode != FFCZ_PACK_REFERENCE) return fail(FFCZ_ERR_INVALID, "unknown pack mode");
+  if (mode != s->pack_mode) FFCZ_TRY(forget_clean_outputs(s));  // the flag words change layout
   s->pack_mode = mode;
   return FFCZ_OK;
 }
@@ -2368,6 +2385,7 @@ int ffcz_solver_decode(ffcz_solver *s, const void *d_decomp, ffcz_huff_result *c
   struct Job { const ffcz_huff_result *r; int sb; void *dst; size_t n; };
   const Job jobs[4] = {{in4[0], 2, s->d_fquant, nf}, {in4[1], 1, s->d_fpack, nf ? fpb : 0},
                        {in4[2], 2, s->d_squant, ns}, {in4[3], 1, s->d_spack, ns ? spb : 0}};
+  FFCZ_TRY(forget_clean_outputs(s));  // the flag words receive the decoded streams
   FFCZ_CUDA(cudaMemsetAsync(s->d_fpack, 0, s->fpack_bytes, s->stream));
   FFCZ_CUDA(cudaMemsetAsync(s->d_spack, 0, s->spack_bytes, s->stream));
   for (const Job &j : jobs) {
