@@ -1435,7 +1435,11 @@ int autotune(ffcz_solver *s, int reps, double *ms6) {
 // *how = 2 (recorded), 1 (transform), 0 (undecided).
 template <typename T>
 int certify(ffcz_solver *s, bool clamp, T eps_t, bool use_recorded, double *smax, double *fmax, double *bound,
-            int *ok, int *how) {
+            int *ok, int *how, bool fold_extract = false, bool *folded = nullptr) {
+  // fold_extract: the compaction of the clamped accumulators joins the
+  // statistics path's kernels ahead of its one synchronisation (*folded
+  // tells whether it ran there and still stands)
+  if (folded) *folded = false;
   cudaStream_t st = s->stream;
   const unsigned g = (unsigned)std::min<size_t>(ceil_div(s->N, 256), 152 * 16);
   if (!s->d_cert) FFCZ_CUDA(cudaMalloc(&s->d_cert, (3 * 152 * 16 + 2) * sizeof(double)));
@@ -1458,6 +1462,10 @@ int certify(ffcz_solver *s, bool clamp, T eps_t, bool use_recorded, double *smax
     k_zstat_clamp<T><<<gc, 256, 0, st>>>(tp<T>(s->d_e), tp<T>(s->d_sedits), lim, (long long)s->za.TW * s->nz,
                                          (long long)s->N, s->d_sdirty, s->d_slist, s->d_zhot);
     FFCZ_CUDA(cudaGetLastError());
+    if (fold_extract) {
+      FFCZ_TRY(enqueue_extract<T>(s, st));
+      FFCZ_CUDA(cudaMemcpyAsync(s->h_ctl, s->d_ctl, sizeof(LoopCtl), cudaMemcpyDeviceToHost, st));
+    }
     double h[2 * kZsScan];
     unsigned hc[3];
     FFCZ_CUDA(cudaMemcpyAsync(h, partial, sizeof(h), cudaMemcpyDeviceToHost, st));
@@ -1470,6 +1478,7 @@ int certify(ffcz_solver *s, bool clamp, T eps_t, bool use_recorded, double *smax
     }
     if (!hc[2] && q >= 0.0) {
       stats = true;
+      if (folded) *folded = fold_extract;
       pre = post = q;  // the clamp only shrinks values: pre bounds post
       const double cnt = (double)hc[1];
       *smax = cnt > 0.0 ? (double)lim : amax;
@@ -1558,8 +1567,13 @@ int strict_finish(ffcz_solver *s, int max_iter, double tol, int max_rounds, int 
   // converged on a frequency projection (no final spatial clamp since);
   // the float-float passes record an upper bound of their values too
   const bool recorded = s->h_ctl->converged && s->h_ctl->iterations >= 1;
-  FFCZ_TRY(certify<T>(s, true, Et, recorded, &cs, &cf, &cb, &cok, &how));
-  s->extracted = false;
+  // a compaction the caller will want (eager mode, or one left pending)
+  // runs with the clamp, ahead of the certificate's synchronisation
+  bool folded = false;
+  FFCZ_TRY(certify<T>(s, true, Et, recorded, &cs, &cf, &cb, &cok, &how, was_extracted || s->extract_pending,
+                      &folded));
+  if (folded && cok) FFCZ_TRY(finish_extract(s));
+  else s->extracted = false;
   s->cert_ok = cok;
   s->cert_how = how;
   s->cert_smax = cs;
@@ -1588,11 +1602,18 @@ int strict_finish(ffcz_solver *s, int max_iter, double tol, int max_rounds, int 
   }
   s->delta = D;
   if (rc != FFCZ_OK) return rc;
-  k_set_iterations<<<1, 1, 0, st>>>(s->d_ctl, total);
-  FFCZ_CUDA(cudaGetLastError());
+  if (r > 0) {
+    k_set_iterations<<<1, 1, 0, st>>>(s->d_ctl, total);
+    FFCZ_CUDA(cudaGetLastError());
+  }
   s->h_ctl->iterations = total;
-  if (was_extracted) FFCZ_TRY(extract<T>(s));
-  else FFCZ_CUDA(cudaStreamSynchronize(st));
+  if (s->extracted) {
+    // compacted with the clamp: nothing changed since
+  } else if (was_extracted) {
+    FFCZ_TRY(extract<T>(s));
+  } else {
+    FFCZ_CUDA(cudaStreamSynchronize(st));
+  }
   if (rounds) *rounds = r;
   if (met) *met = (sm <= E && fm <= D) ? 1 : 0;
   if (smax) *smax = sm;
