@@ -627,6 +627,46 @@ __global__ void __launch_bounds__(EX_LIST_THREADS) k_ex_listed(const T *__restri
     return;
   }
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if ((long long)cnt < n) {
+    // with no listed value active (the strict finish's rounding-size
+    // clamps) the results need no order and no deduplication: count 0, min
+    // and max over the listed values and the zeros of the unlisted entries
+    bool act = false;
+    T mn0 = T(0), mx0 = T(0);
+    for (unsigned i = tid; i < cnt; i += EX_LIST_THREADS) {
+      const T v = a[slist[4 + i]];
+      act |= fabs(v) > thr;
+      mn0 = fmin(mn0, v);
+      mx0 = fmax(mx0, v);
+    }
+    if (!__syncthreads_or(act)) {
+      unsigned long long kmn = ord_key<T>(mn0), kmx = ord_key<T>(mx0);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long p = __shfl_xor_sync(0xffffffffu, kmn, o), q = __shfl_xor_sync(0xffffffffu, kmx, o);
+        kmn = p < kmn ? p : kmn;
+        kmx = q > kmx ? q : kmx;
+      }
+      if (lane == 0) {
+        wmn[warp] = kmn;
+        wmx[warp] = kmx;
+      }
+      __syncthreads();
+      if (tid == 0) {
+        for (int w = 1; w < EX_LIST_THREADS / 32; ++w) {
+          kmn = wmn[w] < kmn ? wmn[w] : kmn;
+          kmx = wmx[w] > kmx ? wmx[w] : kmx;
+        }
+        const T gmn = key_val<T>(kmn), gmx = key_val<T>(kmx);
+        mnmx[0] = gmn;
+        mnmx[1] = gmx;
+        ctl->count[which] = 0ull;
+        ctl->mn[which] = (double)gmn;
+        ctl->mx[which] = (double)gmx;
+      }
+      return;
+    }
+  }
   int P = 1;
   while (P < (int)cnt) P <<= 1;
   for (int i = tid; i < P; i += EX_LIST_THREADS) key[i] = i < (int)cnt ? slist[4 + i] : 0xffffffffu;

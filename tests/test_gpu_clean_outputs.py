@@ -70,6 +70,27 @@ def test_untouched_listed_written_sequence(cuda, dtype):
         assert check(s) == (0, 0)
 
 
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_listed_values_below_threshold(cuda, dtype):
+    # the strict clamp moves a few values by less than the 1e-7 threshold:
+    # listed but inactive (count 0, min and max from the small edits)
+    rng = np.random.default_rng(10)
+    e0 = e0_of(11, 0.9, dtype)
+    idx = rng.choice(e0.size, 50, replace=False)
+    e0[idx] = (np.where(rng.random(50) < 0.5, -1.0, 1.0) * (EPS + 5e-8)).astype(dtype)
+    with F.ProjectionSolver(*SHAPE, dtype=dtype) as s:
+        step(s, e0)
+        se = s.get_spatial_edits_full()
+        assert 0 < np.count_nonzero(se) <= 50 and np.abs(se).max() <= 1e-7
+        assert check(s)[1] == 0
+        mm = s.minmax()
+        assert mm[2] < 0.0 < mm[3]
+        step(s, e0_of(12, 1.3, dtype))  # then active listed values
+        assert check(s)[1] > 0
+        step(s, e0)
+        assert check(s)[1] == 0
+
+
 def test_pack_mode_switch_and_decode(cuda):
     dtype = np.float32
     with F.ProjectionSolver(*SHAPE, dtype=dtype) as s:
