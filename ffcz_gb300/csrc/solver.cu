@@ -1288,9 +1288,8 @@ __global__ void __launch_bounds__(256) k_zstat_clamp(T *__restrict__ e, T *__res
     const long long lo = (long long)hot[3 + h] * span, hi = min(lo + span, n);
     for (long long i = lo + threadIdx.x; i < hi; i += blockDim.x) {
       const T v0 = e[i];
-      const T v = spatial_clamp(v0, lim, sedits, i);
-      if (v != v0) {
-        e[i] = v;
+      if (v0 > lim || v0 < -lim) {
+        e[i] = spatial_clamp(v0, lim, sedits, i);
         ex_list_record(sdirty, slist, i);
         ++c;
       }
