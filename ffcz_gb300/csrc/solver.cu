@@ -1461,6 +1461,7 @@ int certify(ffcz_solver *s, bool clamp, T eps_t, bool use_recorded, double *smax
     k_zstat_clamp<T><<<gc, 256, 0, st>>>(tp<T>(s->d_e), tp<T>(s->d_sedits), lim, (long long)s->za.TW * s->nz,
                                          (long long)s->N, s->d_sdirty, s->d_slist, s->d_zhot);
     FFCZ_CUDA(cudaGetLastError());
+    s->launches += 2;
     if (fold_extract) {
       FFCZ_TRY(enqueue_extract<T>(s, st));
       FFCZ_CUDA(cudaMemcpyAsync(s->h_ctl, s->d_ctl, sizeof(LoopCtl), cudaMemcpyDeviceToHost, st));
@@ -1490,6 +1491,7 @@ int certify(ffcz_solver *s, bool clamp, T eps_t, bool use_recorded, double *smax
     k_clamp_stats<T><<<g, 256, 0, st>>>(tp<T>(s->d_e), tp<T>(s->d_sedits), lim, (long long)s->N, s->d_sdirty,
                                         s->d_slist, partial, mx);
     FFCZ_CUDA(cudaGetLastError());
+    s->launches += 1;
     std::vector<double> h(3 * g + 1);
     FFCZ_CUDA(cudaMemcpyAsync(h.data(), partial, 3 * g * sizeof(double), cudaMemcpyDeviceToHost, st));
     FFCZ_CUDA(cudaMemcpyAsync(h.data() + 3 * g, mx, sizeof(double), cudaMemcpyDeviceToHost, st));
@@ -1530,6 +1532,7 @@ int certify(ffcz_solver *s, bool clamp, T eps_t, bool use_recorded, double *smax
   const unsigned g2 = (unsigned)std::min<size_t>(ceil_div(s->H, 256), 152 * 16);
   k_spec_absmax_t<T><<<g2, 256, 0, st>>>((const c2<T> *)s->d_spec, (long long)s->rows, s->Hz, s->Hzp, mx + 1);
   FFCZ_CUDA(cudaGetLastError());
+  s->launches += 2 + s->has_y + s->has_x;  // the forward transform and the maximum
   unsigned long long bits = 0;
   FFCZ_CUDA(cudaMemcpyAsync(&bits, mx + 1, sizeof(bits), cudaMemcpyDeviceToHost, st));
   FFCZ_CUDA(cudaStreamSynchronize(st));
@@ -1586,6 +1589,7 @@ int strict_finish(ffcz_solver *s, int max_iter, double tol, int max_rounds, int 
     k_final_clamp<T><<<g, 256, 0, st>>>(tp<T>(s->d_e), tp<T>(s->d_sedits), Et, (long long)s->N, nullptr,
                                         s->d_sdirty);
     FFCZ_CUDA(cudaGetLastError());
+    s->launches += 1;
     s->extracted = false;
     s->zstat_ok = false;
     if ((rc = ffcz_verify_bounds(s, &sm, &fm)) != FFCZ_OK) break;
@@ -1593,7 +1597,9 @@ int strict_finish(ffcz_solver *s, int max_iter, double tol, int max_rounds, int 
     dt -= 2.0 * (fm - D);  // twice the worst overshoot of the last check
     if (!(dt > 0.0)) break;
     s->delta = dt;
+    const long long before = s->launches;  // project() counts its own loop afresh
     rc = project<T>(s, PRO_PLAIN, s->d_e, nullptr, max_iter, tol);
+    s->launches += before;
     s->delta = D;
     if (rc != FFCZ_OK) break;
     total += s->h_ctl->iterations;
@@ -1604,6 +1610,7 @@ int strict_finish(ffcz_solver *s, int max_iter, double tol, int max_rounds, int 
   if (r > 0) {
     k_set_iterations<<<1, 1, 0, st>>>(s->d_ctl, total);
     FFCZ_CUDA(cudaGetLastError());
+    s->launches += 1;
   }
   s->h_ctl->iterations = total;
   if (s->extracted) {
@@ -2288,6 +2295,7 @@ int ffcz_verify_bounds(ffcz_solver *s, double *spatial_max, double *freq_max) {
   FFCZ_TRY(forward_spectrum<double>(v, false));
   const unsigned g2 = (unsigned)std::min<size_t>(ceil_div(s->H, 256), 152 * 16);
   k_spec_absmax<<<g2, 256, 0, st>>>((const double2 *)v->d_spec, (long long)v->rows, v->Hz, v->Hzp, s->d_vmax + 1);
+  s->launches += 3 + v->has_y + v->has_x;  // widen, the FP64 forward transform, the maximum
   unsigned long long h[2] = {0, 0};
   FFCZ_CUDA(cudaMemcpyAsync(h, s->d_vmax, sizeof(h), cudaMemcpyDeviceToHost, st));
   FFCZ_CUDA(cudaStreamSynchronize(st));

@@ -345,7 +345,8 @@ int ffcz_get_orig_spectrum(ffcz_solver *s, void *h_dst, size_t cap_complex);
 /* Sizes: n = Nx*Ny*Nz, h = Nx*Ny*(Nz/2+1). */
 int ffcz_get_sizes(ffcz_solver *s, size_t *n, size_t *h);
 /* Kernel launches issued since the last solve started (projection loop,
- * compaction and any encode of its streams). */
+ * compaction, strict finish and FP64 checks, and any encode of its
+ * streams). */
 int ffcz_get_launch_count(ffcz_solver *s, long long *launches);
 /* Per-pass timing: when on, CUDA events are recorded around each pass of
  * the first iteration of every solve (inside the captured graph).
